@@ -1,0 +1,386 @@
+/*
+ * gammaray.h — C ABI of the GB300 rendering hot path.
+ *
+ * Two shared libraries export exactly this ABI:
+ *   - libgammaray_gpu.so  (gammaray_gb300/): the product, hand-written sm_103a CUDA.
+ *   - libgammaray_ref.so  (oracle/): a CPU restatement of the Rust reference, used only
+ *                          by the tests and the benchmark's CPU baseline.
+ *
+ * The reference (sdao/gammaray, Rust) has no FFI of its own.  Each entry point below
+ * replaces one call of the reference's Rust API; the replaced item is cited as
+ * path:line inside the reference project.
+ *
+ * Conventions
+ *   - All buffers are caller-owned host memory unless the name ends in `_dev`.
+ *   - Handles (gr_scene, gr_film, gr_server) are opaque and owned by the library.
+ *   - Every call returns a gr_status; on failure gr_last_error() returns a
+ *     thread-local message.  No exception or panic crosses the ABI.
+ *   - Vectors are float[3] in the reference's world space (right-handed, the camera
+ *     looks down -Z in its own frame, core/camera.rs:87-97).
+ *   - A handle may be used by one host thread at a time; distinct handles are
+ *     independent.
+ */
+#ifndef GAMMARAY_H
+#define GAMMARAY_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GR_ABI_VERSION 1
+
+typedef enum gr_status {
+    GR_OK = 0,
+    GR_ERR_INVALID_ARGUMENT = 1,
+    GR_ERR_OUT_OF_MEMORY = 2,
+    GR_ERR_CUDA = 3,
+    GR_ERR_UNSUPPORTED = 4,
+    GR_ERR_TIMEOUT = 5,
+    /* Traversal stack overflow.  The reference panics here (geom/bvh.rs:156-157). */
+    GR_ERR_STACK_OVERFLOW = 6,
+    GR_ERR_NOT_FOUND = 7,
+    GR_ERR_BUSY = 8,
+    GR_ERR_CANCELLED = 9,
+    GR_ERR_INTERNAL = 10
+} gr_status;
+
+/* Thread-local text of the last failure on this thread ("" if none). */
+const char* gr_last_error(void);
+int gr_abi_version(void);
+/* "cuda-sm_103a" for the GPU library, "oracle-cpu" for the restatement. */
+const char* gr_backend_name(void);
+
+/* ------------------------------------------------------------------ materials */
+
+/* Mirrors Material::{disney().build(), diffuse_light, diffuse, mirror}
+ * (material/material.rs:27-59, 292-333). */
+typedef enum gr_material_kind {
+    GR_MATERIAL_DISNEY = 0,
+    GR_MATERIAL_DIFFUSE_LIGHT = 1,
+    GR_MATERIAL_DIFFUSE = 2, /* PerfectDiffuse lobe, material/lobes.rs:401-414 */
+    GR_MATERIAL_MIRROR = 3   /* PerfectMirror lobe, material/lobes.rs:422-457 */
+} gr_material_kind;
+
+/* DisneyMaterialBuilder fields (material/material.rs:256-268).  There is no
+ * `specular` parameter in the reference: F0 follows from `ior` (1.5 gives 0.04). */
+typedef struct gr_material_desc {
+    int32_t kind;
+    float base_color[3];
+    float roughness;
+    float anisotropic;
+    float ior;
+    float metallic;
+    float specular_trans;
+    float specular_tint;
+    float sheen;
+    float sheen_tint;
+    float clearcoat;
+    float clearcoat_gloss;
+    /* Radiance of GR_MATERIAL_DIFFUSE_LIGHT (DiffuseAreaLight, material/lights.rs:11-22). */
+    float incandescence[3];
+} gr_material_desc;
+
+/* Fills the builder defaults of DisneyMaterialBuilder::new (material/material.rs:276-290). */
+void gr_material_disney_defaults(gr_material_desc* out);
+
+/* ---------------------------------------------------------------------- prims */
+
+typedef enum gr_prim_kind { GR_PRIM_MESH = 0, GR_PRIM_SPHERE = 1 } gr_prim_kind;
+
+#define GR_NO_INDEX 0xFFFFFFFFu
+
+/* One reference Prim (geom/prim.rs:7-52): a triangle Mesh (geom/mesh.rs:50-58) or a
+ * Sphere (geom/sphere.rs:9-24).  Mesh data is already in world space, i.e. after the
+ * Xform that Mesh::from_obj applies (geom/mesh.rs:97-122).
+ *   tri_vertices : 3 indices per triangle (Tri::a,b,c).
+ *   tri_normals  : 3 per triangle or NULL; GR_NO_INDEX as the first index of a
+ *                  triangle selects the geometric normal (the usize::MAX sentinel,
+ *                  geom/mesh.rs:148-153).
+ *   tri_uvs      : 3 per triangle or NULL (NULL = all-zero uvs, geom/mesh.rs:133-136). */
+typedef struct gr_prim_desc {
+    int32_t kind;
+    uint32_t material;
+    const float* vertices;
+    uint32_t num_vertices;
+    const uint32_t* tri_vertices;
+    uint32_t num_tris;
+    const float* normals;
+    uint32_t num_normals;
+    const uint32_t* tri_normals;
+    const float* uvs; /* 2 floats (u, v) per uv */
+    uint32_t num_uvs;
+    const uint32_t* tri_uvs;
+    float center[3]; /* sphere */
+    float radius;    /* sphere */
+} gr_prim_desc;
+
+/* ---------------------------------------------------------------------- scene */
+
+typedef struct gr_scene_desc {
+    const gr_material_desc* materials;
+    uint32_t num_materials;
+    const gr_prim_desc* prims;
+    uint32_t num_prims;
+    /* Constant environment radiance seen by rays that leave the scene.  The reference
+     * has none (black, render/integrators.rs:90-92); {0,0,0} reproduces it. */
+    float environment[3];
+    /* Device BVH width (2, 4 or 8) and maximum primitives per wide leaf; 0 = default.
+     * The CPU restatement ignores both (it keeps the reference's binary BVH). */
+    uint32_t bvh_width;
+    uint32_t leaf_size;
+} gr_scene_desc;
+
+typedef struct gr_scene gr_scene;
+
+typedef struct gr_scene_info {
+    uint64_t num_components;   /* triangles + spheres */
+    uint64_t num_binary_nodes; /* reference SAH tree (geom/bvh.rs:310-337) */
+    uint64_t num_wide_nodes;   /* device layout; 0 for the CPU restatement */
+    uint64_t device_bytes;     /* resident bytes of the scene on the device */
+    uint32_t num_lights;
+    uint32_t bvh_width;
+    double build_seconds;
+} gr_scene_info;
+
+/* Replaces Stage::new / Bvh::build (render/stage.rs:15-20, geom/bvh.rs:339-382):
+ * copies the prims, runs the reference SAH build on the host and (GPU library)
+ * uploads a wide BVH.  The descriptors may be freed when this returns. */
+gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out);
+gr_status gr_scene_destroy(gr_scene* scene);
+gr_status gr_scene_get_info(const gr_scene* scene, gr_scene_info* out);
+
+/* --------------------------------------------------------------------- camera */
+
+/* Camera::new(focal_length, h_ap, v_ap, f_stop, &rotate, &translate)
+ * (core/camera.rs:42-61).  rotate = {real, i, j, k}. */
+typedef struct gr_camera {
+    float focal_length;
+    float horizontal_aperture;
+    float vertical_aperture;
+    float f_stop;
+    float rotate[4];
+    float translate[3];
+} gr_camera;
+
+/* ----------------------------------------------------------------------- film */
+
+typedef struct gr_film gr_film;
+
+/* Film::new(width, height) (render/film.rs:45-53): accum and weight start at zero. */
+gr_status gr_film_create(uint32_t width, uint32_t height, gr_film** out);
+gr_status gr_film_destroy(gr_film* film);
+gr_status gr_film_clear(gr_film* film);
+/* Copies Film::pixels out: accum as 3 floats and weight as 1 float per pixel,
+ * row-major, row 0 first (render/film.rs:26-36). */
+gr_status gr_film_read(const gr_film* film, float* accum, float* weight);
+/* accum / weight per pixel (render/exr.rs:154-156), 3 floats per pixel. */
+gr_status gr_film_resolve(const gr_film* film, float* rgb);
+/* Uncompressed scanline EXR with B, G, R float channels, rows flipped, as
+ * ExrWriter::update + write (render/exr.rs:168-199). */
+gr_status gr_film_write_exr(const gr_film* film, const char* path);
+/* Number of passes accumulated so far. */
+gr_status gr_film_passes(const gr_film* film, uint32_t* passes);
+
+/* --------------------------------------------------------------------- render */
+
+typedef enum gr_integrator_kind {
+    GR_INTEGRATOR_PATH_TRACER = 0,  /* render/integrators.rs:39-100 */
+    GR_INTEGRATOR_BDPT = 1,         /* render/integrators.rs:102-418 */
+    GR_INTEGRATOR_DISPLAY_COLOR = 2 /* render/integrators.rs:18-34 */
+} gr_integrator_kind;
+
+/* Per-render settings.  gr_render_params_default gives "reference mode": the
+ * compile-time constants of render/integrators.rs:36-37 and 102-103. */
+typedef struct gr_render_params {
+    int32_t integrator;
+    /* Number of 1-spp passes; one pass is one Stage::trace call (render/stage.rs:23-36). */
+    uint32_t spp;
+    /* Path tracer: maximum number of path segments, 0 = unlimited (reference).
+     * BDPT: maximum vertices per walk and per connected path (BDPT_MAX_DEPTH = 16). */
+    uint32_t max_depth;
+    /* Path tracer: roulette when depth > rr_depth (10).  BDPT: when walk length >= rr_depth (4). */
+    uint32_t rr_depth;
+    /* Path tracer: aggressive roulette when depth > rr_aggressive_depth (20). */
+    uint32_t rr_aggressive_depth;
+    /* BDPT strategy weights: 0 = uniform 1/(c+l) (reference, integrators.rs:345-354),
+     * 1 = power heuristic over the stored forward/reverse densities (extension). */
+    uint32_t mis;
+    /* BDPT: 1 adds light-tracing (t=1) connections splatted onto the film (extension). */
+    uint32_t light_tracing;
+    uint32_t first_pass; /* pass index of the first pass (selects the random streams) */
+    uint64_t seed;
+} gr_render_params;
+
+void gr_render_params_default(int32_t integrator, gr_render_params* out);
+
+/* Replaces `for _ in 0..spp { stage.trace(&camera, &integrator, &mut film) }`
+ * (render/stage.rs:23-36).  Each pass jitters one sample per pixel, integrates it and
+ * splats it with the Mitchell filter (render/film.rs:55-114), in pass order. */
+gr_status gr_render(gr_scene* scene, const gr_camera* camera,
+                    const gr_render_params* params, gr_film* film);
+
+/* One pass without the film: per pixel, the FilmSample {s, t, color} that
+ * Stage::trace computes before Film::report_samples (render/stage.rs:28-34).
+ * samples: 5 floats (s, t, r, g, b) per pixel.  params->spp is ignored. */
+gr_status gr_render_samples(gr_scene* scene, const gr_camera* camera,
+                            const gr_render_params* params, uint32_t width,
+                            uint32_t height, float* samples);
+
+/* Counters of the last gr_render on this scene (GPU library; zeros otherwise). */
+typedef struct gr_render_stats {
+    uint64_t samples;         /* camera paths completed */
+    uint64_t extension_rays;  /* closest-hit rays traced */
+    uint64_t shadow_rays;     /* visibility rays traced */
+    uint64_t kernel_launches;
+    double device_ms;         /* CUDA-event time of the render */
+} gr_render_stats;
+gr_status gr_scene_last_stats(const gr_scene* scene, gr_render_stats* out);
+
+/* ---------------------------------------------------------------- ray queries */
+
+/* Closest hit.  prim = -1 for a miss (Intersection::NoHit).  component is the
+ * triangle index within the mesh (0 for spheres); u, v are the Moller-Trumbore
+ * barycentrics (0 for spheres). */
+typedef struct gr_hit {
+    float t;
+    int32_t prim;
+    int32_t component;
+    float u;
+    float v;
+} gr_hit;
+
+/* Bvh::intersect (geom/bvh.rs:406-456) for n rays given as 6 floats (origin,
+ * direction) each. */
+gr_status gr_trace_rays(gr_scene* scene, const float* rays, uint64_t n, gr_hit* hits);
+/* Same on device-resident buffers, asynchronous on `stream` (a cudaStream_t, or 0). */
+gr_status gr_trace_rays_dev(gr_scene* scene, const float* rays_dev, uint64_t n,
+                            gr_hit* hits_dev, void* stream);
+/* Bvh::intersect_naive (geom/bvh.rs:385-400): every component, no BVH. */
+gr_status gr_intersect_naive(gr_scene* scene, const float* rays, uint64_t n, gr_hit* hits);
+/* Bvh::visibility (geom/bvh.rs:460-477) for n (start, target) point pairs,
+ * 6 floats each.  visible[i] = 1 if unoccluded. */
+gr_status gr_visibility(gr_scene* scene, const float* pairs, uint64_t n, uint8_t* visible);
+
+/* Light sampling: Bvh::sample_light (geom/bvh.rs:481-496) with the uniforms given
+ * explicitly, 6 per sample (light pick, component pick, two area uniforms, two
+ * direction uniforms). */
+typedef struct gr_light_sample {
+    float origin[3];
+    float direction[3];
+    float normal[3];
+    float tangent[3];
+    float binormal[3];
+    float geom_normal[3];
+    int32_t prim;
+    float point_pdf;
+    float dir_pdf;
+} gr_light_sample;
+gr_status gr_sample_light(gr_scene* scene, const float* u, uint64_t n, gr_light_sample* out);
+
+/* -------------------------------------------------------------- BSDF queries */
+
+/* SurfaceProperties (geom/prim.rs:57-79). */
+typedef struct gr_frame {
+    float normal[3];
+    float tangent[3];
+    float binormal[3];
+    float geom_normal[3];
+} gr_frame;
+
+/* MaterialSample (material/material.rs:12-18). */
+typedef struct gr_bsdf_sample {
+    float emission[3];
+    float radiance[3];
+    float outgoing[3];
+    float pdf;
+    uint32_t kind; /* LobeKind bits (material/lobes.rs:25-40) */
+} gr_bsdf_sample;
+
+/* Material::f_world (material/material.rs:66-93); f: 3 floats per query. */
+gr_status gr_bsdf_eval(const gr_material_desc* material, uint64_t n, const gr_frame* frames,
+                       const float* incoming, const float* outgoing, int32_t camera_to_light,
+                       float* f);
+/* Material::pdf_world (material/material.rs:95-119). */
+gr_status gr_bsdf_pdf(const gr_material_desc* material, uint64_t n, const gr_frame* frames,
+                      const float* incoming, const float* outgoing, float* pdf);
+/* Material::sample_world (material/material.rs:140-235) with the random numbers given
+ * explicitly: u holds 3 floats per query (lobe choice, then the lobe's two uniforms). */
+gr_status gr_bsdf_sample_batch(const gr_material_desc* material, uint64_t n,
+                               const gr_frame* frames, const float* incoming, const float* u,
+                               int32_t camera_to_light, gr_bsdf_sample* out);
+/* Material::light_world (material/material.rs:123-134); L: 3 floats per query. */
+gr_status gr_light_eval(const gr_material_desc* material, uint64_t n, const gr_frame* frames,
+                        const float* incoming, float* radiance);
+
+/* ------------------------------------------------------------------- batching */
+
+/* Many independent renders in one persistent wavefront (no reference counterpart:
+ * the reference renders one image per Stage::trace call). */
+typedef struct gr_job {
+    gr_scene* scene;
+    gr_camera camera;
+    gr_render_params params;
+    gr_film* film;
+} gr_job;
+
+typedef struct gr_batch_options {
+    uint32_t path_capacity;  /* paths in flight; 0 = autotuned */
+    uint32_t block_size;     /* threads per block; 0 = autotuned */
+    uint32_t use_graph;      /* capture the bounce loop in a CUDA graph */
+    uint32_t reserved;
+} gr_batch_options;
+
+gr_status gr_render_batch(const gr_job* jobs, uint32_t n, const gr_batch_options* options);
+
+/* -------------------------------------------------------------------- serving */
+
+typedef struct gr_server gr_server;
+
+typedef struct gr_server_options {
+    uint64_t memory_budget_bytes; /* admission limit; 0 = 90% of free device memory */
+    uint32_t max_active;          /* concurrent renders; 0 = unlimited */
+    uint32_t path_capacity;       /* paths in flight per wavefront; 0 = default */
+} gr_server_options;
+
+typedef struct gr_request {
+    gr_scene* scene;
+    gr_camera camera;
+    gr_render_params params;
+    uint32_t width;
+    uint32_t height;
+} gr_request;
+
+typedef enum gr_request_state {
+    GR_REQUEST_QUEUED = 0,
+    GR_REQUEST_RUNNING = 1,
+    GR_REQUEST_DONE = 2,
+    GR_REQUEST_CANCELLED = 3,
+    GR_REQUEST_FAILED = 4
+} gr_request_state;
+
+typedef struct gr_request_status {
+    int32_t state;
+    uint32_t passes_done;
+    double submit_ms;  /* host clock, milliseconds since server creation */
+    double start_ms;
+    double finish_ms;
+} gr_request_status;
+
+gr_status gr_server_create(const gr_server_options* options, gr_server** out);
+gr_status gr_server_destroy(gr_server* server);
+gr_status gr_server_submit(gr_server* server, const gr_request* request, uint64_t* id);
+/* Runs scheduling steps until no work is left or `budget_ms` elapses. */
+gr_status gr_server_step(gr_server* server, double budget_ms);
+gr_status gr_server_poll(gr_server* server, uint64_t id, gr_request_status* out);
+gr_status gr_server_cancel(gr_server* server, uint64_t id);
+/* Copies the finished film (accum, weight) of a request and releases it. */
+gr_status gr_server_take(gr_server* server, uint64_t id, float* accum, float* weight);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GAMMARAY_H */
