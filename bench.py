@@ -1,0 +1,302 @@
+"""Benchmark: plain per-image GPU path tracing on the 102,400-triangle displaced sphere.
+
+Workload (the configuration the headline metric is quoted on): 1024 x 1024, 64 spp,
+max depth 12, FP32; a 160 x 320 UV sphere radially displaced by 3-octave value noise
+on a 20-triangle ground plane, one quad light and a constant environment of 0.2, with
+per-object Disney parameters from a seed (gammaray_gb300.scenes.displaced_sphere).
+One step = one complete render (64 passes of Stage::trace).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Output: one JSON line (rank 0).  `value` is Msamples/s from CUDA events on the render
+stream with the scene resident; `e2e` is the same metric through the C ABI with host
+buffers (scene build + upload, render, film read-back).  `--impl reference` times the
+reference's CPU algorithm (the C++ restatement under oracle/, the reference itself is
+Rust and cannot be built here) on all host threads.
+Multi-GPU: replicas only (each rank renders its own copy; no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=1024)
+    ap.add_argument("--height", type=int, default=1024)
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def hbm_peak():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, n in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(n)
+            except Exception:
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(args):
+    from gammaray_gb300 import scenes
+
+    return scenes.displaced_sphere(args.width, args.height, args.spp)
+
+
+def cpu_baseline(w, budget_s, lib=None):
+    """The oracle on all host threads over whole 1-spp passes of the same workload until
+    the budget is spent (at least one pass)."""
+    import gammaray_gb300 as g
+    from gammaray_gb300 import _abi
+
+    lib = lib or _abi.Lib(os.path.join(ROOT, "oracle", "libgammaray_ref.so"))
+    st = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1)
+    film = g.Film(w.width, w.height, lib=lib)
+    passes, t0 = 0, time.perf_counter()
+    while passes == 0 or time.perf_counter() - t0 < budget_s:
+        st.render(w.camera, w.integrator, film, 1)
+        passes += 1
+    dt = time.perf_counter() - t0
+    samples = passes * w.width * w.height
+    cores = int(os.environ.get("GR_ORACLE_THREADS", os.cpu_count() or 1))
+    return {"value": samples / dt / 1e6, "unit": "Msamples/s", "cores": cores, "kind": "port",
+            "sample": f"{passes} x 1-spp pass(es) of the {w.width}x{w.height} workload ({samples} samples, "
+                      f"{dt:.1f} s, serial film splat as the reference)"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    if not os.path.exists(os.path.join(ROOT, "oracle", "libgammaray_ref.so")):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    w = workload(args)
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_baseline(w, 0.0)
+    vals = [cpu_baseline(w, per_step) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    cb = dict(vals[0])
+    cb["value"] = v
+    ms = w.width * w.height * w.spp / (v * 1e6) * 1e3
+    line = {"impl": "reference", "metric": "Msamples/s", "value": v, "unit": "Msamples/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_of(w), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(w):
+    return {"workload": "pt_displaced_sphere_102k", "width": w.width, "height": w.height, "spp": w.spp,
+            "max_depth": w.integrator.max_depth, "triangles": w.num_triangles(), "integrator": "path_tracer",
+            "bvh": "reference SAH, collapsed to width 4", "l2": "flushed (256 MiB write) between timed steps",
+            "unit_of_step": "one complete render"}
+
+
+def run_ours(args, rank, world, local):
+    import ctypes as C
+
+    import torch
+
+    import gammaray_gb300 as g
+    from gammaray_gb300 import _abi
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    lib = g.load()
+    w = workload(args)
+    st = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1)
+    info = st.info()
+    film = g.Film(w.width, w.height, lib=lib)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    samples_per_step = w.width * w.height * w.spp
+
+    def render(flags=0, spp=None, first=None):
+        p = st.params(w.integrator, spp or w.spp, first)
+        p.flags = flags
+        cam = w.camera.desc()
+        lib.call("gr_render", st.handle, C.byref(cam), C.byref(p), film.handle)
+        return st.last_stats()
+
+    # Traversal counts per extension ray (untimed, one pass).
+    cs = render(_abi.RENDER_COUNT_TRAVERSAL, spp=1)
+    nodes_per_ray = cs.node_visits / max(1, cs.extension_rays)
+    prims_per_ray = cs.prim_tests / max(1, cs.extension_rays)
+    for _ in range(args.warmup):
+        render()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    dev_ms, ext_ms, ext_launch, rays, launches, shade_ms = [], 0.0, 0, 0, 0, 0.0
+    barrier()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            s = render(_abi.RENDER_TIME_KERNELS)
+            dev_ms.append(s.device_ms)
+            ext_ms += s.extend_ms
+            shade_ms += s.shade_ms
+            ext_launch += s.extend_launches
+            rays += s.extension_rays
+            launches += s.kernel_launches
+        barrier()
+        wall = time.perf_counter() - t0
+    total_ms = sum(dev_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps * samples_per_step / (total_ms * 1e-3) / 1e6
+    mrays = world * rays / (total_ms * 1e-3) / 1e6
+
+    # End to end through the C ABI with host buffers: scene build + upload, render, read-back.
+    e2e_ms, h2d, d2h = [], 0, 0
+    acc = np.empty((w.height, w.width, 3), np.float32)
+    wt = np.empty((w.height, w.width), np.float32)
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        st2 = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1)
+        f2 = g.Film(w.width, w.height, lib=lib)
+        st2.render(w.camera, w.integrator, f2, w.spp)
+        lib.call("gr_film_read", f2.handle, _abi.fptr(acc), _abi.fptr(wt))
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
+        h2d = st2.info().device_bytes
+        d2h = acc.nbytes + wt.nbytes
+        st2.close()
+        f2.close()
+    e2e = {"value": world * samples_per_step / (statistics.median(e2e_ms) * 1e-3) / 1e6, "unit": "Msamples/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "includes": "host SAH build + wide collapse + upload, 64-spp render, film read-back"}
+
+    # Roofline of the dominant kernel (extension / closest hit): counted bytes per ray.
+    node_bytes = 32 * info.bvh_width
+    b_ray = nodes_per_ray * node_bytes + prims_per_ray * 48 + 48
+    achieved = b_ray * rays / (ext_ms * 1e-3) / 1e9 if ext_ms > 0 else None
+    peak, peak_kind = hbm_peak()
+    roofline = {"bound": "hbm", "kernel": "k_extend (closest-hit traversal)", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "peak_source": peak_kind,
+                "bytes_per_ray": b_ray, "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
+                "extend_share_of_device_time": ext_ms / total_ms if total_ms else None,
+                "extend_ms_per_launch": ext_ms / max(1, ext_launch)}
+    ncu_traffic = os.path.join(ROOT, "profiles", "extend_traffic.json")
+    if os.path.exists(ncu_traffic):
+        try:
+            with open(ncu_traffic) as f:
+                tr = json.load(f)
+            roofline["traffic"] = tr.get("dram_bytes_per_ray", 0) * rays / max(1, ext_launch)
+            roofline["traffic_source"] = tr.get("source")
+        except Exception:
+            pass
+
+    if rank == 0:
+        cb = cpu_baseline(w, args.cpu_seconds) if world == 1 else None
+        line = {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config_of(w), "mrays_per_s": mrays, "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
+                "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s": wall,
+                "scene": {"components": int(info.num_components), "wide_nodes": int(info.num_wide_nodes),
+                          "device_bytes": int(info.device_bytes), "build_s": info.build_seconds}}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

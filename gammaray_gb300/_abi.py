@@ -128,7 +128,13 @@ class RenderParams(C.Structure):
         ("light_tracing", C.c_uint32),
         ("first_pass", C.c_uint32),
         ("seed", C.c_uint64),
+        ("flags", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
+
+
+RENDER_COUNT_TRAVERSAL = 1
+RENDER_TIME_KERNELS = 2
 
 
 class RenderStats(C.Structure):
@@ -137,7 +143,12 @@ class RenderStats(C.Structure):
         ("extension_rays", C.c_uint64),
         ("shadow_rays", C.c_uint64),
         ("kernel_launches", C.c_uint64),
+        ("node_visits", C.c_uint64),
+        ("prim_tests", C.c_uint64),
+        ("extend_launches", C.c_uint64),
         ("device_ms", C.c_double),
+        ("extend_ms", C.c_double),
+        ("shade_ms", C.c_double),
     ]
 
 

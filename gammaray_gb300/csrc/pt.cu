@@ -1,0 +1,415 @@
+// Wavefront unidirectional path tracer: PathTracerIntegrator::integrate
+// (render/integrators.rs:42-100) and DisplayColorIntegrator (integrators.rs:18-34),
+// driven as Stage::trace passes (render/stage.rs:23-36).
+//
+// State lives in "slots", one per camera path (pass-local sample index); the rays of
+// live paths travel in a compacted queue:
+//   raygen   one slot per pixel and pass: jitter (film.rs:55-76), camera ray
+//            (camera.rs:87-97), throughput 1, radiance 0
+//   extend   closest hit for every queued ray (wide BVH, shared-memory stack)
+//   shade    emission, Material::sample_world, throughput update, roulette and the
+//            next ray; surviving paths are appended to the next queue with one
+//            atomic per warp (ballot + popc)
+//   film     after the last bounce, the deterministic tile gather in film.cu
+// Extend and shade run as grid-stride loops over the device-side queue count, so the
+// host never waits for a bounce; it polls the count two bounces behind to stop.
+#include <algorithm>
+#include <cstdlib>
+#include <utility>
+#include <vector>
+
+#include "runtime.hpp"
+#include "traverse.cuh"
+
+#define GR_TRY_S(expr)                \
+    do {                              \
+        gr_status s__ = (expr);       \
+        if (s__ != GR_OK) return s__; \
+    } while (0)
+
+namespace gr {
+
+namespace {
+
+constexpr int BLOCK = 128;
+
+struct PTParams {
+    DevCamera cam;
+    uint32_t width, height, npix;
+    uint32_t first_pass;
+    uint64_t seed;
+    uint32_t max_depth, rr_depth, rr_aggr;
+};
+
+__global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4* __restrict__ tp,
+                                                  float4* __restrict__ L, unsigned long long* __restrict__ key,
+                                                  float2* __restrict__ st, uint32_t* __restrict__ q_slot,
+                                                  float4* __restrict__ q_o, float4* __restrict__ q_d) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t pass_local = i / p.npix;
+    uint32_t pixel = i - pass_local * p.npix;
+    uint32_t row = pixel / p.width;
+    uint32_t col = pixel - row * p.width;
+    uint64_t k = path_key(p.seed, p.first_pass + pass_local, pixel);
+    float s, t;
+    film_sample_point(p.width, p.height, row, col, k, s, t);
+    V3 o, d;
+    camera_ray(p.cam, s, t, o, d);
+    tp[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    key[i] = k;
+    st[i] = make_float2(s, t);
+    q_slot[i] = i;
+    q_o[i] = make_float4(o.x, o.y, o.z, 0.0f);
+    q_d[i] = make_float4(d.x, d.y, d.z, 0.0f);
+}
+
+template <int W, bool COUNT>
+__global__ void __launch_bounds__(BLOCK) k_extend(DeviceScene s, const uint32_t* __restrict__ count,
+                                                  const float4* __restrict__ q_o, const float4* __restrict__ q_d,
+                                                  float4* __restrict__ q_hit, int* err,
+                                                  unsigned long long* rays) {
+    extern __shared__ unsigned char smem[];
+    int32_t* sref = reinterpret_cast<int32_t*>(smem);
+    float* stt = reinterpret_cast<float*>(smem + sizeof(int32_t) * s.stack_depth * blockDim.x);
+    const uint32_t n = *count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
+    uint32_t counts[2] = {0, 0};
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        float4 o4 = q_o[q], d4 = q_d[q];
+        TraceResult r = trace_ray<W, false, COUNT>(s, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX,
+                                                   sref + threadIdx.x, stt + threadIdx.x, blockDim.x, err, counts);
+        q_hit[q] = make_float4(r.t, __int_as_float(r.k), r.u, r.v);
+    }
+    if (COUNT && (counts[0] | counts[1])) {
+        atomicAdd(rays + (CNT_NODES - CNT_RAYS) / 2, static_cast<unsigned long long>(counts[0]));
+        atomicAdd(rays + (CNT_PRIMS - CNT_RAYS) / 2, static_cast<unsigned long long>(counts[1]));
+    }
+}
+
+GR_D void push_warp(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t* __restrict__ nslot,
+                    float4* __restrict__ no, float4* __restrict__ nd) {
+    const unsigned lane = threadIdx.x & 31;
+    unsigned m = __ballot_sync(0xffffffffu, alive);
+    if (!m) return;
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == static_cast<unsigned>(leader)) base = atomicAdd(count_out, static_cast<uint32_t>(__popc(m)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (alive) {
+        uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
+        nslot[pos] = slot;
+        no[pos] = make_float4(o.x, o.y, o.z, 0.0f);
+        nd[pos] = make_float4(d.x, d.y, d.z, 0.0f);
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_shade(DeviceScene s, PTParams p, uint32_t depth,
+                                                 const uint32_t* __restrict__ count_in,
+                                                 const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
+                                                 const float4* __restrict__ q_d, const float4* __restrict__ q_hit,
+                                                 float4* __restrict__ tp_buf, float4* __restrict__ L_buf,
+                                                 const unsigned long long* __restrict__ key_buf, uint32_t* count_out,
+                                                 uint32_t* __restrict__ nslot, float4* __restrict__ no,
+                                                 float4* __restrict__ nd) {
+    const uint32_t n = *count_in;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // Warp-uniform trip count so every lane reaches the ballot in push_warp.
+    for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
+        uint32_t q = b + (threadIdx.x & 31u);
+        bool alive = false;
+        uint32_t slot = 0;
+        V3 new_o = v3zero(), new_d = v3zero();
+        if (q < n) {
+            slot = q_slot[q];
+            float4 h = q_hit[q];
+            float4 o4 = q_o[q], d4 = q_d[q];
+            V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
+            float4 tp4 = tp_buf[slot], L4 = L_buf[slot];
+            V3 tp = V3{tp4.x, tp4.y, tp4.z}, L = V3{L4.x, L4.y, L4.z};
+            int32_t k = __float_as_int(h.y);
+            if (k < 0) {
+                if (s.has_env) L = L + mul(tp, V3{s.env[0], s.env[1], s.env[2]});
+            } else {
+                uint32_t prim;
+                Frame f = hit_frame(s, k, o, d, h.x, h.z, h.w, prim);
+                const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
+                uint64_t key = key_buf[slot];
+                uint32_t base = DIM_CAMERA_WALK + 4 * depth;
+                MaterialSample ms = sample_world(m, -d, f, true, uniform01(key, base), uniform01(key, base + 1),
+                                                 uniform01(key, base + 2));
+                L = L + mul(tp, ms.emission);
+                tp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
+                new_o = nudge(o + (d * h.x), ms.outgoing);
+                new_d = ms.outgoing;
+                if (depth > p.rr_depth || nearly_zero(tp)) {
+                    float rv = uniform01(key, base + 3);
+                    float lum = luminance(tp);
+                    float prob = depth > p.rr_aggr ? clamped_lerp(0.10f, 0.75f, lum) : clamped_lerp(0.25f, 1.00f, lum);
+                    tp = rv < prob ? tp / prob : v3zero();
+                }
+                alive = !is_zero(tp) && (p.max_depth == 0 || depth + 1 < p.max_depth);
+                if (alive) tp_buf[slot] = make_float4(tp.x, tp.y, tp.z, 0.0f);
+            }
+            L_buf[slot] = make_float4(L.x, L.y, L.z, 0.0f);
+        }
+        push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_shade_display(DeviceScene s, const uint32_t* __restrict__ count_in,
+                                                         const uint32_t* __restrict__ q_slot,
+                                                         const float4* __restrict__ q_hit, float4* __restrict__ L_buf) {
+    const uint32_t n = *count_in;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        float4 h = q_hit[q];
+        int32_t k = __float_as_int(h.y);
+        float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (k >= 0) {
+            uint32_t prim = __float_as_uint(__ldg(s.prims + 3 * static_cast<size_t>(k)).w);
+            const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
+            c = make_float4(m.display[0], m.display[1], m.display[2], 0.0f);
+        }
+        L_buf[q_slot[q]] = c;
+    }
+}
+
+__global__ void k_samples_out(uint32_t n, const float2* __restrict__ st, const float4* __restrict__ L, float* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float2 a = st[i];
+    float4 c = L[i];
+    out[5 * i] = a.x;
+    out[5 * i + 1] = a.y;
+    out[5 * i + 2] = c.x;
+    out[5 * i + 3] = c.y;
+    out[5 * i + 4] = c.z;
+}
+
+template <class K>
+int resident_grid(K kernel, size_t smem, uint32_t n) {
+    static int sm = device_sm_count();
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    uint32_t need = (n + BLOCK - 1) / BLOCK;
+    uint32_t cap = static_cast<uint32_t>(sm * per_sm);
+    return static_cast<int>(std::max(1u, std::min(need, cap)));
+}
+
+template <int W, bool COUNT>
+gr_status extend_launch(const DeviceScene& s, uint32_t cap_n, const uint32_t* count, const float4* qo,
+                        const float4* qd, float4* qh, int* err, unsigned long long* rays, cudaStream_t st) {
+    size_t smem = stack_smem_bytes(s.stack_depth, BLOCK);
+    static size_t configured = 0;
+    if (smem > configured) {
+        GR_CUDA_TRY(cudaFuncSetAttribute(k_extend<W, COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+        configured = smem;
+    }
+    int grid = resident_grid(k_extend<W, COUNT>, smem, cap_n);
+    k_extend<W, COUNT><<<grid, BLOCK, smem, st>>>(s, count, qo, qd, qh, err, rays);
+    return GR_OK;
+}
+
+gr_status extend_any(const DeviceScene& s, bool count_traversal, uint32_t cap_n, const uint32_t* count,
+                     const float4* qo, const float4* qd, float4* qh, int* err, unsigned long long* rays,
+                     cudaStream_t st) {
+    if (count_traversal) {
+        switch (s.width) {
+            case 2: return extend_launch<2, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
+            case 4: return extend_launch<4, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
+            default: return extend_launch<8, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
+        }
+    }
+    switch (s.width) {
+        case 2: return extend_launch<2, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
+        case 4: return extend_launch<4, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
+        default: return extend_launch<8, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
+    }
+}
+
+uint32_t paths_in_flight_target() {
+    const char* e = std::getenv("GR_PATHS_IN_FLIGHT");
+    if (e && std::atoi(e) > 0) return static_cast<uint32_t>(std::atoi(e));
+    return 1u << 21;
+}
+
+}  // namespace
+
+cudaError_t PathState::ensure(size_t n) {
+    if (n <= capacity && counters.ptr) return cudaSuccess;
+    cudaError_t e;
+#define GR_ENS(buf, bytes)                  \
+    if ((e = (buf).ensure(bytes)) != cudaSuccess) return e;
+    GR_ENS(tp, n * sizeof(float4));
+    GR_ENS(light, n * sizeof(float4));
+    GR_ENS(key, n * sizeof(unsigned long long));
+    GR_ENS(st, n * sizeof(float2));
+    for (int k = 0; k < 2; ++k) {
+        GR_ENS(q_slot[k], n * sizeof(uint32_t));
+        GR_ENS(q_o[k], n * sizeof(float4));
+        GR_ENS(q_d[k], n * sizeof(float4));
+    }
+    GR_ENS(q_hit, n * sizeof(float4));
+    GR_ENS(counters, NUM_COUNTERS * sizeof(uint32_t));
+#undef GR_ENS
+    capacity = n;
+    return cudaSuccess;
+}
+
+gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
+    const gr_render_params& rp = job.params;
+    const uint32_t npix = job.width * job.height;
+    const bool display = rp.integrator == GR_INTEGRATOR_DISPLAY_COLOR;
+    const uint32_t total = job.samples_out ? 1u : rp.spp;
+    if (total == 0) return GR_OK;
+    uint32_t group = std::max(1u, std::min(total, paths_in_flight_target() / std::max(1u, npix)));
+    if (static_cast<uint64_t>(group) * npix > 0xFFFFFFFFull / 2) group = 1;
+    PathState& ps = sc->paths;
+    GR_CUDA_TRY(ps.ensure(static_cast<size_t>(group) * npix));
+    uint32_t* cnt = ps.counters.as<uint32_t>();
+    int* err = reinterpret_cast<int*>(cnt + CNT_ERROR);
+    unsigned long long* rays = reinterpret_cast<unsigned long long*>(cnt + CNT_RAYS);
+    uint32_t* host_cnt = nullptr;
+    GR_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&host_cnt), 4 * sizeof(uint32_t), cudaHostAllocDefault));
+    struct Free {
+        uint32_t* p;
+        ~Free() { cudaFreeHost(p); }
+    } free_host{host_cnt};
+    cudaEvent_t evs[4];
+    for (auto& e : evs) GR_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    struct FreeEv {
+        cudaEvent_t* e;
+        ~FreeEv() {
+            for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
+        }
+    } free_ev{evs};
+
+    // Optional per-kernel timing: one event pair per extend / shade launch.
+    const bool timed = (rp.flags & GR_RENDER_TIME_KERNELS) != 0;
+    std::vector<cudaEvent_t> tev;
+    struct FreeTev {
+        std::vector<cudaEvent_t>& v;
+        ~FreeTev() {
+            for (cudaEvent_t e : v) cudaEventDestroy(e);
+        }
+    } free_tev{tev};
+    std::vector<std::pair<int, int>> ext_pairs, shade_pairs;
+    auto mark = [&](int& idx) -> gr_status {
+        cudaEvent_t e;
+        GR_CUDA_TRY(cudaEventCreate(&e));
+        tev.push_back(e);
+        idx = static_cast<int>(tev.size()) - 1;
+        GR_CUDA_TRY(cudaEventRecord(e, st));
+        return GR_OK;
+    };
+
+    PTParams p;
+    p.cam = job.camera;
+    p.width = job.width;
+    p.height = job.height;
+    p.npix = npix;
+    p.seed = rp.seed;
+    p.max_depth = display ? 1 : rp.max_depth;
+    p.rr_depth = rp.rr_depth;
+    p.rr_aggr = rp.rr_aggressive_depth;
+    uint64_t launches = 0;
+
+    for (uint32_t done = 0; done < total; done += group) {
+        uint32_t g = std::min(group, total - done);
+        uint32_t n = g * npix;
+        p.first_pass = rp.first_pass + done;
+        GR_CUDA_TRY(cudaMemcpyAsync(cnt + CNT_QUEUE0, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, ps.tp.as<float4>(), ps.light.as<float4>(),
+                                                            ps.key.as<unsigned long long>(), ps.st.as<float2>(),
+                                                            ps.q_slot[0].as<uint32_t>(), ps.q_o[0].as<float4>(),
+                                                            ps.q_d[0].as<float4>());
+        GR_CUDA_TRY(cudaGetLastError());
+        ++launches;
+        for (uint32_t depth = 0;; ++depth) {
+            if (p.max_depth && depth >= p.max_depth) break;
+            int cur = depth & 1, nxt = cur ^ 1;
+            int e0 = -1, e1 = -1;
+            if (timed) GR_TRY_S(mark(e0));
+            gr_status s1 = extend_any(job.scene, (rp.flags & GR_RENDER_COUNT_TRAVERSAL) != 0, n, cnt + cur, ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
+                                      ps.q_hit.as<float4>(), err, rays, st);
+            if (s1 != GR_OK) return s1;
+            GR_CUDA_TRY(cudaGetLastError());
+            ++launches;
+            if (timed) {
+                GR_TRY_S(mark(e1));
+                ext_pairs.emplace_back(e0, e1);
+            }
+            if (display) {
+                int grid = resident_grid(k_shade_display, 0, n);
+                k_shade_display<<<grid, BLOCK, 0, st>>>(job.scene, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
+                                                        ps.q_hit.as<float4>(), ps.light.as<float4>());
+                GR_CUDA_TRY(cudaGetLastError());
+                ++launches;
+                break;
+            }
+            GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
+            if (timed) GR_TRY_S(mark(e0));
+            int grid = resident_grid(k_shade, 0, n);
+            k_shade<<<grid, BLOCK, 0, st>>>(job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
+                                            ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
+                                            ps.q_hit.as<float4>(), ps.tp.as<float4>(), ps.light.as<float4>(),
+                                            ps.key.as<unsigned long long>(), cnt + nxt,
+                                            ps.q_slot[nxt].as<uint32_t>(), ps.q_o[nxt].as<float4>(),
+                                            ps.q_d[nxt].as<float4>());
+            GR_CUDA_TRY(cudaGetLastError());
+            ++launches;
+            if (timed) {
+                GR_TRY_S(mark(e1));
+                shade_pairs.emplace_back(e0, e1);
+            }
+            GR_CUDA_TRY(cudaMemcpyAsync(host_cnt + (depth & 3), cnt + nxt, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                        st));
+            GR_CUDA_TRY(cudaEventRecord(evs[depth & 3], st));
+            if (depth >= 2) {
+                GR_CUDA_TRY(cudaEventSynchronize(evs[(depth - 2) & 3]));
+                if (host_cnt[(depth - 2) & 3] == 0) break;
+            }
+        }
+        if (job.film) {
+            gr_status s2 = film_gather(ps.st.as<float2>(), ps.light.as<float4>(), job.width, job.height, g, job.film,
+                                       st);
+            if (s2 != GR_OK) return s2;
+            ++launches;
+        }
+        if (job.samples_out) {
+            k_samples_out<<<(n + 255) / 256, 256, 0, st>>>(n, ps.st.as<float2>(), ps.light.as<float4>(),
+                                                          job.samples_out);
+            GR_CUDA_TRY(cudaGetLastError());
+            ++launches;
+        }
+    }
+    sc->stats.samples += static_cast<uint64_t>(total) * npix;
+    sc->stats.kernel_launches += launches;
+    if (timed) {
+        GR_CUDA_TRY(cudaStreamSynchronize(st));
+        for (auto& pr : ext_pairs) {
+            float ms = 0.0f;
+            GR_CUDA_TRY(cudaEventElapsedTime(&ms, tev[pr.first], tev[pr.second]));
+            sc->stats.extend_ms += ms;
+        }
+        for (auto& pr : shade_pairs) {
+            float ms = 0.0f;
+            GR_CUDA_TRY(cudaEventElapsedTime(&ms, tev[pr.first], tev[pr.second]));
+            sc->stats.shade_ms += ms;
+        }
+        sc->stats.extend_launches += ext_pairs.size();
+    }
+    return GR_OK;
+}
+
+int device_sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace gr

@@ -1,0 +1,132 @@
+// Host objects behind the C ABI handles, device buffers and the launch interface
+// between the C ABI (api.cu) and the kernel files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "scene.hpp"
+#include "shading.cuh"
+
+namespace gr {
+
+void set_error(const std::string& msg);
+
+#define GR_CUDA_TRY(expr)                                                                          \
+    do {                                                                                           \
+        cudaError_t e__ = (expr);                                                                  \
+        if (e__ != cudaSuccess) {                                                                  \
+            ::gr::set_error(std::string(#expr) + ": " + cudaGetErrorString(e__));                  \
+            return e__ == cudaErrorMemoryAllocation ? GR_ERR_OUT_OF_MEMORY : GR_ERR_CUDA;          \
+        }                                                                                          \
+    } while (0)
+
+// A device allocation that frees itself.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() {}
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e == cudaSuccess) bytes = n;
+        else ptr = nullptr;
+        return e;
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(ptr);
+    }
+};
+
+// Wavefront path state, reused across renders of a scene (grown on demand).
+struct PathState {
+    DevBuf tp, light, key, st;       // per slot: throughput, radiance, random key, film (s, t)
+    DevBuf q_slot[2], q_o[2], q_d[2], q_hit;  // ping-pong queues
+    DevBuf counters;                 // [0..1] queue counts, [2] error flag, [3..] stats
+    size_t capacity = 0;
+    cudaError_t ensure(size_t n);
+};
+
+constexpr int CNT_QUEUE0 = 0;
+constexpr int CNT_QUEUE1 = 1;
+constexpr int CNT_ERROR = 2;
+constexpr int CNT_RAYS = 4;    // 64-bit counter at index 4..5
+constexpr int CNT_SHADOW = 6;  // 64-bit counter at index 6..7
+constexpr int CNT_NODES = 8;   // 64-bit: BVH nodes visited (GR_RENDER_COUNT_TRAVERSAL)
+constexpr int CNT_PRIMS = 10;  // 64-bit: primitives tested
+constexpr int NUM_COUNTERS = 16;
+
+struct SceneBuffers {
+    DevBuf nodes, prims, tri_nidx, tri_uvidx, normals, uvs, prim_material, materials, lights, light_tris,
+        light_nidx, light_uvidx, light_cdf;
+};
+
+}  // namespace gr
+
+struct gr_scene {
+    gr::HostBuild host;
+    gr::SceneBuffers buf;
+    gr::DeviceScene dev{};
+    gr::PathState paths;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    gr_render_stats stats{};
+    double build_seconds = 0.0;
+    uint64_t device_bytes = 0;
+    std::mutex mu;
+};
+
+struct gr_film {
+    uint32_t width = 0, height = 0;
+    gr::DevBuf pixels;  // float4 (accum.rgb, weight) per pixel
+    uint32_t passes = 0;
+    int device = 0;
+};
+
+namespace gr {
+
+// Kernel-side entry points (implemented in the .cu files).
+gr_status launch_trace(const DeviceScene& s, const float* rays, uint64_t n, gr_hit* hits, bool any_hit,
+                       const float* tmax, int* err, cudaStream_t st);
+gr_status launch_naive(const DeviceScene& s, const float* rays, uint64_t n, gr_hit* hits, cudaStream_t st);
+gr_status launch_visibility(const DeviceScene& s, const float* pairs, uint64_t n, uint8_t* vis, int* err,
+                            cudaStream_t st);
+gr_status launch_sample_light(const DeviceScene& s, const float* u, uint64_t n, gr_light_sample* out,
+                              cudaStream_t st);
+gr_status launch_bsdf(int op, const DevMaterial* m, uint64_t n, const gr_frame* frames, const float* wi,
+                      const float* wo, const float* u, int c2l, void* out, cudaStream_t st);
+
+struct RenderJob {
+    DeviceScene scene;
+    DevCamera camera;
+    gr_render_params params;
+    uint32_t width, height;
+    float4* film;  // accumulate target, or null (samples only)
+    float* samples_out;  // device (s, t, r, g, b) per pixel for gr_render_samples, or null
+};
+
+gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st);
+gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st);
+gr_status film_gather(const float2* st_buf, const float4* color, uint32_t width, uint32_t height, uint32_t passes,
+                      float4* film, cudaStream_t s);
+gr_status film_resolve(const float4* film, uint32_t n, float* rgb, cudaStream_t s);
+gr_status film_exr_pack(const float4* film, uint32_t width, uint32_t height, unsigned char* out, size_t data_offset,
+                        cudaStream_t s);
+
+int device_sm_count();
+
+}  // namespace gr

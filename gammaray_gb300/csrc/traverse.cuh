@@ -1,0 +1,191 @@
+// Closest-hit and shadow traversal of the wide BVH (replaces Bvh::intersect,
+// geom/bvh.rs:406-456, and Bvh::visibility, bvh.rs:460-477).
+//
+// One thread per ray.  A node is 2W float4s (W = 2, 4, 8) read with vector loads;
+// every child box is slab-tested (far distances inflated by 1 + 2 gamma(3) as in
+// core/bbox.rs:78-113), the hit children are ordered near-to-far by a sorting network
+// on (distance | slot) keys, and the farther ones go on a per-thread stack of
+// (child, entry distance) pairs kept in shared memory, column `threadIdx.x`.  Popped
+// entries whose entry distance is no longer below the closest hit are skipped.
+// Leaves hold up to 16 consecutive primitive records.  The primitive tests are the
+// reference's Moller-Trumbore (geom/mesh.rs:270-308) and sphere quadratic
+// (geom/sphere.rs:70-101) with the same operation order, so a hit distance is
+// bit-identical to the reference's for the same triangle.
+#pragma once
+
+#include "scene.hpp"
+
+namespace gr {
+
+struct TraceResult {
+    float t;
+    int32_t k;  // leaf-order primitive index, -1 = miss
+    float u, v;
+};
+
+// Reference primitive tests.  Returns the distance (0 = miss).
+GR_D float intersect_prim(const float4 p0, const float4 p1, const float4 p2, V3 o, V3 d, float& uo, float& vo) {
+    if (__float_as_int(p2.w) == PRIM_TRIANGLE) {
+        V3 c = V3{p0.x, p0.y, p0.z};
+        V3 e1 = V3{p1.x, p1.y, p1.z};
+        V3 e2 = V3{p2.x, p2.y, p2.z};
+        V3 p = cross(d, e2);
+        float det = dot(e1, p);
+        if (nearly_zero(det)) return 0.0f;
+        float inv_det = 1.0f / det;
+        V3 t = o - c;
+        float u = dot(t, p) * inv_det;
+        if (u < 0.0f || u > 1.0f) return 0.0f;
+        V3 q = cross(t, e1);
+        float v = dot(d, q) * inv_det;
+        if (v < 0.0f || (u + v) > 1.0f) return 0.0f;
+        float dist = dot(e2, q) * inv_det;
+        if (!is_positive(dist)) return 0.0f;
+        uo = u;
+        vo = v;
+        return dist;
+    }
+    V3 oc = o - V3{p0.x, p0.y, p0.z};
+    float r = p1.x;
+    float a = dot(d, d);
+    float b = dot(d, oc);
+    float c = dot(oc, oc) - (r * r);
+    float disc = (b * b) - (a * c);
+    if (disc > 0.0f) {
+        float sq = sqrtf(disc);
+        float res_pos = -b + sq;
+        float res_neg = -b - sq;
+        if (is_positive(res_neg)) return res_neg;
+        if (is_positive(res_pos)) return res_pos;
+    }
+    return 0.0f;
+}
+
+// child[slot] without dynamic register indexing (keeps the node in registers).
+template <int W>
+GR_D int32_t select_child(const float (&f)[8 * W], uint32_t slot) {
+    int32_t r = 0;
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+        if (static_cast<uint32_t>(j) == slot) r = __float_as_int(f[6 * W + j]);
+    return r;
+}
+
+template <int N>
+GR_D void sort_keys(uint32_t (&k)[N]) {
+    // Odd-even transposition network, fully unrolled (N <= 8).
+#pragma unroll
+    for (int pass = 0; pass < N; ++pass) {
+#pragma unroll
+        for (int i = pass & 1; i + 1 < N; i += 2) {
+            uint32_t a = k[i], b = k[i + 1];
+            k[i] = min(a, b);
+            k[i + 1] = max(a, b);
+        }
+    }
+}
+
+// Traces one ray.  ANY_HIT: stop at the first hit closer than t_max (shadow rays).
+// `stk_ref` / `stk_t` point at this thread's column of the shared stack (stride =
+// blockDim.x).  Sets *err = 1 if the stack bound is exceeded (cannot happen when
+// `stack_depth` comes from the build).
+// With COUNT, `counts[0]` / `counts[1]` accumulate nodes visited / primitives tested.
+template <int W, bool ANY_HIT, bool COUNT = false>
+GR_D TraceResult trace_ray(const DeviceScene& s, V3 o, V3 d, float t_max, int32_t* stk_ref, float* stk_t,
+                           int stride, int* err, uint32_t* counts = nullptr) {
+    const float inflate = 1.0f + 2.0f * gamma_n(3.0f);
+    V3 inv = V3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+    const bool nx = d.x < 0.0f, ny = d.y < 0.0f, nz = d.z < 0.0f;
+    TraceResult res{t_max, -1, 0.0f, 0.0f};
+    float closest = t_max;
+    int sp = 0;
+    int32_t ref = 0;  // root node
+    const int cap = static_cast<int>(s.stack_depth);
+    for (;;) {
+        if (ref >= 0) {
+            if (COUNT) counts[0] += 1;
+            const float4* nb = s.nodes + static_cast<size_t>(ref) * (2 * W);
+            float f[8 * W];
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) {
+                float4 x = __ldg(nb + q);
+                f[4 * q] = x.x;
+                f[4 * q + 1] = x.y;
+                f[4 * q + 2] = x.z;
+                f[4 * q + 3] = x.w;
+            }
+            uint32_t key[W];
+            int h = 0;
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+                float lx = f[0 * W + j], ly = f[1 * W + j], lz = f[2 * W + j];
+                float hx = f[3 * W + j], hy = f[4 * W + j], hz = f[5 * W + j];
+                float t0x = ((nx ? hx : lx) - o.x) * inv.x;
+                float t1x = ((nx ? lx : hx) - o.x) * inv.x;
+                float t0y = ((ny ? hy : ly) - o.y) * inv.y;
+                float t1y = ((ny ? ly : hy) - o.y) * inv.y;
+                float t0z = ((nz ? hz : lz) - o.z) * inv.z;
+                float t1z = ((nz ? lz : hz) - o.z) * inv.z;
+                float tmin = fmaxf(fmaxf(t0x, t0y), t0z);
+                float tmax = fminf(fminf(t1x, t1y), t1z) * inflate;
+                bool hit = tmin <= tmax && tmin < closest && tmax > 0.0f;
+                float te = fmaxf(tmin, 0.0f);
+                key[j] = hit ? ((__float_as_uint(te) & ~7u) | static_cast<uint32_t>(j)) : 0xFFFFFFFFu;
+                h += hit ? 1 : 0;
+            }
+            if (h > 0) {
+                sort_keys<W>(key);
+                if (sp + h - 1 > cap) {
+                    *err = 1;
+                    return TraceResult{t_max, -1, 0.0f, 0.0f};
+                }
+#pragma unroll
+                for (int j = W - 1; j >= 1; --j) {
+                    if (j < h) {
+                        stk_ref[sp * stride] = select_child<W>(f, key[j] & 7u);
+                        stk_t[sp * stride] = __uint_as_float(key[j] & ~7u);
+                        ++sp;
+                    }
+                }
+                ref = select_child<W>(f, key[0] & 7u);
+                continue;
+            }
+        } else {
+            uint32_t enc = ~static_cast<uint32_t>(ref);
+            uint32_t first = enc >> LEAF_COUNT_BITS;
+            uint32_t count = (enc & (MAX_LEAF_PRIMS - 1)) + 1;
+            if (COUNT) counts[1] += count;
+            for (uint32_t k = first; k < first + count; ++k) {
+                const float4* pr = s.prims + 3 * static_cast<size_t>(k);
+                float4 p0 = __ldg(pr), p1 = __ldg(pr + 1), p2 = __ldg(pr + 2);
+                float u, v;
+                float dist = intersect_prim(p0, p1, p2, o, d, u, v);
+                if (dist != 0.0f && dist < closest) {
+                    closest = dist;
+                    res = TraceResult{dist, static_cast<int32_t>(k), u, v};
+                    if (ANY_HIT) return res;
+                }
+            }
+        }
+        // pop
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            float te = stk_t[sp * stride];
+            if (te < closest) {
+                ref = stk_ref[sp * stride];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return res;
+}
+
+// Shared-memory stack bytes for a block of `threads` threads.
+inline size_t stack_smem_bytes(uint32_t stack_depth, int threads) {
+    return static_cast<size_t>(stack_depth) * threads * (sizeof(int32_t) + sizeof(float));
+}
+
+}  // namespace gr

@@ -212,7 +212,16 @@ typedef struct gr_render_params {
     uint32_t light_tracing;
     uint32_t first_pass; /* pass index of the first pass (selects the random streams) */
     uint64_t seed;
+    uint32_t flags;      /* GR_RENDER_* bits */
+    uint32_t reserved;
 } gr_render_params;
+
+/* Count BVH nodes visited and primitives tested by the extension rays
+ * (gr_render_stats.node_visits / prim_tests); slows the render slightly. */
+#define GR_RENDER_COUNT_TRAVERSAL 1u
+/* Time every extension (closest-hit) and shade launch with CUDA events on the render
+ * stream (gr_render_stats.extend_ms / shade_ms). */
+#define GR_RENDER_TIME_KERNELS 2u
 
 void gr_render_params_default(int32_t integrator, gr_render_params* out);
 
@@ -235,7 +244,12 @@ typedef struct gr_render_stats {
     uint64_t extension_rays;  /* closest-hit rays traced */
     uint64_t shadow_rays;     /* visibility rays traced */
     uint64_t kernel_launches;
+    uint64_t node_visits;     /* with GR_RENDER_COUNT_TRAVERSAL */
+    uint64_t prim_tests;      /* with GR_RENDER_COUNT_TRAVERSAL */
+    uint64_t extend_launches; /* with GR_RENDER_TIME_KERNELS */
     double device_ms;         /* CUDA-event time of the render */
+    double extend_ms;         /* with GR_RENDER_TIME_KERNELS: sum over extension launches */
+    double shade_ms;          /* with GR_RENDER_TIME_KERNELS: sum over shade launches */
 } gr_render_stats;
 gr_status gr_scene_last_stats(const gr_scene* scene, gr_render_stats* out);
 

@@ -1,0 +1,225 @@
+"""CUDA library vs the CPU oracle on identical inputs (both through the C ABI).
+
+Tolerances (from the parity contract):
+  closest-hit (prim, component) bit-exact, except near-ties: a differing id is accepted
+  only if the two hit distances agree within 1e-6 relative;
+  hit distance within 1e-5 relative;
+  BSDF value and pdf within 1e-5 relative (absolute floor 1e-6 for values near 0);
+  images: per-path radiance agrees for >= 99% of paths, and the image relMSE between the
+  two backends is far below the Monte Carlo noise.
+"""
+from __future__ import annotations
+
+import zlib
+
+import numpy as np
+import pytest
+
+import gammaray_gb300 as g
+from gammaray_gb300 import _abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+RTOL_T = 1e-5
+TIE_RTOL = 1e-6
+RTOL_BSDF = 1e-5
+ATOL_BSDF = 1e-6
+
+
+def random_rays(n, seed, lo=-3.0, hi=3.0, target=None):
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    if target is None:
+        d = rng.normal(size=(n, 3))
+    else:  # aim near the object so most rays hit
+        d = rng.normal(size=(n, 3)) * 0.6 + (np.asarray(target) - o)
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    return np.concatenate([o, d], axis=1).astype(np.float32)
+
+
+def check_hits(hg, ho):
+    hit_g, hit_o = hg["prim"] >= 0, ho["prim"] >= 0
+    same = (hg["prim"] == ho["prim"]) & (hg["component"] == ho["component"])
+    both = hit_g & hit_o
+    tie = both & ~same & (np.abs(hg["t"] - ho["t"]) <= TIE_RTOL * np.abs(ho["t"]))
+    bad_id = both & ~same & ~tie
+    bad_flag = hit_g != hit_o
+    assert bad_flag.sum() == 0, f"{bad_flag.sum()} rays hit on one backend only"
+    assert bad_id.sum() == 0, f"{bad_id.sum()} rays hit different primitives (not ties)"
+    m = both & same
+    np.testing.assert_allclose(hg["t"][m], ho["t"][m], rtol=RTOL_T)
+    return int(both.sum()), int(tie.sum()), float((hg["t"][m] == ho["t"][m]).mean() if m.any() else 1.0)
+
+
+@pytest.fixture(scope="module")
+def mesh_scene(gpu, oracle):
+    w = scenes.displaced_sphere(64, 64, 1)
+    return w, g.Stage(w.prims, lib=gpu, environment=w.environment), g.Stage(w.prims, lib=oracle,
+                                                                             environment=w.environment)
+
+
+def test_trace_rays_2p20_mesh(mesh_scene):
+    w, sg, so = mesh_scene
+    rays = random_rays(1 << 20, 11, target=(0, 0, 0))
+    hg, ho = sg.intersect(rays), so.intersect(rays)
+    hits, ties, exact = check_hits(hg, ho)
+    assert hits > (1 << 19)  # most rays hit the mesh
+    assert exact == 1.0  # same triangle => bit-identical distance (same arithmetic)
+
+
+@pytest.mark.parametrize("width", [2, 4, 8])
+def test_trace_rays_widths(gpu, oracle, width):
+    w = scenes.displaced_sphere(64, 64, 1, tris=20_000)
+    sg = g.Stage(w.prims, lib=gpu, bvh_width=width, leaf_size=3)
+    so = g.Stage(w.prims, lib=oracle)
+    rays = random_rays(1 << 16, 12 + width, target=(0, 0, 0))
+    check_hits(sg.intersect(rays), so.intersect(rays))
+
+
+def test_trace_rays_spheres_and_naive(gpu, oracle):
+    w = scenes.cornell_spheres()
+    sg = g.Stage(w.prims, lib=gpu)
+    so = g.Stage(w.prims, lib=oracle)
+    rays = random_rays(1 << 16, 13, lo=-0.9, hi=1.9)
+    hg = sg.intersect(rays)
+    check_hits(hg, so.intersect(rays))
+    check_hits(hg, sg.intersect_naive(rays))
+    check_hits(hg, so.intersect_naive(rays))
+
+
+def test_visibility(mesh_scene):
+    w, sg, so = mesh_scene
+    rng = np.random.default_rng(14)
+    a = rng.uniform(-2.5, 2.5, (1 << 16, 3)).astype(np.float32)
+    b = rng.uniform(-2.5, 2.5, (1 << 16, 3)).astype(np.float32)
+    b[:16] = a[:16]  # coincident points are never visible
+    pairs = np.concatenate([a, b], axis=1)
+    vg, vo = sg.visibility(pairs), so.visibility(pairs)
+    assert not vg[:16].any()
+    assert (vg != vo).mean() < 1e-4
+    assert 0.05 < vg.mean() < 0.95
+
+
+def test_sample_light(gpu, oracle):
+    w = scenes.displaced_sphere(64, 64, 1)
+    prims = w.prims + [g.Sphere(g.Material.diffuse_light((2, 2, 2)), g.Mat.translation((2, 2, 0)), 0.5)]
+    sg = g.Stage(prims, lib=gpu)
+    so = g.Stage(prims, lib=oracle)
+    u = np.random.default_rng(15).random((4096, 6), dtype=np.float32)
+    lg, lo = sg.sample_light(u), so.sample_light(u)
+    assert (lg["prim"] == lo["prim"]).all()
+    for f in ("origin", "direction", "normal", "tangent", "binormal", "geom_normal"):
+        np.testing.assert_allclose(lg[f], lo[f], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(lg["point_pdf"], lo["point_pdf"], rtol=1e-6)
+    np.testing.assert_allclose(lg["dir_pdf"], lo["dir_pdf"], rtol=1e-5, atol=1e-6)
+
+
+def random_frames(n, rng):
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    t = np.cross(nrm, rng.normal(size=(n, 3)))
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    b = np.cross(nrm, t)
+    gn = nrm + 0.05 * rng.normal(size=(n, 3))
+    gn /= np.linalg.norm(gn, axis=1, keepdims=True)
+    fr = np.zeros(n, _abi.FRAME_DTYPE)
+    fr["normal"], fr["tangent"], fr["binormal"], fr["geom_normal"] = nrm, t, b, gn
+    return fr
+
+
+def materials():
+    D = g.Material.disney
+    yield "default", D().build()
+    yield "rough_aniso_sheen", D().base_color((0.8, 0.3, 0.1)).roughness(0.9).anisotropic(0.7).sheen(1.0).build()
+    yield "metal", D().base_color((0.9, 0.6, 0.2)).metallic(1.0).roughness(0.2).specular_tint(0.5).build()
+    yield "clearcoat", D().base_color((0.2, 0.4, 0.9)).clearcoat(1.0).clearcoat_gloss(0.7).build()
+    yield "glass", D().base_color((1.0, 1.0, 1.0)).specular_trans(1.0).roughness(0.3).ior(1.5).build()
+    yield "glass_exit", D().specular_trans(0.6).roughness(0.05).ior(1.8).metallic(0.2).build()
+    yield "diffuse_only", D().base_color((0.5, 0.7, 0.2)).ior(1.0).build()
+    yield "trans_only", D().specular_trans(1.0).ior(1.0).roughness(0.5).build()
+    yield "perfect_diffuse", g.Material.diffuse()
+    yield "mirror", g.Material.mirror()
+    yield "light", g.Material.diffuse_light((3.0, 2.0, 1.0))
+
+
+@pytest.mark.parametrize("name,mat", list(materials()))
+def test_bsdf_parity(gpu, oracle, name, mat):
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
+    n = 1 << 15
+    fr = random_frames(n, rng)
+    wi = rng.normal(size=(n, 3))
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    wo = rng.normal(size=(n, 3))
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    wi, wo = wi.astype(np.float32), wo.astype(np.float32)
+    for c2l in (True, False):
+        fg = g.bsdf_eval(mat, fr, wi, wo, c2l, lib=gpu)
+        fo = g.bsdf_eval(mat, fr, wi, wo, c2l, lib=oracle)
+        np.testing.assert_allclose(fg, fo, rtol=RTOL_BSDF, atol=ATOL_BSDF)
+    np.testing.assert_allclose(g.bsdf_pdf(mat, fr, wi, wo, lib=gpu), g.bsdf_pdf(mat, fr, wi, wo, lib=oracle),
+                               rtol=RTOL_BSDF, atol=ATOL_BSDF)
+    np.testing.assert_allclose(g.light_eval(mat, fr, wi, lib=gpu), g.light_eval(mat, fr, wi, lib=oracle),
+                               rtol=0, atol=0)
+    u = rng.random((n, 3), dtype=np.float32)
+    sg = g.bsdf_sample(mat, fr, wi, u, True, lib=gpu)
+    so = g.bsdf_sample(mat, fr, wi, u, True, lib=oracle)
+    ok = np.ones(n, bool)
+    for f in ("radiance", "outgoing", "emission"):
+        ok &= np.isclose(sg[f], so[f], rtol=1e-4, atol=1e-5).all(axis=1)
+    ok &= np.isclose(sg["pdf"], so["pdf"], rtol=1e-4, atol=1e-6)
+    ok &= sg["kind"] == so["kind"]
+    # Transcendentals (cos/sin/log/pow) differ by an ulp between CUDA and libm; a sample
+    # right at a branch point may fall on the other side.  Allow 1 in 10^4.
+    assert ok.mean() > 0.9999, f"{(~ok).sum()} of {n} samples differ"
+
+
+def test_render_samples_per_path(gpu, oracle):
+    for w in (scenes.cornell_spheres(48, 48, 1), scenes.displaced_sphere(48, 48, 1)):
+        sg = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=7)
+        so = g.Stage(w.prims, lib=oracle, environment=w.environment, seed=7)
+        for pass_index in (0, 3):
+            a = sg.samples(w.camera, w.integrator, w.width, w.height, pass_index)
+            b = so.samples(w.camera, w.integrator, w.width, w.height, pass_index)
+            np.testing.assert_array_equal(a[..., :2], b[..., :2])
+            close = np.isclose(a[..., 2:], b[..., 2:], rtol=1e-4, atol=1e-5).all(axis=-1)
+            assert close.mean() >= 0.99, f"{w.name}: {close.mean():.4f} of paths agree"
+
+
+def test_display_color_film_bit_exact(gpu, oracle):
+    w = scenes.cornell_spheres(40, 30, 1)
+    films = []
+    for L in (gpu, oracle):
+        st = g.Stage(w.prims, lib=L, seed=3)
+        f = g.Film(40, 30, lib=L)
+        st.render(w.camera, g.DisplayColorIntegrator(), f, 3)
+        films.append(f.read())
+    (ag, wg), (ao, wo) = films
+    np.testing.assert_array_equal(wg, wo)  # weights depend on the jitter only
+    same = (ag == ao).all(axis=-1)
+    assert same.mean() > 0.999
+
+
+def test_image_statistics(gpu, oracle):
+    w = scenes.cornell_spheres(64, 64, 16)
+    imgs = []
+    for L in (gpu, oracle):
+        st = g.Stage(w.prims, lib=L, seed=5)
+        f = g.Film(64, 64, lib=L)
+        st.render(w.camera, w.integrator, f, 16)
+        imgs.append(f.resolve())
+    a, b = imgs
+    rel_mse = float(np.mean((a - b) ** 2) / np.mean(b ** 2))
+    assert rel_mse < 1e-3, rel_mse
+
+
+def test_exr_matches_oracle(gpu, oracle, tmp_path):
+    w = scenes.cornell_spheres(20, 12, 1)
+    out = []
+    for L, name in ((gpu, "g.exr"), (oracle, "o.exr")):
+        st = g.Stage(w.prims, lib=L, seed=3)
+        f = g.Film(20, 12, lib=L)
+        st.render(w.camera, g.DisplayColorIntegrator(), f, 2)
+        f.write_exr(str(tmp_path / name))
+        out.append((tmp_path / name).read_bytes())
+    assert len(out[0]) == len(out[1])
+    assert out[0][:400] == out[1][:400]  # header and offset table identical
