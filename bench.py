@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--height", type=int, default=1024)
     ap.add_argument("--spp", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="render the workload once (untimed, --spp passes) and exit: the small case for ncu")
     return ap.parse_args()
 
 
@@ -289,10 +291,25 @@ def run_ours(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+def profile_case(args):
+    import gammaray_gb300 as g
+
+    lib = g.load()
+    w = workload(args)
+    st = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1)
+    film = g.Film(w.width, w.height, lib=lib)
+    st.render(w.camera, w.integrator, film, w.spp)
+    s = st.last_stats()
+    print(json.dumps({"profile_case": config_of(w), "device_ms": s.device_ms, "rays": s.extension_rays,
+                      "launches": s.kernel_launches}))
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
-    if args.impl == "reference":
+    if args.profile_case:
+        profile_case(args)
+    elif args.impl == "reference":
         run_reference(args, rank)
     else:
         run_ours(args, rank, world, local)

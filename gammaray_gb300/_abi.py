@@ -262,6 +262,7 @@ SIGNATURES = {
     "gr_material_disney_defaults": (None, [C.POINTER(MaterialDesc)]),
     "gr_scene_create": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(_VP)]),
     "gr_scene_destroy": (C.c_int, [_VP]),
+    "gr_scene_plan": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(SceneInfo)]),
     "gr_scene_get_info": (C.c_int, [_VP, C.POINTER(SceneInfo)]),
     "gr_film_create": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(_VP)]),
     "gr_film_destroy": (C.c_int, [_VP]),
@@ -303,6 +304,10 @@ SIGNATURES = {
 }
 
 
+# Entry points that only the CUDA library exports.
+GPU_ONLY: set = set()
+
+
 def fptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
@@ -320,6 +325,8 @@ class Lib:
         self.path = path
         self.dll = C.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
+            if name in GPU_ONLY and not hasattr(self.dll, name):
+                continue
             fn = getattr(self.dll, name)
             fn.restype = res
             fn.argtypes = args

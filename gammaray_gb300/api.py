@@ -424,6 +424,40 @@ class Film:
         return n.value
 
 
+def scene_desc(prims, environment=(0.0, 0.0, 0.0), bvh_width: int = 0, leaf_size: int = 0):
+    """gr_scene_desc for `prims` (materials deduplicated by identity, in first-use order).
+    Returns (desc, keepalive); the keepalive owns the arrays the desc points into."""
+    materials: list[Material] = []
+    index = {}
+    prim_descs = (_abi.PrimDesc * max(1, len(prims)))()
+    for i, p in enumerate(prims):
+        key = id(p.material)
+        if key not in index:
+            index[key] = len(materials)
+            materials.append(p.material)
+        p.fill(prim_descs[i], index[key])
+    mat_descs = (_abi.MaterialDesc * max(1, len(materials)))(*[m.desc for m in materials])
+    d = _abi.SceneDesc()
+    d.materials = mat_descs
+    d.num_materials = len(materials)
+    d.prims = prim_descs
+    d.num_prims = len(prims)
+    d.environment[:] = [float(x) for x in environment]
+    d.bvh_width = bvh_width
+    d.leaf_size = leaf_size
+    return d, (materials, mat_descs, prim_descs, list(prims))
+
+
+def plan_scene(prims, lib: _abi.Lib | None = None, environment=(0.0, 0.0, 0.0), bvh_width: int = 0,
+               leaf_size: int = 0) -> _abi.SceneInfo:
+    """gr_scene_plan: the BVH build and device footprint of a scene, on the host only."""
+    lib = _default_lib(lib)
+    d, keep = scene_desc(prims, environment, bvh_width, leaf_size)
+    info = _abi.SceneInfo()
+    lib.call("gr_scene_plan", C.byref(d), C.byref(info))
+    return info
+
+
 class Stage:
     """render/stage.rs:10-36 — owns the prims and their BVH; trace() renders one pass.
 
@@ -437,28 +471,11 @@ class Stage:
         self.prims = list(prims)
         self.seed = int(seed)
         self._pass = 0
-        materials: list[Material] = []
-        index = {}
-        prim_descs = (_abi.PrimDesc * max(1, len(self.prims)))()
-        for i, p in enumerate(self.prims):
-            key = id(p.material)
-            if key not in index:
-                index[key] = len(materials)
-                materials.append(p.material)
-            p.fill(prim_descs[i], index[key])
-        mat_descs = (_abi.MaterialDesc * max(1, len(materials)))(*[m.desc for m in materials])
-        d = _abi.SceneDesc()
-        d.materials = mat_descs
-        d.num_materials = len(materials)
-        d.prims = prim_descs
-        d.num_prims = len(self.prims)
-        d.environment[:] = [float(x) for x in environment]
-        d.bvh_width = bvh_width
-        d.leaf_size = leaf_size
+        d, keep = scene_desc(self.prims, environment, bvh_width, leaf_size)
         h = C.c_void_p()
         self.lib.call("gr_scene_create", C.byref(d), C.byref(h))
         self.handle = h
-        self.materials = materials
+        self.materials = keep[0]
 
     def close(self):
         if self.handle:

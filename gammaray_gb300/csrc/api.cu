@@ -184,6 +184,30 @@ gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out) {
     return GR_OK;
 }
 
+static uint64_t planned_bytes(const HostBuild& h) {
+    return h.nodes.size() * 4 + h.prims.size() * 4 + (h.tri_normal_idx.size() + h.tri_uv_idx.size()) * 4 +
+           (h.normals.size() + h.uvs.size()) * 4 + h.prim_material.size() * 4 + h.materials.size() * sizeof(DevMaterial) +
+           h.lights.size() * sizeof(LightRec) + h.light_tris.size() * 4 +
+           (h.light_tri_normal_idx.size() + h.light_tri_uv_idx.size()) * 4 + h.light_cdf.size() * 4;
+}
+
+gr_status gr_scene_plan(const gr_scene_desc* desc, gr_scene_info* o) {
+    if (!desc || !o) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
+    auto t0 = std::chrono::steady_clock::now();
+    HostBuild h;
+    std::string err;
+    if (!build_scene(*desc, h, err)) return fail(GR_ERR_INVALID_ARGUMENT, err);
+    std::memset(o, 0, sizeof(*o));
+    o->num_components = h.num_components;
+    o->num_binary_nodes = h.num_binary_nodes;
+    o->num_wide_nodes = h.num_wide_nodes;
+    o->device_bytes = planned_bytes(h);
+    o->num_lights = static_cast<uint32_t>(h.lights.size());
+    o->bvh_width = h.width;
+    o->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return GR_OK;
+}
+
 gr_status gr_scene_destroy(gr_scene* s) {
     if (!s) return GR_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);

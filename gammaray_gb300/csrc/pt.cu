@@ -413,3 +413,4 @@ int device_sm_count() {
 }
 
 }  // namespace gr
+

@@ -150,6 +150,10 @@ typedef struct gr_scene_info {
  * uploads a wide BVH.  The descriptors may be freed when this returns. */
 gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out);
 gr_status gr_scene_destroy(gr_scene* scene);
+/* Host-only dry run of gr_scene_create: validates the descriptor and runs the BVH
+ * build, without touching a device.  Fills the counts and the device bytes the scene
+ * would occupy (used for admission by free device memory). */
+gr_status gr_scene_plan(const gr_scene_desc* desc, gr_scene_info* out);
 gr_status gr_scene_get_info(const gr_scene* scene, gr_scene_info* out);
 
 /* --------------------------------------------------------------------- camera */

@@ -237,6 +237,15 @@ gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out) {
     return GR_OK;
 }
 
+gr_status gr_scene_plan(const gr_scene_desc* desc, gr_scene_info* o) {
+    gr_scene* s = nullptr;
+    gr_status st = gr_scene_create(desc, &s);
+    if (st != GR_OK) return st;
+    st = gr_scene_get_info(s, o);
+    delete s;
+    return st;
+}
+
 gr_status gr_scene_destroy(gr_scene* s) {
     delete s;
     return GR_OK;

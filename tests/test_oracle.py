@@ -1,0 +1,243 @@
+"""Known-answer and invariant tests of the CPU oracle.
+
+The reference ships no tests, golden vectors or fixtures, and it cannot be built here
+(Rust, no toolchain): the oracle's parity with it is unpinned.  These tests pin the
+restatement against analytic answers and physical invariants instead:
+  - ray/sphere and ray/triangle hits with closed-form distances and barycentrics;
+  - BVH traversal equal to the brute-force Bvh::intersect_naive (geom/bvh.rs:385-400);
+  - a diffuse plane under a white sky returns exactly its albedo (0.5) per path;
+  - reflection-only BSDFs are reciprocal, sampling is consistent with pdf_world
+    (E[cos/pdf] = pi) and the GGX / PerfectDiffuse albedo is at most 1;
+  - the film resolves a constant colour exactly, and the EXR layout of exr.rs.
+"""
+from __future__ import annotations
+
+import math
+import struct
+
+import numpy as np
+import pytest
+
+import gammaray_gb300 as g
+from gammaray_gb300 import _abi, scenes
+
+
+def one_sphere(lib, r=1.0, center=(0, 0, 0), mat=None):
+    s = g.Sphere(mat or g.Material.disney().build(), g.Mat.translation(center), r)
+    return g.Stage([s], lib=lib)
+
+
+def test_sphere_analytic(oracle):
+    st = one_sphere(oracle)
+    rays = np.array([[0, 0, 5, 0, 0, -1], [0, 0, 0, 1, 0, 0], [0, 3, 5, 0, 0, -1], [0.6, 0, 5, 0, 0, -1]], np.float32)
+    h = st.intersect(rays)
+    assert h["prim"].tolist() == [0, 0, -1, 0]
+    assert h["t"][0] == 4.0
+    assert h["t"][1] == 1.0  # from inside: the far root
+    np.testing.assert_allclose(h["t"][3], 5.0 - math.sqrt(1 - 0.36), rtol=1e-6)
+
+
+def test_triangle_analytic(oracle):
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    m = g.Mesh(g.Material.disney().build(), None, v, np.array([[0, 1, 2]]))
+    st = g.Stage([m], lib=oracle)
+    rays = np.array([[0.25, 0.25, 1, 0, 0, -1], [0.8, 0.8, 1, 0, 0, -1], [0.1, 0.2, -2, 0, 0, 1]], np.float32)
+    h = st.intersect(rays)
+    assert h["prim"].tolist() == [0, -1, 0]
+    assert h["t"][0] == 1.0 and h["t"][2] == 2.0
+    # Moller-Trumbore with edges a - c, b - c: the point is u a + v b + (1 - u - v) c.
+    u, vv = h["u"][0], h["v"][0]
+    p = u * v[0] + vv * v[1] + (1 - u - vv) * v[2]
+    np.testing.assert_allclose(p[:2], [0.25, 0.25], atol=1e-6)
+
+
+def test_bvh_equals_naive(oracle):
+    w = scenes.displaced_sphere(8, 8, 1, tris=20_000)
+    st = g.Stage(w.prims, lib=oracle)
+    rng = np.random.default_rng(3)
+    o = rng.uniform(-3, 3, (20000, 3))
+    d = rng.normal(size=(20000, 3)) * 0.5 - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    a, b = st.intersect(rays), st.intersect_naive(rays)
+    assert ((a["prim"] >= 0) == (b["prim"] >= 0)).all()
+    same = (a["prim"] == b["prim"]) & (a["component"] == b["component"])
+    tie = np.abs(a["t"] - b["t"]) <= 1e-6 * np.abs(b["t"])
+    assert (same | tie).all()
+    assert (a["t"][same] == b["t"][same]).all()
+
+
+def test_sah_leaves_hold_one_component(oracle):
+    # geom/bvh.rs:290-296: the SAH "leaf" branch still splits, so a binary tree over N
+    # components with distinct centroids has 2N - 1 nodes.
+    rng = np.random.default_rng(8)
+    c = rng.uniform(-5, 5, (3000, 1, 3))
+    v = (c + rng.uniform(-0.2, 0.2, (3000, 3, 3))).reshape(-1, 3).astype(np.float32)
+    m = g.Mesh(g.Material.disney().build(), None, v, np.arange(len(v)).reshape(-1, 3))
+    info = g.Stage([m], lib=oracle).info()
+    assert info.num_binary_nodes == 2 * info.num_components - 1
+
+
+def test_visibility(oracle):
+    wall = g.Mesh(g.Material.disney().build(), None, *scenes.quad((-1, -1, 0), (2, 0, 0), (0, 2, 0)))
+    st = g.Stage([wall], lib=oracle)
+    pairs = np.array([[0, 0, 1, 0, 0, -1], [0, 0, 1, 0, 0.5, 2], [0, 0, 1, 0, 0, 1.0005], [2, 0, 1, 2, 0, -1]],
+                     np.float32)
+    assert st.visibility(pairs).tolist() == [False, True, False, True]
+
+
+def test_white_sky_diffuse_plane(oracle):
+    # PerfectDiffuse (albedo 0.5) sampled by its own cosine pdf: f cos / pdf = 0.5 exactly,
+    # the bounce escapes to the sky of radiance 1, so every path that sees the plane is 0.5.
+    v, t = scenes.quad((-50, 0, -50), (0, 0, 100), (100, 0, 0))
+    st = g.Stage([g.Mesh(g.Material.diffuse(), None, v, t)], lib=oracle, environment=(1, 1, 1))
+    cam = g.Camera.with_fov(40.0, translate=(0, 1.0, 0), rotate=g.Quat.axis_angle((1, 0, 0), -1.2))
+    s = st.samples(cam, g.PathTracerIntegrator(), 32, 32)
+    col = s[..., 2:]
+    hit_plane = np.abs(col - 0.5).max(axis=-1) < 1e-5
+    sky = np.abs(col - 1.0).max(axis=-1) < 1e-6
+    assert (hit_plane | sky).all()
+    assert hit_plane.mean() > 0.5
+
+
+def random_frames(n, rng):
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    t = np.cross(nrm, rng.normal(size=(n, 3)))
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    fr = np.zeros(n, _abi.FRAME_DTYPE)
+    fr["normal"], fr["tangent"], fr["binormal"], fr["geom_normal"] = nrm, t, np.cross(nrm, t), nrm
+    return fr
+
+
+def hemisphere_dirs(fr, rng):
+    d = rng.normal(size=(len(fr), 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    flip = (d * fr["normal"]).sum(1) < 0
+    d[flip] *= -1
+    return d.astype(np.float32)
+
+
+REFLECTION_MATERIALS = {
+    "disney_default": lambda: g.Material.disney().build(),
+    "rough_sheen": lambda: g.Material.disney().base_color((0.7, 0.2, 0.4)).roughness(0.8).sheen(1).build(),
+    "metal_aniso": lambda: g.Material.disney().metallic(1).roughness(0.4).anisotropic(0.6).build(),
+    "clearcoat": lambda: g.Material.disney().clearcoat(1).clearcoat_gloss(0.5).build(),
+    "perfect_diffuse": lambda: g.Material.diffuse(),
+}
+
+
+@pytest.mark.parametrize("name", list(REFLECTION_MATERIALS))
+def test_reciprocity(oracle, name):
+    rng = np.random.default_rng(1)
+    fr = random_frames(4096, rng)
+    wi, wo = hemisphere_dirs(fr, rng), hemisphere_dirs(fr, rng)
+    m = REFLECTION_MATERIALS[name]()
+    a = g.bsdf_eval(m, fr, wi, wo, lib=oracle)
+    b = g.bsdf_eval(m, fr, wo, wi, lib=oracle)
+    np.testing.assert_allclose(a, b, rtol=2e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("name", ["disney_default", "rough_sheen", "metal_aniso", "perfect_diffuse"])
+def test_sampling_matches_pdf(oracle, name):
+    # For directions drawn by sample_world, E[cos(o) / pdf(o)] = integral of cos over the
+    # hemisphere = pi exactly when pdf_world is the density the sampler draws from.
+    rng = np.random.default_rng(2)
+    n = 200_000
+    fr = random_frames(n, rng)
+    wi = hemisphere_dirs(fr, rng)
+    u = rng.random((n, 3), dtype=np.float32)
+    m = REFLECTION_MATERIALS[name]()
+    s = g.bsdf_sample(m, fr, wi, u, lib=oracle)
+    cos = (s["outgoing"] * fr["normal"]).sum(1)
+    valid = (s["kind"] != 0) & (cos > 0)
+    est = np.where(valid, cos / np.where(valid, s["pdf"], 1.0), 0.0)
+    se = est.std() / math.sqrt(n)
+    assert abs(est.mean() - math.pi) < 5 * se + 2e-3, (est.mean(), se)
+
+
+def test_clearcoat_pdf_quirk(oracle):
+    # GTR1 samples the half vector with density D(h) cos(theta_h), but its pdf() returns
+    # D(h) alone (material/util.rs:291-308), so pdf_world over-states the density by
+    # 1 / cos(theta_h) >= 1 and E[cos / pdf] falls below pi.  Kept as in the reference.
+    rng = np.random.default_rng(6)
+    n = 200_000
+    fr = random_frames(n, rng)
+    wi = hemisphere_dirs(fr, rng)
+    u = rng.random((n, 3), dtype=np.float32)
+    m = g.Material.disney().metallic(1).ior(1.0).clearcoat(1).clearcoat_gloss(0.2).build()  # clearcoat lobe only
+    s = g.bsdf_sample(m, fr, wi, u, lib=oracle)
+    cos = (s["outgoing"] * fr["normal"]).sum(1)
+    valid = (s["kind"] != 0) & (cos > 0)
+    est = np.where(valid, cos / np.where(valid, s["pdf"], 1.0), 0.0)
+    assert est.mean() < math.pi - 10 * est.std() / math.sqrt(n)
+
+
+@pytest.mark.parametrize("name", ["metal_aniso", "perfect_diffuse"])
+def test_albedo_at_most_one(oracle, name):
+    rng = np.random.default_rng(4)
+    n = 100_000
+    fr = random_frames(n, rng)
+    wi = hemisphere_dirs(fr, rng)
+    u = rng.random((n, 3), dtype=np.float32)
+    s = g.bsdf_sample(REFLECTION_MATERIALS[name](), fr, wi, u, lib=oracle)
+    cos = np.abs((s["outgoing"] * fr["normal"]).sum(1))
+    w = s["radiance"].max(1) * cos / s["pdf"]
+    assert w.mean() <= 1.0 + 5 * w.std() / math.sqrt(n)
+    if name == "perfect_diffuse":
+        np.testing.assert_allclose(w, 0.5, rtol=1e-5)
+
+
+def test_light_one_sided(oracle):
+    fr = random_frames(2, np.random.default_rng(5))
+    wi = np.stack([fr["geom_normal"][0], -fr["geom_normal"][1]]).astype(np.float32)
+    L = g.light_eval(g.Material.diffuse_light((3, 2, 1)), fr, wi, lib=oracle)
+    assert L[0].tolist() == [3, 2, 1] and L[1].tolist() == [0, 0, 0]
+
+
+def test_film_constant_colour(oracle):
+    # Camera inside a big sphere of one display colour: accum / weight is that colour.
+    mat = g.Material.disney().base_color((0.3, 0.5, 0.7)).build()
+    st = g.Stage([g.Sphere(mat, None, 10.0)], lib=oracle)
+    f = g.Film(24, 16, lib=oracle)
+    st.render(g.Camera.with_fov(60.0, 1.5), g.DisplayColorIntegrator(), f, 3)
+    np.testing.assert_allclose(f.resolve(), np.broadcast_to([0.3, 0.5, 0.7], (16, 24, 3)), rtol=1e-5)
+    assert f.passes() == 3
+
+
+def test_exr_layout(oracle, tmp_path):
+    st = g.Stage([g.Sphere(g.Material.disney().base_color((0.3, 0.5, 0.7)).build(), None, 10.0)], lib=oracle)
+    f = g.Film(5, 3, lib=oracle)
+    st.render(g.Camera.with_fov(60.0), g.DisplayColorIntegrator(), f, 1)
+    path = tmp_path / "o.exr"
+    f.write_exr(str(path))
+    b = path.read_bytes()
+    assert struct.unpack("<ii", b[:8]) == (20000630, 2)
+    line = 8 + 5 * 12
+    offsets = [struct.unpack("<Q", b[len(b) - 3 * line - 8 * 3 + 8 * k:][:8])[0] for k in range(3)]
+    assert offsets == [len(b) - 3 * line + k * line for k in range(3)]
+    rgb = f.resolve()
+    first = b[offsets[0]:offsets[0] + line]
+    assert struct.unpack("<iI", first[:8]) == (0, line - 8)
+    planes = np.frombuffer(first[8:], "<f4").reshape(3, 5)
+    np.testing.assert_array_equal(planes[0], rgb[2, :, 2])  # B plane of the bottom row
+    np.testing.assert_array_equal(planes[2], rgb[2, :, 0])  # R plane
+
+
+def test_bdpt_runs_and_agrees_with_pt(oracle):
+    w = scenes.cornell_spheres(24, 24, 1)
+    st = g.Stage(w.prims, lib=oracle, seed=2)
+    fp, fb = g.Film(24, 24, lib=oracle), g.Film(24, 24, lib=oracle)
+    st.render(w.camera, g.PathTracerIntegrator(), fp, 32)
+    st.render(w.camera, g.BdptIntegrator(), fb, 32)
+    a, b = fp.resolve().mean(), fb.resolve().mean()
+    assert np.isfinite(b) and b > 0
+    assert abs(a - b) / a < 0.2  # the reference BDPT's uniform weights are close to, not equal to, PT
+
+
+def test_invalid_inputs(oracle):
+    with pytest.raises(_abi.GrError):
+        g.Stage([g.Sphere(g.Material.disney().build(), None, -1.0)], lib=oracle)
+    m = g.Mesh(g.Material.disney().build(), None, np.zeros((3, 3), np.float32), np.array([[0, 1, 5]]))
+    with pytest.raises(_abi.GrError):
+        g.Stage([m], lib=oracle)
