@@ -278,6 +278,10 @@ SIGNATURES = {
         [_VP, C.POINTER(CameraDesc), C.POINTER(RenderParams), C.c_uint32, C.c_uint32, _PF],
     ),
     "gr_scene_last_stats": (C.c_int, [_VP, C.POINTER(RenderStats)]),
+    "gr_render_static": (
+        C.c_int,
+        [_VP, C.POINTER(CameraDesc), C.POINTER(RenderParams), C.c_uint32, C.c_uint32, _VP, _VP],
+    ),
     "gr_trace_rays": (C.c_int, [_VP, _PF, C.c_uint64, C.POINTER(Hit)]),
     "gr_trace_rays_dev": (C.c_int, [_VP, _VP, C.c_uint64, _VP, _VP]),
     "gr_intersect_naive": (C.c_int, [_VP, _PF, C.c_uint64, C.POINTER(Hit)]),
@@ -305,7 +309,7 @@ SIGNATURES = {
 
 
 # Entry points that only the CUDA library exports.
-GPU_ONLY: set = set()
+GPU_ONLY = {"gr_render_static"}
 
 
 def fptr(a: np.ndarray):

@@ -30,7 +30,7 @@ static gr_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st, uin
 }
 
 // Camera::new (core/camera.rs:42-61): xform = translation * rotation (row vectors).
-static DevCamera make_camera(const gr_camera& c) {
+DevCamera make_camera(const gr_camera& c) {
     float T[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {c.translate[0], c.translate[1], c.translate[2], 1}};
     float r = c.rotate[0], ix = c.rotate[1], iy = c.rotate[2], iz = c.rotate[3];
     float R[4][4];  // core/matrix.rs:97-121

@@ -15,6 +15,8 @@
 // host never waits for a bounce; it polls the count two bounces behind to stop.
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
+#include <string>
 #include <utility>
 #include <vector>
 
@@ -414,3 +416,158 @@ int device_sm_count() {
 
 }  // namespace gr
 
+// ---------------------------------------------------------------------------
+// Render entry point that allocates nothing.
+//
+// Some callers cannot let a library allocate device memory: a host that owns all GPU
+// memory through its own pool and forbids hidden allocations, a real-time frame loop
+// where cudaMalloc / cudaFree would stall it (they synchronise the device), or code
+// that enqueues work on a stream it does not want the library to synchronise.  For
+// them, gr_render_static runs the same wavefront kernels as gr_render, with the path
+// state and queues in one fixed device array of this library instead of buffers of
+// the scene.  The caller passes the inputs (scene, camera, settings) and the output
+// (a device film of width * height float4 {accum.rgb, weight}, accumulated into).
+//
+// Limits and sharing:
+//   - at most STATIC_MAX_PATHS (131072) pixels per image; larger sizes are rejected;
+//   - the array (STATIC_SCRATCH_BYTES, about 18 MB) is held by every GPU that loads the
+//     library until the process exits;
+//   - every call uses the same array and it keeps the last call's contents, so calls
+//     that overlap on the GPU (other threads, other streams) race: serialise them;
+//   - the first call on a device looks up the array's device address
+//     (cudaGetSymbolAddress) with that device current; make that first call before any
+//     stream capture.
+namespace gr {
+namespace {
+
+constexpr uint32_t STATIC_MAX_PATHS = 1u << 17;
+// Per path: tp, light (float4), key (u64), st (float2), queue slot x2, queue o/d x2
+// (float4), hit (float4); plus a 256-byte block of counters.
+constexpr size_t STATIC_PER_PATH = 16 + 16 + 8 + 8 + 2 * 4 + 2 * 16 + 2 * 16 + 16;
+constexpr size_t STATIC_SCRATCH_BYTES = STATIC_MAX_PATHS * STATIC_PER_PATH + 256;
+
+static __device__ __align__(256) unsigned char g_static_scratch[STATIC_SCRATCH_BYTES];
+
+constexpr int STATIC_MAX_DEVICES = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[STATIC_MAX_DEVICES] = {nullptr};
+
+// Device address of g_static_scratch for the current device, looked up once.
+gr_status static_scratch(void** out) {
+    int dev = 0;
+    GR_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= STATIC_MAX_DEVICES) {
+        set_error("device index out of range for the static scratch table");
+        return GR_ERR_INTERNAL;
+    }
+    std::lock_guard<std::mutex> g(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void* p = nullptr;
+        GR_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+        g_static_ptr[dev] = p;
+    }
+    *out = g_static_ptr[dev];
+    return GR_OK;
+}
+
+}  // namespace
+
+}  // namespace gr
+
+using namespace gr;
+
+extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, const gr_render_params* rp,
+                                      uint32_t width, uint32_t height, float* film_dev, void* stream) {
+    if (!sc || !camera || !rp || !film_dev || width == 0 || height == 0) {
+        set_error("gr_render_static: null argument or empty image");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    if (rp->integrator != GR_INTEGRATOR_PATH_TRACER && rp->integrator != GR_INTEGRATOR_DISPLAY_COLOR) {
+        set_error("gr_render_static: only the path tracer and the display-colour integrator are supported");
+        return GR_ERR_UNSUPPORTED;
+    }
+    const uint64_t npix64 = static_cast<uint64_t>(width) * height;
+    if (npix64 > STATIC_MAX_PATHS) {
+        set_error("gr_render_static: width * height = " + std::to_string(npix64) + " exceeds the fixed maximum of " +
+                  std::to_string(STATIC_MAX_PATHS) + " pixels");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    if (rp->spp == 0) return GR_OK;
+    void* base = nullptr;
+    GR_TRY_S(static_scratch(&base));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const uint32_t npix = static_cast<uint32_t>(npix64);
+    const size_t cap = STATIC_MAX_PATHS;
+    // Carve the array (same layout for every call; every region is 16-byte aligned).
+    unsigned char* b = static_cast<unsigned char*>(base);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(b);
+    size_t off = 256;
+    auto take = [&](size_t bytes) {
+        void* p = b + off;
+        off += bytes;
+        return p;
+    };
+    float4* tp = static_cast<float4*>(take(cap * sizeof(float4)));
+    float4* light = static_cast<float4*>(take(cap * sizeof(float4)));
+    unsigned long long* key = static_cast<unsigned long long*>(take(cap * sizeof(unsigned long long)));
+    float2* stb = static_cast<float2*>(take(cap * sizeof(float2)));
+    float4* q_o[2];
+    float4* q_d[2];
+    q_o[0] = static_cast<float4*>(take(cap * sizeof(float4)));
+    q_o[1] = static_cast<float4*>(take(cap * sizeof(float4)));
+    q_d[0] = static_cast<float4*>(take(cap * sizeof(float4)));
+    q_d[1] = static_cast<float4*>(take(cap * sizeof(float4)));
+    float4* q_hit = static_cast<float4*>(take(cap * sizeof(float4)));
+    uint32_t* q_slot[2];
+    q_slot[0] = static_cast<uint32_t*>(take(cap * sizeof(uint32_t)));
+    q_slot[1] = static_cast<uint32_t*>(take(cap * sizeof(uint32_t)));
+    int* err = reinterpret_cast<int*>(cnt + CNT_ERROR);
+    unsigned long long* rays = reinterpret_cast<unsigned long long*>(cnt + CNT_RAYS);
+
+    const bool display = rp->integrator == GR_INTEGRATOR_DISPLAY_COLOR;
+    PTParams p;
+    p.cam = make_camera(*camera);
+    p.width = width;
+    p.height = height;
+    p.npix = npix;
+    p.seed = rp->seed;
+    p.max_depth = display ? 1 : rp->max_depth;
+    p.rr_depth = rp->rr_depth;
+    p.rr_aggr = rp->rr_aggressive_depth;
+    // The array keeps the previous call's contents: clear the counters every call.
+    GR_CUDA_TRY(cudaMemsetAsync(cnt, 0, 256, st));
+    for (uint32_t pass = 0; pass < rp->spp; ++pass) {
+        p.first_pass = rp->first_pass + pass;
+        uint32_t n = npix;
+        GR_CUDA_TRY(cudaMemcpyAsync(cnt + CNT_QUEUE0, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, tp, light, key, stb, q_slot[0], q_o[0], q_d[0]);
+        GR_CUDA_TRY(cudaGetLastError());
+        for (uint32_t depth = 0;; ++depth) {
+            if (p.max_depth && depth >= p.max_depth) break;
+            int cur = depth & 1, nxt = cur ^ 1;
+            GR_TRY_S(extend_any(sc->dev, false, n, cnt + cur, q_o[cur], q_d[cur], q_hit, err, rays, st));
+            GR_CUDA_TRY(cudaGetLastError());
+            if (display) {
+                int grid = resident_grid(k_shade_display, 0, n);
+                k_shade_display<<<grid, BLOCK, 0, st>>>(sc->dev, cnt + cur, q_slot[cur], q_hit, light);
+                GR_CUDA_TRY(cudaGetLastError());
+                break;
+            }
+            GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
+            int grid = resident_grid(k_shade, 0, n);
+            k_shade<<<grid, BLOCK, 0, st>>>(sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit, tp,
+                                            light, key, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt]);
+            GR_CUDA_TRY(cudaGetLastError());
+            if (p.max_depth == 0 && (depth & 3) == 3) {
+                // Unbounded (reference) depth: stop once no path is left.  The copy goes
+                // to a stack variable; no host or device memory is allocated.
+                uint32_t left = 0;
+                GR_CUDA_TRY(cudaMemcpyAsync(&left, cnt + nxt, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+                GR_CUDA_TRY(cudaStreamSynchronize(st));
+                if (left == 0) break;
+            }
+        }
+        GR_TRY_S(film_gather(stb, light, width, height, 1, reinterpret_cast<float4*>(film_dev), st));
+    }
+    return GR_OK;
+}

@@ -129,4 +129,7 @@ gr_status film_exr_pack(const float4* film, uint32_t width, uint32_t height, uns
 
 int device_sm_count();
 
+// Camera::new (core/camera.rs:42-61) evaluated on the host.
+DevCamera make_camera(const gr_camera& c);
+
 }  // namespace gr

@@ -242,6 +242,20 @@ gr_status gr_render_samples(gr_scene* scene, const gr_camera* camera,
                             const gr_render_params* params, uint32_t width,
                             uint32_t height, float* samples);
 
+/* A render that allocates nothing, for callers that cannot let a library allocate
+ * device memory (an application that owns all GPU memory through its own pool, or a
+ * frame loop that cudaMalloc / cudaFree would stall by synchronising the device).
+ * No counterpart in the reference.  Runs the same path-tracer (or display-colour)
+ * passes as gr_render on `stream` (a cudaStream_t, or 0) and accumulates them into
+ * `film_dev`, caller-owned device memory of width * height float4 {accum.rgb, weight}.
+ * Its scratch is one fixed array inside the library (about 18 MB, held by every GPU
+ * that loads the library until exit): at most 131072 pixels per image, larger images
+ * are rejected with GR_ERR_INVALID_ARGUMENT.  All calls share that array, so calls
+ * that overlap on the GPU race.  The first call on a device resolves the array's
+ * address; make it before any stream capture.  Exported by the GPU library only. */
+gr_status gr_render_static(gr_scene* scene, const gr_camera* camera, const gr_render_params* params,
+                           uint32_t width, uint32_t height, float* film_dev, void* stream);
+
 /* Counters of the last gr_render on this scene (GPU library; zeros otherwise). */
 typedef struct gr_render_stats {
     uint64_t samples;         /* camera paths completed */
