@@ -3,7 +3,10 @@
 // scene's own stream; host-buffer calls copy in, launch and copy out on that stream.
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <fstream>
 #include <memory>
 
@@ -17,6 +20,36 @@ void set_error(const std::string& msg) { g_err = msg; }
 static gr_status fail(gr_status s, const std::string& msg) {
     g_err = msg;
     return s;
+}
+
+gr_status sync_check(cudaStream_t st, const char* what, uint32_t bounce, uint32_t n) {
+    static const double limit = [] {
+        const char* e = std::getenv("GR_SYNC_CHECK");
+        return e ? std::atof(e) : 0.0;
+    }();
+    if (limit <= 0.0) return GR_OK;
+    cudaEvent_t ev;
+    GR_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    GR_CUDA_TRY(cudaEventRecord(ev, st));
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t q = cudaEventQuery(ev);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) {
+            cudaEventDestroy(ev);
+            return fail(GR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(q));
+        }
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > limit) {
+            std::string msg = std::string(what) + " did not finish within " + std::to_string(limit) + " s (bounce " +
+                              std::to_string(bounce) + ", capacity " + std::to_string(n) + ")";
+            std::fprintf(stderr, "gammaray: %s\n", msg.c_str());
+            return fail(GR_ERR_TIMEOUT, msg);
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    cudaEventDestroy(ev);
+    return GR_OK;
 }
 
 template <class T>
@@ -408,6 +441,8 @@ static gr_status run_render(gr_scene* s, const gr_camera* c, const gr_render_par
     s->stats.shadow_rays = shadow;
     std::memcpy(&s->stats.node_visits, cnt + CNT_NODES, 8);
     std::memcpy(&s->stats.prim_tests, cnt + CNT_PRIMS, 8);
+    if (cnt[CNT_ERROR] == 2)
+        return fail(GR_ERR_TIMEOUT, "traversal step budget exceeded (ray " + std::to_string(cnt[CNT_ERROR + 1]) + ")");
     if (cnt[CNT_ERROR]) return fail(GR_ERR_STACK_OVERFLOW, "traversal stack bound exceeded");
     return GR_OK;
 }

@@ -1,11 +1,498 @@
-// Wavefront BDPT (render/integrators.rs:102-418).
+// Wavefront BDPT: BdptIntegrator::integrate (render/integrators.rs:357-418) with the
+// reference's uniform strategy weights 1 / (c + l) (integrators.rs:345-354).
+//
+//   raygen    per path: jitter + camera ray (camera walk, slot 2i) and Bvh::sample_light
+//             + the light vertex (light walk, slot 2i+1), both pushed to one queue
+//   extend    closest hit (shared with the path tracer)
+//   shade     random_walk (integrators.rs:138-229) for both walks: Material::sample_world,
+//             throughput, shading-normal correction on light paths, roulette from
+//             length rr_len; each vertex is stored SoA, the escape vertex too
+//   connect   per path, every strategy (c >= 1, l >= 0, c + l <= max) in the reference's
+//             loop order: connect() (integrators.rs:269-343) without the visibility test;
+//             terms that need one queue a shadow ray
+//   shadow    Bvh::visibility (bvh.rs:460-477) as an any-hit query
+//   gather    per path, sums the strategy terms in loop order (deterministic, same
+//             order as the reference)
+//   film      the deterministic splat of film.cu
+#include <algorithm>
+#include <cstdlib>
+
 #include "runtime.hpp"
+#include "wavefront.cuh"
 
 namespace gr {
 
-gr_status render_bdpt(gr_scene*, const RenderJob&, cudaStream_t) {
-    set_error("BDPT is not built yet");
-    return GR_ERR_UNSUPPORTED;
+namespace {
+
+constexpr int VREC = 7;            // float4 per stored vertex
+constexpr uint32_t F_SKIP = 1;     // light sample had a zero pdf: the reference returns early
+constexpr uint32_t F_ESCAPE = 2;   // the camera walk escaped (environment term)
+constexpr float E_NO_TEST = 0.0f;  // entry flags (float in .w)
+constexpr float E_PENDING = 1.0f;
+constexpr float E_VISIBLE = 2.0f;
+constexpr float E_OCCLUDED = 3.0f;
+constexpr int CNT_ENTRIES = 12;
+constexpr int CNT_SHADOWQ = 13;
+
+struct BdptParams {
+    DevCamera cam;
+    uint32_t width, height, npix, first_pass;
+    uint64_t seed;
+    uint32_t max_len, rr_len;
+    uint32_t n;       // paths in this group
+    uint32_t nslots;  // 2 n
+};
+
+// Stored vertex (BdptVertex, integrators.rs:107-130) as 7 float4, field-major:
+//   0: point, prim     1: incoming, connectible   2: normal, tp.x   3: tangent, tp.y
+//   4: binormal, tp.z  5: geom_normal, material   6: emission
+struct Verts {
+    float4* v;
+    uint32_t nslots;
+    GR_D float4& at(uint32_t k, int f, uint32_t slot) const {
+        return v[(static_cast<size_t>(k) * VREC + f) * nslots + slot];
+    }
+};
+
+struct Vtx {
+    V3 point, incoming, tp, emission;
+    Frame frame;
+    uint32_t prim, material;
+    bool connectible;
+};
+
+GR_D Vtx load_vertex(const Verts& vs, uint32_t k, uint32_t slot) {
+    float4 f0 = vs.at(k, 0, slot), f1 = vs.at(k, 1, slot), f2 = vs.at(k, 2, slot), f3 = vs.at(k, 3, slot),
+           f4 = vs.at(k, 4, slot), f5 = vs.at(k, 5, slot), f6 = vs.at(k, 6, slot);
+    Vtx x;
+    x.point = V3{f0.x, f0.y, f0.z};
+    x.prim = __float_as_uint(f0.w);
+    x.incoming = V3{f1.x, f1.y, f1.z};
+    x.connectible = __float_as_uint(f1.w) != 0;
+    x.frame.normal = V3{f2.x, f2.y, f2.z};
+    x.frame.tangent = V3{f3.x, f3.y, f3.z};
+    x.frame.binormal = V3{f4.x, f4.y, f4.z};
+    x.frame.geom_normal = V3{f5.x, f5.y, f5.z};
+    x.tp = V3{f2.w, f3.w, f4.w};
+    x.material = __float_as_uint(f5.w);
+    x.emission = V3{f6.x, f6.y, f6.z};
+    return x;
+}
+
+GR_D void store_vertex(const Verts& vs, uint32_t k, uint32_t slot, V3 point, uint32_t prim, V3 incoming,
+                       bool connectible, const Frame& f, V3 tp, uint32_t material, V3 emission) {
+    vs.at(k, 0, slot) = make_float4(point.x, point.y, point.z, __uint_as_float(prim));
+    vs.at(k, 1, slot) = make_float4(incoming.x, incoming.y, incoming.z, __uint_as_float(connectible ? 1u : 0u));
+    vs.at(k, 2, slot) = make_float4(f.normal.x, f.normal.y, f.normal.z, tp.x);
+    vs.at(k, 3, slot) = make_float4(f.tangent.x, f.tangent.y, f.tangent.z, tp.y);
+    vs.at(k, 4, slot) = make_float4(f.binormal.x, f.binormal.y, f.binormal.z, tp.z);
+    vs.at(k, 5, slot) = make_float4(f.geom_normal.x, f.geom_normal.y, f.geom_normal.z, __uint_as_float(material));
+    vs.at(k, 6, slot) = make_float4(emission.x, emission.y, emission.z, 0.0f);
+}
+
+// Warp-aggregated counter increment for divergent code (the lanes active here).
+GR_D uint32_t agg_inc(uint32_t* ctr) {
+    unsigned m = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(ctr, static_cast<uint32_t>(__popc(m)));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+GR_D float correct_shading_normal(V3 in_w, V3 out_w, const Frame& f, bool c2l) {  // integrators.rs:232-251
+    if (c2l) return 1.0f;
+    float num = fabsf(dot(in_w, f.normal)) * fabsf(dot(out_w, f.geom_normal));
+    float den = fabsf(dot(in_w, f.geom_normal)) * fabsf(dot(out_w, f.normal));
+    if (den == 0.0f) return 0.0f;
+    return num / den;
+}
+
+GR_D float convert_density(V3 prev, V3 next, const Frame& nf) {  // integrators.rs:253-266
+    float dist = magnitude(next - prev);
+    if (dist == 0.0f) return 0.0f;
+    V3 p2n = (next - prev) / dist;
+    return fabsf(dot(nf.normal, p2n)) / (dist * dist);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams p, Verts vs,
+                                                       uint32_t* __restrict__ vcount, float4* __restrict__ tp_buf,
+                                                       uint32_t* __restrict__ flags,
+                                                       unsigned long long* __restrict__ key_buf,
+                                                       float2* __restrict__ st_buf, float4* __restrict__ escape,
+                                                       uint32_t* count_out, uint32_t* __restrict__ nslot,
+                                                       float4* __restrict__ no, float4* __restrict__ nd) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool cam_alive = false, light_alive = false;
+    V3 co = v3zero(), cd = v3zero(), lo = v3zero(), ld = v3zero();
+    if (i < p.n) {
+        uint32_t pass_local = i / p.npix;
+        uint32_t pixel = i - pass_local * p.npix;
+        uint32_t row = pixel / p.width, col = pixel - (pixel / p.width) * p.width;
+        uint64_t key = path_key(p.seed, p.first_pass + pass_local, pixel);
+        float s0, t0;
+        film_sample_point(p.width, p.height, row, col, key, s0, t0);
+        camera_ray(p.cam, s0, t0, co, cd);
+        key_buf[i] = key;
+        st_buf[i] = make_float2(s0, t0);
+        escape[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        uint32_t fl = 0;
+        vcount[2 * i] = 0;
+        tp_buf[2 * i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        cam_alive = p.max_len > 0;
+        vcount[2 * i + 1] = 0;
+        if (s.num_lights > 0) {
+            float u[6];
+            for (int k = 0; k < 6; ++k) u[k] = uniform01(key, DIM_LIGHT_SAMPLE + k);
+            DevLightSample ls = sample_light(s, u);
+            if (ls.point_pdf == 0.0f || ls.dir_pdf == 0.0f) {
+                fl |= F_SKIP;
+            } else {
+                uint32_t mi = __ldg(s.prim_material + ls.prim);
+                const DevMaterial& m = s.materials[mi];
+                V3 ie = light_world(m, ls.direction, ls.frame) *
+                        (fabsf(dot(ls.frame.geom_normal, ls.direction)) / (ls.point_pdf * ls.dir_pdf));
+                store_vertex(vs, 0, 2 * i + 1, ls.origin, ls.prim, v3zero(), true, ls.frame, v3one() / ls.point_pdf,
+                             mi, v3zero());
+                vcount[2 * i + 1] = 1;
+                tp_buf[2 * i + 1] = make_float4(ie.x, ie.y, ie.z, 0.0f);
+                light_alive = !is_zero(ie) && 1 < p.max_len;
+                lo = nudge(ls.origin, ls.direction);
+                ld = ls.direction;
+            }
+        }
+        flags[i] = fl;
+    }
+    push_warp(cam_alive, count_out, 2 * i, co, cd, nslot, no, nd);
+    push_warp(light_alive, count_out, 2 * i + 1, lo, ld, nslot, no, nd);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_bdpt_shade(DeviceScene s, BdptParams p, Verts vs,
+                                                      const uint32_t* __restrict__ count_in,
+                                                      const uint32_t* __restrict__ q_slot,
+                                                      const float4* __restrict__ q_o, const float4* __restrict__ q_d,
+                                                      const float4* __restrict__ q_hit, uint32_t* __restrict__ vcount,
+                                                      float4* __restrict__ tp_buf,
+                                                      const unsigned long long* __restrict__ key_buf,
+                                                      uint32_t* __restrict__ flags, float4* __restrict__ escape,
+                                                      uint32_t* count_out, uint32_t* __restrict__ nslot,
+                                                      float4* __restrict__ no, float4* __restrict__ nd) {
+    const uint32_t n = *count_in;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
+        uint32_t q = b + (threadIdx.x & 31u);
+        bool alive = false;
+        uint32_t slot = 0;
+        V3 new_o = v3zero(), new_d = v3zero();
+        if (q < n) {
+            slot = q_slot[q];
+            const uint32_t walk = slot & 1u, path = slot >> 1;
+            const bool c2l = walk == 0;
+            float4 h = q_hit[q];
+            float4 o4 = q_o[q], d4 = q_d[q];
+            V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
+            float4 t4 = tp_buf[slot];
+            V3 tp = V3{t4.x, t4.y, t4.z};
+            uint32_t k = vcount[slot];
+            int32_t pk = __float_as_int(h.y);
+            if (pk < 0) {
+                // As if a black infinite light was hit (integrators.rs:210-225).  The
+                // throughput at the escape is kept for the environment extension.
+                Frame z{v3zero(), v3zero(), v3zero(), v3zero()};
+                store_vertex(vs, k, slot, v3zero(), NO_INDEX, -d, false, z, tp, 0, v3zero());
+                vcount[slot] = k + 1;
+                if (walk == 0) {
+                    escape[path] = make_float4(tp.x, tp.y, tp.z, 0.0f);
+                    flags[path] |= F_ESCAPE;
+                }
+            } else {
+                uint32_t prim;
+                Frame f = hit_frame(s, pk, o, d, h.x, h.z, h.w, prim);
+                uint32_t mi = __ldg(s.prim_material + prim);
+                const DevMaterial& m = s.materials[mi];
+                uint64_t key = key_buf[path];
+                uint32_t base = (walk ? DIM_LIGHT_WALK : DIM_CAMERA_WALK) + 4 * k;
+                V3 incoming = -d;
+                V3 hit_point = o + (d * h.x);
+                MaterialSample ms = sample_world(m, incoming, f, c2l, uniform01(key, base), uniform01(key, base + 1),
+                                                 uniform01(key, base + 2));
+                bool connectible = count_lobes(m, LOBE_DIFFUSE | LOBE_GLOSSY) != 0;
+                V3 ntp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
+                ntp = ntp * correct_shading_normal(incoming, ms.outgoing, f, c2l);
+                store_vertex(vs, k, slot, hit_point, prim, incoming, connectible, f, tp, mi, ms.emission);
+                vcount[slot] = k + 1;
+                if (k + 1 >= p.rr_len || nearly_zero(ntp)) {
+                    float rv = uniform01(key, base + 3);
+                    float prob = clamped_lerp(0.25f, 0.75f, luminance(ntp));
+                    ntp = rv < prob ? ntp / prob : v3zero();
+                }
+                alive = !is_zero(ntp) && k + 1 < p.max_len;
+                new_o = nudge(hit_point, ms.outgoing);
+                new_d = ms.outgoing;
+                if (alive) tp_buf[slot] = make_float4(ntp.x, ntp.y, ntp.z, 0.0f);
+            }
+        }
+        push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
+    }
+}
+
+GR_D uint32_t num_entries(uint32_t cs, uint32_t ls, uint32_t max_len) {
+    uint32_t e = 0;
+    for (uint32_t c = 1; c <= cs; ++c) e += min(ls, max_len - c) + 1;
+    return e;
+}
+
+// connect() for every strategy of one path, in the reference's loop order.
+__global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParams p, Verts vs,
+                                                        const uint32_t* __restrict__ vcount,
+                                                        const uint32_t* __restrict__ flags, uint32_t* counters,
+                                                        uint32_t* __restrict__ entry_base, float4* __restrict__ entries,
+                                                        uint4* __restrict__ shadow_q) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    uint32_t fl = flags[i];
+    if (fl & F_SKIP) return;
+    uint32_t cs = vcount[2 * i], ls = vcount[2 * i + 1];
+    uint32_t ne = num_entries(cs, ls, p.max_len);
+    uint32_t base = ne ? atomicAdd(counters + CNT_ENTRIES, ne) : 0;
+    entry_base[i] = base;
+    uint32_t j = base;
+    for (uint32_t c = 1; c <= cs; ++c) {
+        Vtx cv = load_vertex(vs, c - 1, 2 * i);
+        for (uint32_t l = 0; l <= ls; ++l) {
+            if (c + l > p.max_len) continue;
+            V3 term = v3zero();
+            float flag = E_NO_TEST;
+            if (l == 0) {
+                if (cv.prim != NO_INDEX) term = mul(cv.tp, cv.emission);
+            } else {
+                Vtx lv = load_vertex(vs, l - 1, 2 * i + 1);
+                if (cv.prim != NO_INDEX && lv.prim != NO_INDEX && cv.connectible && lv.connectible) {
+                    V3 c2l = normalized(lv.point - cv.point);
+                    V3 l2c = -c2l;
+                    const DevMaterial& cm = s.materials[cv.material];
+                    const DevMaterial& lm = s.materials[lv.material];
+                    V3 cr = f_world(cm, cv.incoming, c2l, cv.frame, true);
+                    V3 ce = l == 1 ? light_world(lm, l2c, lv.frame) : f_world(lm, lv.incoming, l2c, lv.frame, false);
+                    float g = fabsf(dot(cv.frame.normal, c2l));
+                    float cdn = convert_density(cv.point, lv.point, lv.frame);
+                    term = mul(mul(mul(cv.tp, cr), ce), lv.tp) * (g * cdn);
+                    if (!nearly_zero(term)) {
+                        flag = E_PENDING;
+                        uint32_t sq = agg_inc(counters + CNT_SHADOWQ);
+                        // float4 index of field 0 (point) of each vertex
+                        shadow_q[sq] = make_uint4(j, (c - 1) * VREC * p.nslots + 2 * i,
+                                                  (l - 1) * VREC * p.nslots + 2 * i + 1, 0);
+                    }
+                }
+            }
+            entries[j] = make_float4(term.x, term.y, term.z, flag);
+            ++j;
+        }
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(BLOCK) k_bdpt_shadow(DeviceScene s, const uint32_t* __restrict__ count,
+                                                       const uint4* __restrict__ shadow_q, const float4* __restrict__ v0,
+                                                       float4* __restrict__ entries, int* err,
+                                                       unsigned long long* shadow_rays) {
+    extern __shared__ unsigned char smem[];
+    int32_t* sref = reinterpret_cast<int32_t*>(smem);
+    float* stt = reinterpret_cast<float*>(smem + sizeof(int32_t) * s.stack_depth * blockDim.x);
+    const uint32_t n = *count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(shadow_rays, static_cast<unsigned long long>(n));
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        uint4 e = shadow_q[q];
+        float4 a4 = v0[e.y], b4 = v0[e.z];
+        V3 a = V3{a4.x, a4.y, a4.z}, b = V3{b4.x, b4.y, b4.z};
+        bool visible;
+        if (fabsf(a.x - b.x) < 1e-3f && fabsf(a.y - b.y) < 1e-3f && fabsf(a.z - b.z) < 1e-3f) {
+            visible = false;
+        } else {
+            V3 d = normalized(b - a);
+            V3 o = nudge(a, d);
+            float target = magnitude(b - o);
+            TraceResult r = trace_ray<W, true>(s, o, d, target - 1e-3f, sref + threadIdx.x, stt + threadIdx.x,
+                                               blockDim.x, err);
+            visible = r.k < 0;
+        }
+        entries[e.x].w = visible ? E_VISIBLE : E_OCCLUDED;
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_bdpt_gather(DeviceScene s, BdptParams p,
+                                                       const uint32_t* __restrict__ vcount,
+                                                       const uint32_t* __restrict__ flags,
+                                                       const float4* __restrict__ escape,
+                                                       const uint32_t* __restrict__ entry_base,
+                                                       const float4* __restrict__ entries, float4* __restrict__ L_out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    uint32_t fl = flags[i];
+    V3 light = v3zero();
+    if (s.has_env && (fl & F_ESCAPE)) {
+        float4 e = escape[i];
+        light = light + mul(V3{e.x, e.y, e.z}, V3{s.env[0], s.env[1], s.env[2]});
+    }
+    if (!(fl & F_SKIP)) {
+        uint32_t cs = vcount[2 * i], ls = vcount[2 * i + 1];
+        uint32_t j = entry_base[i];
+        for (uint32_t c = 1; c <= cs; ++c) {
+            for (uint32_t l = 0; l <= ls; ++l) {
+                if (c + l > p.max_len) continue;
+                float4 e = entries[j++];
+                V3 term = (e.w == E_NO_TEST || e.w == E_VISIBLE) ? V3{e.x, e.y, e.z} : v3zero();
+                float w = 1.0f / static_cast<float>(c + l);
+                light = light + (term * w);
+            }
+        }
+    }
+    L_out[i] = make_float4(light.x, light.y, light.z, 0.0f);
+}
+
+__global__ void k_bdpt_samples_out(uint32_t n, const float2* __restrict__ st, const float4* __restrict__ L,
+                                   float* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[5 * i] = st[i].x;
+    out[5 * i + 1] = st[i].y;
+    out[5 * i + 2] = L[i].x;
+    out[5 * i + 3] = L[i].y;
+    out[5 * i + 4] = L[i].z;
+}
+
+uint32_t max_pairs(uint32_t max_len) { return max_len * (max_len + 1) / 2; }
+
+template <int W>
+gr_status shadow_launch(const DeviceScene& s, uint32_t cap, const uint32_t* count, const uint4* q, const float4* v0,
+                        float4* entries, int* err, unsigned long long* shadow_rays, cudaStream_t st) {
+    size_t smem = stack_smem_bytes(s.stack_depth, BLOCK);
+    GR_CUDA_TRY(
+        cudaFuncSetAttribute(k_bdpt_shadow<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int grid = resident_grid(k_bdpt_shadow<W>, smem, cap);
+    k_bdpt_shadow<W><<<grid, BLOCK, smem, st>>>(s, count, q, v0, entries, err, shadow_rays);
+    GR_CUDA_TRY(cudaGetLastError());
+    return GR_OK;
+}
+
+}  // namespace
+
+cudaError_t BdptState::ensure(size_t paths, uint32_t max_len) {
+    size_t slots = 2 * paths;
+    size_t pairs = static_cast<size_t>(max_pairs(max_len)) * paths;
+    cudaError_t e;
+    if ((e = verts.ensure(slots * max_len * VREC * sizeof(float4))) != cudaSuccess) return e;
+    if ((e = vcount.ensure(slots * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = flags.ensure(paths * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = escape.ensure(paths * sizeof(float4))) != cudaSuccess) return e;
+    if ((e = entry_base.ensure(paths * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = entries.ensure(pairs * sizeof(float4))) != cudaSuccess) return e;
+    if ((e = shadow.ensure(pairs * sizeof(uint4))) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
+    const gr_render_params& rp = job.params;
+    if (rp.mis || rp.light_tracing) {
+        set_error("BDPT: only the reference's uniform strategy weights are implemented (mis = 0, light_tracing = 0)");
+        return GR_ERR_UNSUPPORTED;
+    }
+    const uint32_t npix = job.width * job.height;
+    const uint32_t total = job.samples_out ? 1u : rp.spp;
+    if (total == 0) return GR_OK;
+    const uint32_t max_len = rp.max_depth ? rp.max_depth : 16;
+    const char* env = std::getenv("GR_BDPT_PATHS_IN_FLIGHT");
+    uint32_t target = env && std::atoi(env) > 0 ? static_cast<uint32_t>(std::atoi(env)) : (1u << 19);
+    uint32_t group = std::max(1u, std::min(total, target / std::max(1u, npix)));
+    const size_t npaths = static_cast<size_t>(group) * npix;
+    PathState& ps = sc->paths;
+    GR_CUDA_TRY(ps.ensure(2 * npaths));
+    GR_CUDA_TRY(sc->bdpt.ensure(npaths, max_len));
+    BdptState& bs = sc->bdpt;
+    uint32_t* cnt = ps.counters.as<uint32_t>();
+    int* err = reinterpret_cast<int*>(cnt + CNT_ERROR);
+    unsigned long long* rays = reinterpret_cast<unsigned long long*>(cnt + CNT_RAYS);
+    unsigned long long* shadow = reinterpret_cast<unsigned long long*>(cnt + CNT_SHADOW);
+    uint64_t launches = 0;
+
+    BdptParams p;
+    p.cam = job.camera;
+    p.width = job.width;
+    p.height = job.height;
+    p.npix = npix;
+    p.seed = rp.seed;
+    p.max_len = max_len;
+    p.rr_len = rp.rr_depth;
+    for (uint32_t done = 0; done < total; done += group) {
+        uint32_t g = std::min(group, total - done);
+        p.n = g * npix;
+        p.nslots = 2 * p.n;
+        p.first_pass = rp.first_pass + done;
+        Verts vs{bs.verts.as<float4>(), p.nslots};
+        GR_CUDA_TRY(cudaMemsetAsync(cnt + CNT_QUEUE0, 0, sizeof(uint32_t), st));
+        GR_CUDA_TRY(cudaMemsetAsync(cnt + CNT_ENTRIES, 0, 2 * sizeof(uint32_t), st));
+        k_bdpt_raygen<<<(p.n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(
+            job.scene, p, vs, bs.vcount.as<uint32_t>(), ps.tp.as<float4>(), bs.flags.as<uint32_t>(),
+            ps.key.as<unsigned long long>(), ps.st.as<float2>(), bs.escape.as<float4>(), cnt + CNT_QUEUE0,
+            ps.q_slot[0].as<uint32_t>(), ps.q_o[0].as<float4>(), ps.q_d[0].as<float4>());
+        GR_CUDA_TRY(cudaGetLastError());
+        ++launches;
+        // Every walk ends within max_len bounces (one vertex per bounce).
+        for (uint32_t depth = 0; depth < max_len; ++depth) {
+            int cur = depth & 1, nxt = cur ^ 1;
+            gr_status s1 = extend_any(job.scene, false, p.nslots, cnt + cur, ps.q_o[cur].as<float4>(),
+                                      ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(), err, rays, st);
+            if (s1 != GR_OK) return s1;
+            GR_CUDA_TRY(cudaGetLastError());
+            GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
+            int grid = resident_grid(k_bdpt_shade, 0, p.nslots);
+            k_bdpt_shade<<<grid, BLOCK, 0, st>>>(job.scene, p, vs, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
+                                                 ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
+                                                 ps.q_hit.as<float4>(), bs.vcount.as<uint32_t>(), ps.tp.as<float4>(),
+                                                 ps.key.as<unsigned long long>(), bs.flags.as<uint32_t>(),
+                                                 bs.escape.as<float4>(), cnt + nxt, ps.q_slot[nxt].as<uint32_t>(),
+                                                 ps.q_o[nxt].as<float4>(), ps.q_d[nxt].as<float4>());
+            GR_CUDA_TRY(cudaGetLastError());
+            launches += 2;
+        }
+        k_bdpt_connect<<<(p.n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(
+            job.scene, p, vs, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), cnt, bs.entry_base.as<uint32_t>(),
+            bs.entries.as<float4>(), bs.shadow.as<uint4>());
+        GR_CUDA_TRY(cudaGetLastError());
+        uint32_t cap = p.n * max_pairs(max_len);
+        gr_status s2;
+        switch (job.scene.width) {
+            case 2: s2 = shadow_launch<2>(job.scene, cap, cnt + CNT_SHADOWQ, bs.shadow.as<uint4>(),
+                                          bs.verts.as<float4>(), bs.entries.as<float4>(), err, shadow, st); break;
+            case 4: s2 = shadow_launch<4>(job.scene, cap, cnt + CNT_SHADOWQ, bs.shadow.as<uint4>(),
+                                          bs.verts.as<float4>(), bs.entries.as<float4>(), err, shadow, st); break;
+            default: s2 = shadow_launch<8>(job.scene, cap, cnt + CNT_SHADOWQ, bs.shadow.as<uint4>(),
+                                           bs.verts.as<float4>(), bs.entries.as<float4>(), err, shadow, st); break;
+        }
+        if (s2 != GR_OK) return s2;
+        k_bdpt_gather<<<(p.n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(
+            job.scene, p, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), bs.escape.as<float4>(),
+            bs.entry_base.as<uint32_t>(), bs.entries.as<float4>(), ps.light.as<float4>());
+        GR_CUDA_TRY(cudaGetLastError());
+        launches += 3;
+        if (job.film) {
+            gr_status s3 = film_gather(ps.st.as<float2>(), ps.light.as<float4>(), job.width, job.height, g, job.film,
+                                       st);
+            if (s3 != GR_OK) return s3;
+            ++launches;
+        }
+        if (job.samples_out) {
+            k_bdpt_samples_out<<<(p.n + 255) / 256, 256, 0, st>>>(p.n, ps.st.as<float2>(), ps.light.as<float4>(),
+                                                                 job.samples_out);
+            GR_CUDA_TRY(cudaGetLastError());
+            ++launches;
+        }
+    }
+    sc->stats.samples += static_cast<uint64_t>(total) * npix;
+    sc->stats.kernel_launches += launches;
+    return GR_OK;
 }
 
 }  // namespace gr

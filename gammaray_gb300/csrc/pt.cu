@@ -21,7 +21,7 @@
 #include <vector>
 
 #include "runtime.hpp"
-#include "traverse.cuh"
+#include "wavefront.cuh"
 
 #define GR_TRY_S(expr)                \
     do {                              \
@@ -32,8 +32,6 @@
 namespace gr {
 
 namespace {
-
-constexpr int BLOCK = 128;
 
 struct PTParams {
     DevCamera cam;
@@ -65,46 +63,6 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
     q_slot[i] = i;
     q_o[i] = make_float4(o.x, o.y, o.z, 0.0f);
     q_d[i] = make_float4(d.x, d.y, d.z, 0.0f);
-}
-
-template <int W, bool COUNT>
-__global__ void __launch_bounds__(BLOCK) k_extend(DeviceScene s, const uint32_t* __restrict__ count,
-                                                  const float4* __restrict__ q_o, const float4* __restrict__ q_d,
-                                                  float4* __restrict__ q_hit, int* err,
-                                                  unsigned long long* rays) {
-    extern __shared__ unsigned char smem[];
-    int32_t* sref = reinterpret_cast<int32_t*>(smem);
-    float* stt = reinterpret_cast<float*>(smem + sizeof(int32_t) * s.stack_depth * blockDim.x);
-    const uint32_t n = *count;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
-    uint32_t counts[2] = {0, 0};
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        float4 o4 = q_o[q], d4 = q_d[q];
-        TraceResult r = trace_ray<W, false, COUNT>(s, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX,
-                                                   sref + threadIdx.x, stt + threadIdx.x, blockDim.x, err, counts);
-        q_hit[q] = make_float4(r.t, __int_as_float(r.k), r.u, r.v);
-    }
-    if (COUNT && (counts[0] | counts[1])) {
-        atomicAdd(rays + (CNT_NODES - CNT_RAYS) / 2, static_cast<unsigned long long>(counts[0]));
-        atomicAdd(rays + (CNT_PRIMS - CNT_RAYS) / 2, static_cast<unsigned long long>(counts[1]));
-    }
-}
-
-GR_D void push_warp(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t* __restrict__ nslot,
-                    float4* __restrict__ no, float4* __restrict__ nd) {
-    const unsigned lane = threadIdx.x & 31;
-    unsigned m = __ballot_sync(0xffffffffu, alive);
-    if (!m) return;
-    int leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane == static_cast<unsigned>(leader)) base = atomicAdd(count_out, static_cast<uint32_t>(__popc(m)));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (alive) {
-        uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
-        nslot[pos] = slot;
-        no[pos] = make_float4(o.x, o.y, o.z, 0.0f);
-        nd[pos] = make_float4(d.x, d.y, d.z, 0.0f);
-    }
 }
 
 __global__ void __launch_bounds__(BLOCK) k_shade(DeviceScene s, PTParams p, uint32_t depth,
@@ -187,49 +145,6 @@ __global__ void k_samples_out(uint32_t n, const float2* __restrict__ st, const f
     out[5 * i + 2] = c.x;
     out[5 * i + 3] = c.y;
     out[5 * i + 4] = c.z;
-}
-
-template <class K>
-int resident_grid(K kernel, size_t smem, uint32_t n) {
-    static int sm = device_sm_count();
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    uint32_t need = (n + BLOCK - 1) / BLOCK;
-    uint32_t cap = static_cast<uint32_t>(sm * per_sm);
-    return static_cast<int>(std::max(1u, std::min(need, cap)));
-}
-
-template <int W, bool COUNT>
-gr_status extend_launch(const DeviceScene& s, uint32_t cap_n, const uint32_t* count, const float4* qo,
-                        const float4* qd, float4* qh, int* err, unsigned long long* rays, cudaStream_t st) {
-    size_t smem = stack_smem_bytes(s.stack_depth, BLOCK);
-    static size_t configured = 0;
-    if (smem > configured) {
-        GR_CUDA_TRY(cudaFuncSetAttribute(k_extend<W, COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem)));
-        configured = smem;
-    }
-    int grid = resident_grid(k_extend<W, COUNT>, smem, cap_n);
-    k_extend<W, COUNT><<<grid, BLOCK, smem, st>>>(s, count, qo, qd, qh, err, rays);
-    return GR_OK;
-}
-
-gr_status extend_any(const DeviceScene& s, bool count_traversal, uint32_t cap_n, const uint32_t* count,
-                     const float4* qo, const float4* qd, float4* qh, int* err, unsigned long long* rays,
-                     cudaStream_t st) {
-    if (count_traversal) {
-        switch (s.width) {
-            case 2: return extend_launch<2, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
-            case 4: return extend_launch<4, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
-            default: return extend_launch<8, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
-        }
-    }
-    switch (s.width) {
-        case 2: return extend_launch<2, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
-        case 4: return extend_launch<4, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
-        default: return extend_launch<8, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
-    }
 }
 
 uint32_t paths_in_flight_target() {
@@ -330,6 +245,7 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
                                                             ps.q_d[0].as<float4>());
         GR_CUDA_TRY(cudaGetLastError());
         ++launches;
+        GR_TRY_S(sync_check(st, "raygen", 0, n));
         for (uint32_t depth = 0;; ++depth) {
             if (p.max_depth && depth >= p.max_depth) break;
             int cur = depth & 1, nxt = cur ^ 1;
@@ -340,6 +256,7 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             if (s1 != GR_OK) return s1;
             GR_CUDA_TRY(cudaGetLastError());
             ++launches;
+            GR_TRY_S(sync_check(st, "extend", depth, n));
             if (timed) {
                 GR_TRY_S(mark(e1));
                 ext_pairs.emplace_back(e0, e1);
@@ -363,6 +280,7 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
                                             ps.q_d[nxt].as<float4>());
             GR_CUDA_TRY(cudaGetLastError());
             ++launches;
+            GR_TRY_S(sync_check(st, "shade", depth, n));
             if (timed) {
                 GR_TRY_S(mark(e1));
                 shade_pairs.emplace_back(e0, e1);

@@ -61,6 +61,12 @@ struct PathState {
     cudaError_t ensure(size_t n);
 };
 
+// BDPT vertex storage, strategy entries and the shadow queue (grown on demand).
+struct BdptState {
+    DevBuf verts, vcount, flags, escape, entry_base, entries, shadow;
+    cudaError_t ensure(size_t paths, uint32_t max_len);
+};
+
 constexpr int CNT_QUEUE0 = 0;
 constexpr int CNT_QUEUE1 = 1;
 constexpr int CNT_ERROR = 2;
@@ -82,6 +88,7 @@ struct gr_scene {
     gr::SceneBuffers buf;
     gr::DeviceScene dev{};
     gr::PathState paths;
+    gr::BdptState bdpt;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     gr_render_stats stats{};
@@ -128,6 +135,12 @@ gr_status film_exr_pack(const float4* film, uint32_t width, uint32_t height, uns
                         cudaStream_t s);
 
 int device_sm_count();
+
+// Bounded host wait (GR_SYNC_CHECK=<seconds> in the environment; 0 = off): after a
+// launch, polls the stream until it drains or the deadline passes.  On a timeout it
+// records which kernel and bounce did not finish and returns GR_ERR_TIMEOUT, so a stuck
+// kernel is reported instead of blocking the caller forever.
+gr_status sync_check(cudaStream_t st, const char* what, uint32_t bounce, uint32_t n);
 
 // Camera::new (core/camera.rs:42-61) evaluated on the host.
 DevCamera make_camera(const gr_camera& c);

@@ -189,3 +189,154 @@ inline size_t stack_smem_bytes(uint32_t stack_depth, int threads) {
 }
 
 }  // namespace gr
+
+namespace gr {
+
+// ---------------------------------------------------------------------------
+// Step-wise traversal for the persistent extension kernel.  The state of one ray lives
+// in registers; trav_step() processes one interior node or one leaf.  The stack keeps
+// its first SMEM_STACK entries in this thread's shared-memory column and spills deeper
+// entries to a per-thread local array (rarely touched, cached in L1), so the shared
+// footprint no longer scales with the tree's worst-case depth.
+constexpr int SMEM_STACK = 16;
+constexpr int MAX_STACK = 96;  // the build rejects trees whose worst case exceeds this
+
+struct TravState {
+    V3 o, d, inv;
+    float closest;
+    float hu, hv;
+    int32_t ref;
+    int32_t hit;
+    int sp;
+    bool nx, ny, nz;
+};
+
+GR_D void trav_init(TravState& t, V3 o, V3 d, float t_max) {
+    t.o = o;
+    t.d = d;
+    t.inv = V3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+    t.nx = d.x < 0.0f;
+    t.ny = d.y < 0.0f;
+    t.nz = d.z < 0.0f;
+    t.closest = t_max;
+    t.hu = t.hv = 0.0f;
+    t.ref = 0;
+    t.hit = -1;
+    t.sp = 0;
+}
+
+struct StackView {
+    int32_t* sref;  // this thread's shared column (stride = blockDim.x)
+    float* st;
+    int stride;
+    int2* spill;    // local overflow, MAX_STACK - SMEM_STACK entries
+    GR_D void push(int sp, int32_t ref, float te) const {
+        if (sp < SMEM_STACK) {
+            sref[sp * stride] = ref;
+            st[sp * stride] = te;
+        } else {
+            spill[sp - SMEM_STACK] = make_int2(ref, __float_as_int(te));
+        }
+    }
+    GR_D void pop(int sp, int32_t& ref, float& te) const {
+        if (sp < SMEM_STACK) {
+            ref = sref[sp * stride];
+            te = st[sp * stride];
+        } else {
+            int2 e = spill[sp - SMEM_STACK];
+            ref = e.x;
+            te = __int_as_float(e.y);
+        }
+    }
+};
+
+// One traversal step.  Returns true when the ray is finished (t.hit / t.closest hold
+// the closest hit).  With ANY_HIT it finishes at the first hit closer than t_max.
+template <int W, bool ANY_HIT, bool COUNT>
+GR_D bool trav_step(const DeviceScene& s, TravState& t, const StackView& stk, int* err, uint32_t* counts) {
+    const float inflate = 1.0f + 2.0f * gamma_n(3.0f);
+    if (t.ref >= 0) {
+        if (COUNT) counts[0] += 1;
+        const float4* nb = s.nodes + static_cast<size_t>(t.ref) * (2 * W);
+        float f[8 * W];
+#pragma unroll
+        for (int q = 0; q < 2 * W; ++q) {
+            float4 x = __ldg(nb + q);
+            f[4 * q] = x.x;
+            f[4 * q + 1] = x.y;
+            f[4 * q + 2] = x.z;
+            f[4 * q + 3] = x.w;
+        }
+        uint32_t key[W];
+        int h = 0;
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+            float lx = f[0 * W + j], ly = f[1 * W + j], lz = f[2 * W + j];
+            float hx = f[3 * W + j], hy = f[4 * W + j], hz = f[5 * W + j];
+            float t0x = ((t.nx ? hx : lx) - t.o.x) * t.inv.x;
+            float t1x = ((t.nx ? lx : hx) - t.o.x) * t.inv.x;
+            float t0y = ((t.ny ? hy : ly) - t.o.y) * t.inv.y;
+            float t1y = ((t.ny ? ly : hy) - t.o.y) * t.inv.y;
+            float t0z = ((t.nz ? hz : lz) - t.o.z) * t.inv.z;
+            float t1z = ((t.nz ? lz : hz) - t.o.z) * t.inv.z;
+            float tmin = fmaxf(fmaxf(t0x, t0y), t0z);
+            float tmax = fminf(fminf(t1x, t1y), t1z) * inflate;
+            bool hit = tmin <= tmax && tmin < t.closest && tmax > 0.0f;
+            float te = fmaxf(tmin, 0.0f);
+            key[j] = hit ? ((__float_as_uint(te) & ~7u) | static_cast<uint32_t>(j)) : 0xFFFFFFFFu;
+            h += hit ? 1 : 0;
+        }
+        if (h > 0) {
+            sort_keys<W>(key);
+            if (t.sp + h - 1 > MAX_STACK) {
+                *err = 1;
+                t.hit = -1;
+                return true;
+            }
+#pragma unroll
+            for (int j = W - 1; j >= 1; --j) {
+                if (j < h) {
+                    stk.push(t.sp, select_child<W>(f, key[j] & 7u), __uint_as_float(key[j] & ~7u));
+                    ++t.sp;
+                }
+            }
+            t.ref = select_child<W>(f, key[0] & 7u);
+            return false;
+        }
+    } else {
+        uint32_t enc = ~static_cast<uint32_t>(t.ref);
+        uint32_t first = enc >> LEAF_COUNT_BITS;
+        uint32_t count = (enc & (MAX_LEAF_PRIMS - 1)) + 1;
+        if (COUNT) counts[1] += count;
+        for (uint32_t k = first; k < first + count; ++k) {
+            const float4* pr = s.prims + 3 * static_cast<size_t>(k);
+            float4 p0 = __ldg(pr), p1 = __ldg(pr + 1), p2 = __ldg(pr + 2);
+            float u, v;
+            float dist = intersect_prim(p0, p1, p2, t.o, t.d, u, v);
+            if (dist != 0.0f && dist < t.closest) {
+                t.closest = dist;
+                t.hit = static_cast<int32_t>(k);
+                t.hu = u;
+                t.hv = v;
+                if (ANY_HIT) return true;
+            }
+        }
+    }
+    while (t.sp > 0) {
+        --t.sp;
+        int32_t r;
+        float te;
+        stk.pop(t.sp, r, te);
+        if (te < t.closest) {
+            t.ref = r;
+            return false;
+        }
+    }
+    return true;
+}
+
+inline size_t step_stack_smem_bytes(int threads) {
+    return static_cast<size_t>(SMEM_STACK) * threads * (sizeof(int32_t) + sizeof(float));
+}
+
+}  // namespace gr

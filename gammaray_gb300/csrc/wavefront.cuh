@@ -1,0 +1,112 @@
+// Pieces shared by the wavefront integrators (pt.cu, bdpt.cu): the extension kernel
+// over a compacted ray queue, the warp-aggregated queue push and grid sizing.
+#pragma once
+
+#include <algorithm>
+#include <cstdlib>
+
+#include "runtime.hpp"
+#include "traverse.cuh"
+
+namespace gr {
+namespace {
+
+constexpr int BLOCK = 128;
+
+// Closest hit for every queued ray: a grid-stride loop over the device-side count, so
+// launches never depend on a host read of the queue length.  Each thread traverses one
+// ray at a time with the step function and the shared/local hybrid stack; a ray that
+// needs more steps than the tree could ever require is abandoned and flagged (err = 2).
+template <int W, bool COUNT>
+__global__ void __launch_bounds__(BLOCK) k_extend(DeviceScene s, const uint32_t* __restrict__ count,
+                                                     const float4* __restrict__ q_o, const float4* __restrict__ q_d,
+                                                     float4* __restrict__ q_hit, int* err,
+                                                     unsigned long long* rays) {
+    extern __shared__ unsigned char smem[];
+    int32_t* sref = reinterpret_cast<int32_t*>(smem);
+    float* stt = reinterpret_cast<float*>(smem + sizeof(int32_t) * SMEM_STACK * blockDim.x);
+    int2 spill[MAX_STACK - SMEM_STACK];
+    StackView stk{sref + threadIdx.x, stt + threadIdx.x, static_cast<int>(blockDim.x), spill};
+    const uint32_t n = *count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
+    uint32_t counts[2] = {0, 0};
+    const uint32_t budget = 8u * s.num_components + 4096u;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        float4 o4 = q_o[q], d4 = q_d[q];
+        TravState t;
+        trav_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX);
+        uint32_t steps = 0;
+        while (!trav_step<W, false, COUNT>(s, t, stk, err, counts)) {
+            if (++steps > budget) {
+                atomicExch(err, 2);
+                atomicExch(err + 1, static_cast<int>(q));
+                t.hit = -1;
+                break;
+            }
+        }
+        q_hit[q] = make_float4(t.closest, __int_as_float(t.hit), t.hu, t.hv);
+    }
+    if (COUNT && (counts[0] | counts[1])) {
+        atomicAdd(rays + (CNT_NODES - CNT_RAYS) / 2, static_cast<unsigned long long>(counts[0]));
+        atomicAdd(rays + (CNT_PRIMS - CNT_RAYS) / 2, static_cast<unsigned long long>(counts[1]));
+    }
+}
+
+// Appends this lane's ray to the next queue with one atomic per warp (ballot + popc).
+// Every lane of the warp must call it (warp-uniform trip counts).
+GR_D void push_warp(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t* __restrict__ nslot,
+                    float4* __restrict__ no, float4* __restrict__ nd) {
+    const unsigned lane = threadIdx.x & 31;
+    unsigned m = __ballot_sync(0xffffffffu, alive);
+    if (!m) return;
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == static_cast<unsigned>(leader)) base = atomicAdd(count_out, static_cast<uint32_t>(__popc(m)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (alive) {
+        uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
+        nslot[pos] = slot;
+        no[pos] = make_float4(o.x, o.y, o.z, 0.0f);
+        nd[pos] = make_float4(d.x, d.y, d.z, 0.0f);
+    }
+}
+
+template <class K>
+int resident_grid(K kernel, size_t smem, uint32_t n) {
+    static int sm = device_sm_count();
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    uint32_t need = (n + BLOCK - 1) / BLOCK;
+    uint32_t cap = static_cast<uint32_t>(sm * per_sm);
+    return static_cast<int>(std::max(1u, std::min(need, cap)));
+}
+
+template <int W, bool COUNT>
+gr_status extend_launch(const DeviceScene& s, uint32_t cap_n, const uint32_t* count, const float4* qo,
+                        const float4* qd, float4* qh, int* err, unsigned long long* rays, cudaStream_t st) {
+    size_t smem = step_stack_smem_bytes(BLOCK);
+    int grid = resident_grid(k_extend<W, COUNT>, smem, cap_n);
+    k_extend<W, COUNT><<<grid, BLOCK, smem, st>>>(s, count, qo, qd, qh, err, rays);
+    return GR_OK;
+}
+
+gr_status extend_any(const DeviceScene& s, bool count_traversal, uint32_t cap_n, const uint32_t* count,
+                     const float4* qo, const float4* qd, float4* qh, int* err, unsigned long long* rays,
+                     cudaStream_t st) {
+    if (count_traversal) {
+        switch (s.width) {
+            case 2: return extend_launch<2, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
+            case 4: return extend_launch<4, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
+            default: return extend_launch<8, true>(s, cap_n, count, qo, qd, qh, err, rays, st);
+        }
+    }
+    switch (s.width) {
+        case 2: return extend_launch<2, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
+        case 4: return extend_launch<4, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
+        default: return extend_launch<8, false>(s, cap_n, count, qo, qd, qh, err, rays, st);
+    }
+}
+
+}  // namespace
+}  // namespace gr

@@ -223,3 +223,54 @@ def test_exr_matches_oracle(gpu, oracle, tmp_path):
         out.append((tmp_path / name).read_bytes())
     assert len(out[0]) == len(out[1])
     assert out[0][:400] == out[1][:400]  # header and offset table identical
+
+
+@pytest.mark.parametrize("scene", ["cornell", "displaced", "displaced_env_spheres", "no_lights"])
+def test_bdpt_samples_per_path(gpu, oracle, scene):
+    if scene == "cornell":
+        w = scenes.cornell_spheres(40, 40, 1)
+        prims, env, integ = w.prims, w.environment, g.BdptIntegrator()
+    elif scene == "displaced":
+        w = scenes.displaced_sphere(40, 40, 1, bdpt=True)
+        prims, env, integ = w.prims, (0, 0, 0), w.integrator
+    elif scene == "displaced_env_spheres":
+        w = scenes.displaced_sphere(40, 40, 1, bdpt=True, tris=20_000)
+        prims = w.prims + [g.Sphere(g.Material.diffuse_light((3, 3, 3)), g.Mat.translation((1.5, 1.0, 0)), 0.3),
+                           g.Sphere(g.Material.mirror(), g.Mat.translation((-1.5, -0.6, 0.5)), 0.5)]
+        env, integ = w.environment, w.integrator
+    else:
+        w = scenes.cornell_spheres(40, 40, 1)
+        prims = [p for p in w.prims if not p.material.has_light()]
+        env, integ = (0.5, 0.5, 0.5), g.BdptIntegrator(max_depth=8)
+    sg = g.Stage(prims, lib=gpu, environment=env, seed=21)
+    so = g.Stage(prims, lib=oracle, environment=env, seed=21)
+    for pass_index in (0, 5):
+        a = sg.samples(w.camera, integ, 40, 40, pass_index)
+        b = so.samples(w.camera, integ, 40, 40, pass_index)
+        np.testing.assert_array_equal(a[..., :2], b[..., :2])
+        close = np.isclose(a[..., 2:], b[..., 2:], rtol=1e-4, atol=1e-5).all(axis=-1)
+        assert close.mean() >= 0.99, f"{scene}: {close.mean():.4f} of paths agree"
+        assert np.isfinite(a[..., 2:]).all()
+
+
+def test_bdpt_image_statistics(gpu, oracle):
+    w = scenes.cornell_spheres(48, 48, 8)
+    imgs = []
+    for L in (gpu, oracle):
+        st = g.Stage(w.prims, lib=L, seed=6)
+        f = g.Film(48, 48, lib=L)
+        st.render(w.camera, g.BdptIntegrator(), f, 8)
+        imgs.append(f.resolve())
+    a, b = imgs
+    rel_mse = float(np.mean((a - b) ** 2) / np.mean(b ** 2))
+    assert rel_mse < 1e-3, rel_mse
+    assert gpu.backend == "cuda-sm_103a"
+
+
+def test_bdpt_counts_shadow_rays(gpu):
+    w = scenes.cornell_spheres(32, 32, 2)
+    st = g.Stage(w.prims, lib=gpu, seed=1)
+    f = g.Film(32, 32, lib=gpu)
+    st.render(w.camera, g.BdptIntegrator(), f, 2)
+    s = st.last_stats()
+    assert s.samples == 2 * 32 * 32 and s.extension_rays > s.samples and s.shadow_rays > 0
