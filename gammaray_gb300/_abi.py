@@ -229,7 +229,13 @@ class BatchOptions(C.Structure):
 
 
 class ServerOptions(C.Structure):
-    _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_active", C.c_uint32), ("path_capacity", C.c_uint32)]
+    _fields_ = [
+        ("memory_budget_bytes", C.c_uint64),
+        ("max_active", C.c_uint32),
+        ("path_capacity", C.c_uint32),
+        ("bvh_width", C.c_uint32),
+        ("block_size", C.c_uint32),
+    ]
 
 
 class Request(C.Structure):
@@ -298,6 +304,8 @@ SIGNATURES = {
     ),
     "gr_light_eval": (C.c_int, [C.POINTER(MaterialDesc), C.c_uint64, C.POINTER(Frame), _PF, _PF]),
     "gr_render_batch": (C.c_int, [C.POINTER(Job), C.c_uint32, C.POINTER(BatchOptions)]),
+    "gr_batch_autotune": (C.c_int, [C.POINTER(Job), C.c_uint32, C.POINTER(BatchOptions)]),
+    "gr_batch_last_stats": (C.c_int, [C.POINTER(RenderStats)]),
     "gr_server_create": (C.c_int, [C.POINTER(ServerOptions), C.POINTER(_VP)]),
     "gr_server_destroy": (C.c_int, [_VP]),
     "gr_server_submit": (C.c_int, [_VP, C.POINTER(Request), C.POINTER(C.c_uint64)]),

@@ -1,32 +1,481 @@
-// Batched rendering and the serving loop.
-#include "runtime.hpp"
+// Batched rendering and the serving loop over the multi-job engine (engine.hpp).
+// Neither has a counterpart in the reference, which renders one image per
+// Stage::trace call (render/stage.rs:23-36).
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "engine.hpp"
 
 using namespace gr;
 
-extern "C" {
+namespace {
 
-gr_status gr_render_batch(const gr_job* jobs, uint32_t n, const gr_batch_options*) {
-    if (n && !jobs) {
-        set_error("null jobs");
+thread_local gr_render_stats g_batch_stats{};
+
+// Engines are costly to set up (about 0.5 GB of buffers and a captured graph), so one
+// per configuration is kept and reset between batches.
+std::mutex g_cache_mu;
+std::map<std::tuple<int, uint32_t, uint32_t, uint32_t>, std::unique_ptr<Engine>> g_cache;
+
+gr_status cached_engine(const EngineConfig& cfg, Engine*& out) {
+    int dev = 0;
+    GR_CUDA_TRY(cudaGetDevice(&dev));
+    auto key = std::make_tuple(dev, cfg.capacity, cfg.width, cfg.block);
+    auto it = g_cache.find(key);
+    if (it == g_cache.end()) {
+        std::unique_ptr<Engine> e(new Engine());
+        gr_status s = e->init(cfg, nullptr);
+        if (s != GR_OK) return s;
+        it = g_cache.emplace(key, std::move(e)).first;
+    } else {
+        gr_status s = it->second->reset();
+        if (s != GR_OK) return s;
+    }
+    out = it->second.get();
+    return GR_OK;
+}
+
+gr_status check_job(const gr_job& j) {
+    if (!j.scene || !j.film) {
+        set_error("batch job with a null scene or film");
         return GR_ERR_INVALID_ARGUMENT;
     }
-    for (uint32_t i = 0; i < n; ++i) {
-        gr_status s = gr_render(jobs[i].scene, &jobs[i].camera, &jobs[i].params, jobs[i].film);
-        if (s != GR_OK) return s;
+    if (j.params.integrator < 0 || j.params.integrator > 2) {
+        set_error("batch job with an unknown integrator");
+        return GR_ERR_INVALID_ARGUMENT;
     }
     return GR_OK;
 }
 
-static gr_status unsupported() {
-    set_error("serving is not built yet");
-    return GR_ERR_UNSUPPORTED;
+// Runs PT / display-colour jobs of one BVH width through one engine; units are issued
+// round-robin over jobs, pass by pass.
+gr_status run_engine_batch(const std::vector<const gr_job*>& jobs, const EngineConfig& cfg, gr_render_stats& st,
+                           float4* const* films_override) {
+    Engine* e = nullptr;
+    gr_status s = cached_engine(cfg, e);
+    if (s != GR_OK) return s;
+    uint32_t max_spp = 0;
+    std::vector<uint32_t> idx(jobs.size());
+    for (size_t k = 0; k < jobs.size(); ++k) {
+        const gr_job& j = *jobs[k];
+        float4* film = films_override ? films_override[k] : j.film->pixels.as<float4>();
+        DevJob dj = make_job(j.scene, j.camera, j.params, j.film->width, j.film->height, film);
+        s = e->add_job(dj, 0, 0, idx[k]);
+        if (s != GR_OK) return s;
+        max_spp = std::max(max_spp, j.params.spp);
+    }
+    std::vector<std::pair<uint32_t, uint32_t>> units;
+    for (uint32_t r = 0; r < max_spp; ++r)
+        for (size_t k = 0; k < jobs.size(); ++k)
+            if (r < jobs[k]->params.spp) units.emplace_back(idx[k], jobs[k]->params.first_pass + r);
+    s = e->append_units(units);
+    if (s != GR_OK) return s;
+    cudaEvent_t a, b;
+    GR_CUDA_TRY(cudaEventCreate(&a));
+    GR_CUDA_TRY(cudaEventCreate(&b));
+    GR_CUDA_TRY(cudaEventRecord(a, e->stream()));
+    bool done = false;
+    s = e->run(0xFFFFFFFFu, done);
+    GR_CUDA_TRY(cudaEventRecord(b, e->stream()));
+    GR_CUDA_TRY(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (s != GR_OK) return s;
+    EngineCtl c;
+    s = e->read_ctl(c);
+    if (s != GR_OK) return s;
+    st.samples += c.samples_done;
+    st.extension_rays += c.rays;
+    st.kernel_launches += static_cast<uint64_t>(c.iter) * 6;
+    st.device_ms += ms;
+    if (!done) {
+        set_error("batch did not complete");
+        return GR_ERR_INTERNAL;
+    }
+    return GR_OK;
 }
-gr_status gr_server_create(const gr_server_options*, gr_server**) { return unsupported(); }
-gr_status gr_server_destroy(gr_server*) { return unsupported(); }
-gr_status gr_server_submit(gr_server*, const gr_request*, uint64_t*) { return unsupported(); }
-gr_status gr_server_step(gr_server*, double) { return unsupported(); }
-gr_status gr_server_poll(gr_server*, uint64_t, gr_request_status*) { return unsupported(); }
-gr_status gr_server_cancel(gr_server*, uint64_t) { return unsupported(); }
-gr_status gr_server_take(gr_server*, uint64_t, float*, float*) { return unsupported(); }
+
+EngineConfig config_from(const gr_batch_options* o, uint32_t width) {
+    EngineConfig cfg;
+    cfg.width = width;
+    if (o && o->path_capacity) cfg.capacity = o->path_capacity;
+    if (o && o->block_size) cfg.block = o->block_size;
+    return cfg;
+}
+
+}  // namespace
+
+extern "C" {
+
+gr_status gr_render_batch(const gr_job* jobs, uint32_t n, const gr_batch_options* options) {
+    if (n && !jobs) {
+        set_error("null jobs");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    g_batch_stats = gr_render_stats{};
+    std::map<uint32_t, std::vector<const gr_job*>> by_width;
+    std::vector<const gr_job*> sequential;
+    for (uint32_t i = 0; i < n; ++i) {
+        gr_status s = check_job(jobs[i]);
+        if (s != GR_OK) return s;
+        if (jobs[i].params.integrator == GR_INTEGRATOR_BDPT) sequential.push_back(&jobs[i]);
+        else by_width[jobs[i].scene->dev.width].push_back(&jobs[i]);
+    }
+    for (auto& kv : by_width) {
+        gr_status s = run_engine_batch(kv.second, config_from(options, kv.first), g_batch_stats, nullptr);
+        if (s != GR_OK) return s;
+        for (const gr_job* j : kv.second) j->film->passes += j->params.spp;
+    }
+    // BDPT keeps its own per-image wavefront.
+    for (const gr_job* j : sequential) {
+        gr_status s = gr_render(j->scene, &j->camera, &j->params, j->film);
+        if (s != GR_OK) return s;
+        g_batch_stats.samples += j->scene->stats.samples;
+        g_batch_stats.extension_rays += j->scene->stats.extension_rays;
+        g_batch_stats.shadow_rays += j->scene->stats.shadow_rays;
+        g_batch_stats.device_ms += j->scene->stats.device_ms;
+    }
+    return GR_OK;
+}
+
+gr_status gr_batch_last_stats(gr_render_stats* out) {
+    if (!out) {
+        set_error("null argument");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    *out = g_batch_stats;
+    return GR_OK;
+}
+
+gr_status gr_batch_autotune(const gr_job* jobs, uint32_t n, gr_batch_options* out) {
+    if (!out || (n && !jobs)) {
+        set_error("null argument");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    // Trial: the first two passes of up to 32 path-tracer jobs of the most common width,
+    // rendered into scratch films.
+    std::map<uint32_t, std::vector<const gr_job*>> by_width;
+    for (uint32_t i = 0; i < n; ++i) {
+        gr_status s = check_job(jobs[i]);
+        if (s != GR_OK) return s;
+        if (jobs[i].params.integrator != GR_INTEGRATOR_BDPT) by_width[jobs[i].scene->dev.width].push_back(&jobs[i]);
+    }
+    std::memset(out, 0, sizeof(*out));
+    out->use_graph = 1;
+    if (by_width.empty()) return GR_OK;
+    auto best_w = std::max_element(by_width.begin(), by_width.end(),
+                                   [](auto& a, auto& b) { return a.second.size() < b.second.size(); });
+    std::vector<gr_job> trial;
+    for (size_t k = 0; k < best_w->second.size() && k < 32; ++k) {
+        gr_job j = *best_w->second[k];
+        j.params.spp = std::min<uint32_t>(j.params.spp, 2);
+        trial.push_back(j);
+    }
+    std::vector<DevBuf> films(trial.size());
+    std::vector<float4*> fp(trial.size());
+    for (size_t k = 0; k < trial.size(); ++k) {
+        size_t bytes = static_cast<size_t>(trial[k].film->width) * trial[k].film->height * sizeof(float4);
+        GR_CUDA_TRY(films[k].ensure(bytes));
+        GR_CUDA_TRY(cudaMemset(films[k].ptr, 0, bytes));
+        fp[k] = films[k].as<float4>();
+    }
+    std::vector<const gr_job*> tj;
+    for (auto& j : trial) tj.push_back(&j);
+    double best = 0.0;
+    for (uint32_t cap : {1u << 20, 1u << 21, 1u << 22}) {
+        for (uint32_t bs : {64u, 128u, 256u}) {
+            EngineConfig cfg;
+            cfg.width = best_w->first;
+            cfg.capacity = cap;
+            cfg.block = bs;
+            gr_render_stats st{};
+            gr_status s = run_engine_batch(tj, cfg, st, fp.data());  // warm (engine set-up)
+            if (s != GR_OK) return s;
+            st = gr_render_stats{};
+            s = run_engine_batch(tj, cfg, st, fp.data());
+            if (s != GR_OK) return s;
+            double rate = st.device_ms > 0 ? st.samples / st.device_ms : 0.0;
+            if (rate > best) {
+                best = rate;
+                out->path_capacity = cap;
+                out->block_size = bs;
+            }
+        }
+    }
+    return GR_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------ serving
+
+struct ServerRequest {
+    uint64_t id;
+    gr_request req;
+    int32_t state;
+    DevBuf film;
+    uint32_t job = 0;
+    uint32_t appended = 0;  // passes appended to the engine so far
+    std::vector<uint32_t> units;  // engine unit indices, in pass order
+    uint32_t passes_done = 0;
+    double submit_ms = 0, start_ms = 0, finish_ms = 0;
+    uint64_t bytes = 0;
+};
+
+struct gr_server {
+    std::mutex mu;
+    Engine engine;
+    gr_server_options opts{};
+    uint64_t budget = 0, used = 0;
+    uint64_t next_id = 1;
+    std::vector<std::unique_ptr<ServerRequest>> reqs;
+    std::chrono::steady_clock::time_point t0;
+    double now_ms() const {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    ServerRequest* find(uint64_t id) {
+        for (auto& r : reqs)
+            if (r->id == id) return r.get();
+        return nullptr;
+    }
+};
+
+namespace {
+
+// Admits queued requests while films fit the budget, then tops up the engine's unit
+// backlog one pass per running request at a time (continuous batching: a request that
+// arrives joins the rotation at the next top-up).
+gr_status schedule(gr_server* s) {
+    uint32_t active = 0;
+    for (auto& r : s->reqs) active += r->state == GR_REQUEST_RUNNING ? 1 : 0;
+    for (auto& r : s->reqs) {
+        if (r->state != GR_REQUEST_QUEUED) continue;
+        if (s->opts.max_active && active >= s->opts.max_active) break;
+        if (s->used + r->bytes > s->budget) break;  // admission by free device memory, in arrival order
+        gr_status st;
+        GR_CUDA_TRY(r->film.ensure(r->bytes));
+        GR_CUDA_TRY(cudaMemset(r->film.ptr, 0, r->bytes));
+        DevJob dj = make_job(r->req.scene, r->req.camera, r->req.params, r->req.width, r->req.height,
+                             r->film.as<float4>());
+        st = s->engine.add_job(dj, 0, 0, r->job);
+        if (st != GR_OK) return st;
+        s->used += r->bytes;
+        r->state = GR_REQUEST_RUNNING;
+        r->start_ms = s->now_ms();
+        ++active;
+    }
+    // Keep about two pools' worth of paths appended but not yet issued.
+    EngineCtl c;
+    gr_status st = s->engine.read_ctl(c);
+    if (st != GR_OK) return st;
+    uint64_t backlog = c.paths_total - c.gcur;
+    const uint64_t want = 2ull * s->engine.capacity();
+    while (backlog < want) {
+        std::vector<std::pair<uint32_t, uint32_t>> round;
+        std::vector<ServerRequest*> owners;
+        for (auto& r : s->reqs) {
+            if (r->state != GR_REQUEST_RUNNING || r->appended >= r->req.params.spp) continue;
+            round.emplace_back(r->job, r->req.params.first_pass + r->appended);
+            owners.push_back(r.get());
+        }
+        if (round.empty()) break;
+        size_t first = s->engine.units().size();
+        st = s->engine.append_units(round);
+        if (st != GR_OK) return st;
+        for (size_t k = 0; k < owners.size(); ++k) {
+            owners[k]->units.push_back(static_cast<uint32_t>(first + k));
+            owners[k]->appended += 1;
+            backlog += owners[k]->req.width * owners[k]->req.height;
+        }
+    }
+    return GR_OK;
+}
+
+// Marks passes gathered (every unit below the engine's g_lo is in its film).
+gr_status progress(gr_server* s) {
+    EngineCtl c;
+    gr_status st = s->engine.read_ctl(c);
+    if (st != GR_OK) return st;
+    for (auto& r : s->reqs) {
+        if (r->state != GR_REQUEST_RUNNING) continue;
+        uint32_t d = 0;
+        for (uint32_t u : r->units) d += u < c.g_lo ? 1 : 0;
+        r->passes_done = d;
+        if (d == r->req.params.spp) {
+            r->state = GR_REQUEST_DONE;
+            r->finish_ms = s->now_ms();
+        }
+    }
+    return GR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gr_status gr_server_create(const gr_server_options* o, gr_server** out) {
+    if (!out) {
+        set_error("null argument");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::unique_ptr<gr_server> s(new gr_server());
+    if (o) s->opts = *o;
+    EngineConfig cfg;
+    cfg.capacity = s->opts.path_capacity ? s->opts.path_capacity : (1u << 21);
+    cfg.width = s->opts.bvh_width ? s->opts.bvh_width : 4;
+    cfg.block = s->opts.block_size ? s->opts.block_size : 128;
+    gr_status st = s->engine.init(cfg, nullptr);
+    if (st != GR_OK) return st;
+    size_t free_b = 0, total_b = 0;
+    GR_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    s->budget = s->opts.memory_budget_bytes ? s->opts.memory_budget_bytes : static_cast<uint64_t>(0.9 * free_b);
+    s->t0 = std::chrono::steady_clock::now();
+    *out = s.release();
+    return GR_OK;
+}
+
+gr_status gr_server_destroy(gr_server* s) {
+    delete s;
+    return GR_OK;
+}
+
+gr_status gr_server_submit(gr_server* s, const gr_request* r, uint64_t* id) {
+    if (!s || !r || !id || !r->scene || r->width == 0 || r->height == 0) {
+        set_error("bad request");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    if (r->params.integrator == GR_INTEGRATOR_BDPT) {
+        set_error("the serving loop runs the path tracer and the display-colour integrator");
+        return GR_ERR_UNSUPPORTED;
+    }
+    if (r->scene->dev.width != s->engine.config().width) {
+        set_error("request scene has a different BVH width than the server");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    std::unique_ptr<ServerRequest> q(new ServerRequest());
+    q->id = s->next_id++;
+    q->req = *r;
+    q->state = r->params.spp ? GR_REQUEST_QUEUED : GR_REQUEST_DONE;
+    q->bytes = static_cast<uint64_t>(r->width) * r->height * sizeof(float4);
+    q->submit_ms = s->now_ms();
+    if (q->bytes > s->budget) {
+        set_error("request film exceeds the server's memory budget");
+        return GR_ERR_OUT_OF_MEMORY;
+    }
+    *id = q->id;
+    s->reqs.push_back(std::move(q));
+    return GR_OK;
+}
+
+gr_status gr_server_step(gr_server* s, double budget_ms) {
+    if (!s) {
+        set_error("null server");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    double t_end = s->now_ms() + budget_ms;
+    for (;;) {
+        gr_status st = schedule(s);
+        if (st != GR_OK) return st;
+        bool any = false;
+        for (auto& r : s->reqs) any |= r->state == GR_REQUEST_RUNNING;
+        if (!any) return GR_OK;
+        bool done = false;
+        st = s->engine.run(4, done);
+        if (st != GR_OK) return st;
+        st = progress(s);
+        if (st != GR_OK) return st;
+        if (s->now_ms() >= t_end) return GR_OK;
+    }
+}
+
+gr_status gr_server_poll(gr_server* s, uint64_t id, gr_request_status* out) {
+    if (!s || !out) {
+        set_error("null argument");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    ServerRequest* r = s->find(id);
+    if (!r) {
+        set_error("no such request");
+        return GR_ERR_NOT_FOUND;
+    }
+    out->state = r->state;
+    out->passes_done = r->passes_done;
+    out->submit_ms = r->submit_ms;
+    out->start_ms = r->start_ms;
+    out->finish_ms = r->finish_ms;
+    return GR_OK;
+}
+
+gr_status gr_server_cancel(gr_server* s, uint64_t id) {
+    if (!s) {
+        set_error("null server");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    ServerRequest* r = s->find(id);
+    if (!r) {
+        set_error("no such request");
+        return GR_ERR_NOT_FOUND;
+    }
+    if (r->state == GR_REQUEST_RUNNING) {
+        gr_status st = s->engine.cancel_job(r->job);
+        if (st != GR_OK) return st;
+        // Its appended units still drain (paths die on their next shade; the gather
+        // skips the film); no further passes are appended.
+        r->req.params.spp = r->appended;
+    }
+    if (r->state == GR_REQUEST_QUEUED || r->state == GR_REQUEST_RUNNING) {
+        r->state = GR_REQUEST_CANCELLED;
+        r->finish_ms = s->now_ms();
+    }
+    return GR_OK;
+}
+
+gr_status gr_server_take(gr_server* s, uint64_t id, float* accum, float* weight) {
+    if (!s) {
+        set_error("null server");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    for (size_t k = 0; k < s->reqs.size(); ++k) {
+        ServerRequest* r = s->reqs[k].get();
+        if (r->id != id) continue;
+        if (r->state != GR_REQUEST_DONE && r->state != GR_REQUEST_CANCELLED) {
+            set_error("request not finished");
+            return GR_ERR_BUSY;
+        }
+        size_t n = static_cast<size_t>(r->req.width) * r->req.height;
+        if (r->film.ptr && (accum || weight)) {
+            std::vector<float4> px(n);
+            GR_CUDA_TRY(cudaMemcpy(px.data(), r->film.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < n; ++i) {
+                if (accum) {
+                    accum[3 * i] = px[i].x;
+                    accum[3 * i + 1] = px[i].y;
+                    accum[3 * i + 2] = px[i].z;
+                }
+                if (weight) weight[i] = px[i].w;
+            }
+        }
+        if (r->film.ptr) s->used -= r->bytes;
+        s->reqs.erase(s->reqs.begin() + static_cast<long>(k));
+        return GR_OK;
+    }
+    set_error("no such request");
+    return GR_ERR_NOT_FOUND;
+}
 
 }  // extern "C"

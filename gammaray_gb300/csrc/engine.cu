@@ -1,0 +1,609 @@
+// Multi-job wavefront engine (see engine.hpp): kernels, graph capture and host driver.
+#include <algorithm>
+#include <cstring>
+
+#include "engine.hpp"
+#include "film_gather.cuh"
+#include "traverse.cuh"
+
+namespace gr {
+
+namespace {
+
+constexpr int EBLOCK = 128;
+constexpr int GATHER_BLOCKS = 512;
+
+GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t job,
+                   uint32_t* __restrict__ nslot, float4* __restrict__ no, float4* __restrict__ nd) {
+    const unsigned lane = threadIdx.x & 31;
+    unsigned m = __ballot_sync(0xffffffffu, alive);
+    if (!m) return;
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == static_cast<unsigned>(leader)) base = atomicAdd(count_out, static_cast<uint32_t>(__popc(m)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (alive) {
+        uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
+        nslot[pos] = slot;
+        no[pos] = make_float4(o.x, o.y, o.z, __uint_as_float(job));
+        nd[pos] = make_float4(d.x, d.y, d.z, 0.0f);
+    }
+}
+
+// Single thread: what to gather and how many paths to issue this iteration.
+__global__ void k_eng_plan(EngineCtl* c, const DevUnit* __restrict__ units, const uint32_t* __restrict__ unit_done,
+                           uint32_t arena) {
+    uint32_t u = c->g_lo, gn = 0;
+    uint32_t jobs_in[GATHER_MAX];
+    while (u < c->units_count && gn < GATHER_MAX) {
+        DevUnit U = units[u];
+        if (unit_done[u] < U.npix) break;
+        bool dup = false;
+        for (uint32_t k = 0; k < gn; ++k) dup |= jobs_in[k] == U.job;
+        if (dup) break;  // a job's passes are gathered one per iteration, in order
+        jobs_in[gn] = U.job;
+        c->gather_units[gn++] = u;
+        ++u;
+    }
+    c->gather_n = gn;
+    c->g_lo = u;
+    c->gather_lo_prefix = u < c->units_count ? units[u].prefix : c->paths_total;
+    unsigned long long freec = c->free_tail - c->free_head;
+    unsigned long long rem = c->paths_total - c->gcur;
+    unsigned long long lim = c->gather_lo_prefix + arena - c->gcur;  // arena slots not holding ungathered samples
+    unsigned long long n = min(freec, min(rem, lim));
+    c->fill_n = static_cast<uint32_t>(n);
+    c->fill_base = c->gcur;
+    c->fill_head = c->free_head;
+    c->gcur += n;
+    c->free_head += static_cast<uint32_t>(n);
+    c->done = c->g_lo == c->units_count ? 1u : 0u;
+    c->iter += 1;
+}
+
+struct ArenaIdx {
+    unsigned long long prefix;
+    uint32_t width, arena;
+    GR_D size_t operator()(uint32_t r, uint32_t col) const {
+        return static_cast<size_t>((prefix + static_cast<unsigned long long>(r) * width + col) % arena);
+    }
+};
+
+__global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const EngineCtl* c, const DevJob* __restrict__ jobs,
+                                                                    const DevUnit* __restrict__ units,
+                                                                    const float2* __restrict__ a_st,
+                                                                    const float4* __restrict__ a_c, uint32_t arena) {
+    __shared__ StagedSample sm[FILM_SPAN * FILM_SPAN];
+    const uint32_t gn = c->gather_n;
+    for (uint32_t g = 0; g < gn; ++g) {
+        DevUnit U = units[c->gather_units[g]];
+        const DevJob& J = jobs[U.job];
+        const uint32_t w = J.width, h = J.height;
+        const uint32_t tx = (w + FILM_TILE - 1) / FILM_TILE, tiles = tx * ((h + FILM_TILE - 1) / FILM_TILE);
+        for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+            const int ox = static_cast<int>((t % tx) * FILM_TILE), oy = static_cast<int>((t / tx) * FILM_TILE);
+            const int x = ox + threadIdx.x % FILM_TILE, y = oy + threadIdx.x / FILM_TILE;
+            const bool inside = x < static_cast<int>(w) && y < static_cast<int>(h);
+            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (inside) acc = J.film[static_cast<size_t>(y) * w + x];
+            gather_tile(sm, a_st, a_c, w, h, ox, oy, acc, ArenaIdx{U.prefix, w, arena});
+            if (inside && J.live) J.film[static_cast<size_t>(y) * w + x] = acc;
+        }
+    }
+}
+
+// The unit holding global path p: the last unit whose prefix is <= p.
+GR_D uint32_t find_unit(const DevUnit* __restrict__ units, uint32_t lo, uint32_t hi, unsigned long long p) {
+    while (hi - lo > 1) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        if (units[mid].prefix <= p) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob* __restrict__ jobs,
+                                                     const DevUnit* __restrict__ units,
+                                                     const uint32_t* __restrict__ free_ring, uint32_t cap, int cur,
+                                                     uint32_t* __restrict__ s_unit, uint32_t* __restrict__ s_pixel,
+                                                     uint32_t* __restrict__ s_depth, float4* __restrict__ s_tp,
+                                                     float4* __restrict__ s_L, unsigned long long* __restrict__ s_key,
+                                                     float2* __restrict__ s_st, uint32_t* __restrict__ q_slot,
+                                                     float4* __restrict__ q_o, float4* __restrict__ q_d) {
+    const uint32_t n = c->fill_n;
+    const unsigned long long base = c->fill_base;
+    const uint32_t head = c->fill_head, lo = c->g_lo, hi = c->units_count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
+        uint32_t i = b + (threadIdx.x & 31u);
+        bool alive = false;
+        uint32_t slot = 0, job = 0;
+        V3 o = v3zero(), d = v3zero();
+        if (i < n) {
+            slot = free_ring[(head + i) % cap];
+            unsigned long long p = base + i;
+            uint32_t u = find_unit(units, lo, hi, p);
+            DevUnit U = units[u];
+            uint32_t pixel = static_cast<uint32_t>(p - U.prefix);
+            job = U.job;
+            const DevJob& J = jobs[job];
+            uint32_t row = pixel / J.width, col = pixel - (pixel / J.width) * J.width;
+            uint64_t key = path_key(J.seed, U.pass, pixel);
+            float s, t;
+            film_sample_point(J.width, J.height, row, col, key, s, t);
+            camera_ray(J.cam, s, t, o, d);
+            s_unit[slot] = u;
+            s_pixel[slot] = pixel;
+            s_depth[slot] = 0;
+            s_tp[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            s_L[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            s_key[slot] = key;
+            s_st[slot] = make_float2(s, t);
+            alive = true;
+        }
+        push_ray(alive, &c->q[cur], slot, o, d, job, q_slot, q_o, q_d);
+    }
+}
+
+template <int W, int BS>
+__global__ void __launch_bounds__(BS) k_eng_extend(EngineCtl* c, int cur, const DevJob* __restrict__ jobs,
+                                                   const float4* __restrict__ q_o, const float4* __restrict__ q_d,
+                                                   float4* __restrict__ q_hit) {
+    extern __shared__ unsigned char smem[];
+    int32_t* sref = reinterpret_cast<int32_t*>(smem);
+    float* stt = reinterpret_cast<float*>(smem + sizeof(int32_t) * SMEM_STACK * blockDim.x);
+    int2 spill[MAX_STACK - SMEM_STACK];
+    StackView stk{sref + threadIdx.x, stt + threadIdx.x, static_cast<int>(blockDim.x), spill};
+    const uint32_t n = c->q[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c->rays, static_cast<unsigned long long>(n));
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        float4 o4 = q_o[q], d4 = q_d[q];
+        const DeviceScene& s = jobs[__float_as_uint(o4.w)].scene;
+        TravState t;
+        trav_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX);
+        const uint32_t budget = 8u * s.num_components + 4096u;
+        uint32_t steps = 0;
+        while (!trav_step<W, false, false>(s, t, stk, &c->err, nullptr)) {
+            if (++steps > budget) {
+                atomicExch(&c->err, 2);
+                t.hit = -1;
+                break;
+            }
+        }
+        q_hit[q] = make_float4(t.closest, __int_as_float(t.hit), t.hu, t.hv);
+    }
+}
+
+__global__ void __launch_bounds__(EBLOCK) k_eng_shade(EngineCtl* c, int cur, const DevJob* __restrict__ jobs,
+                                                      const DevUnit* __restrict__ units, uint32_t* unit_done,
+                                                      uint32_t* free_ring, uint32_t cap, uint32_t arena,
+                                                      const uint32_t* __restrict__ q_slot,
+                                                      const float4* __restrict__ q_o, const float4* __restrict__ q_d,
+                                                      const float4* __restrict__ q_hit, uint32_t* __restrict__ s_unit,
+                                                      const uint32_t* __restrict__ s_pixel,
+                                                      uint32_t* __restrict__ s_depth, float4* __restrict__ s_tp,
+                                                      float4* __restrict__ s_L,
+                                                      const unsigned long long* __restrict__ s_key,
+                                                      const float2* __restrict__ s_st, float2* __restrict__ a_st,
+                                                      float4* __restrict__ a_c, uint32_t* __restrict__ nslot,
+                                                      float4* __restrict__ no, float4* __restrict__ nd) {
+    const int nxt = cur ^ 1;
+    const uint32_t n = c->q[cur];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
+        uint32_t q = b + lane;
+        bool alive = false, finished = false;
+        uint32_t slot = 0, job = 0, unit = 0xFFFFFFFFu;
+        V3 new_o = v3zero(), new_d = v3zero();
+        if (q < n) {
+            slot = q_slot[q];
+            float4 h = q_hit[q];
+            float4 o4 = q_o[q], d4 = q_d[q];
+            job = __float_as_uint(o4.w);
+            const DevJob& J = jobs[job];
+            const DeviceScene& s = J.scene;
+            V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
+            float4 tp4 = s_tp[slot], L4 = s_L[slot];
+            V3 tp = V3{tp4.x, tp4.y, tp4.z}, L = V3{L4.x, L4.y, L4.z};
+            uint32_t depth = s_depth[slot];
+            int32_t k = __float_as_int(h.y);
+            if (!J.live) {
+                // cancelled: drop the path
+            } else if (k < 0) {
+                // DisplayColorIntegrator returns black on a miss (render/integrators.rs:29-31).
+                if (s.has_env && !J.display) L = L + mul(tp, V3{s.env[0], s.env[1], s.env[2]});
+            } else if (J.display) {
+                uint32_t prim = __float_as_uint(__ldg(s.prims + 3 * static_cast<size_t>(k)).w);
+                const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
+                L = V3{m.display[0], m.display[1], m.display[2]};
+            } else {
+                // PathTracerIntegrator::integrate (render/integrators.rs:42-100), one segment.
+                uint32_t prim;
+                Frame f = hit_frame(s, k, o, d, h.x, h.z, h.w, prim);
+                const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
+                uint64_t key = s_key[slot];
+                uint32_t base = DIM_CAMERA_WALK + 4 * depth;
+                MaterialSample ms = sample_world(m, -d, f, true, uniform01(key, base), uniform01(key, base + 1),
+                                                 uniform01(key, base + 2));
+                L = L + mul(tp, ms.emission);
+                tp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
+                new_o = nudge(o + (d * h.x), ms.outgoing);
+                new_d = ms.outgoing;
+                if (depth > J.rr_depth || nearly_zero(tp)) {
+                    float rv = uniform01(key, base + 3);
+                    float lum = luminance(tp);
+                    float prob = depth > J.rr_aggr ? clamped_lerp(0.10f, 0.75f, lum) : clamped_lerp(0.25f, 1.00f, lum);
+                    tp = rv < prob ? tp / prob : v3zero();
+                }
+                alive = !is_zero(tp) && (J.max_depth == 0 || depth + 1 < J.max_depth);
+            }
+            if (alive) {
+                s_tp[slot] = make_float4(tp.x, tp.y, tp.z, 0.0f);
+                s_L[slot] = make_float4(L.x, L.y, L.z, 0.0f);
+                s_depth[slot] = depth + 1;
+            } else {
+                finished = true;
+                unit = s_unit[slot];
+                unsigned long long p = units[unit].prefix + s_pixel[slot];
+                size_t a = static_cast<size_t>(p % arena);
+                a_st[a] = s_st[slot];
+                a_c[a] = make_float4(L.x, L.y, L.z, 0.0f);
+            }
+        }
+        // Finished paths: count their unit done (one atomic per unit per warp) and free
+        // their slot (one atomic per warp).
+        unsigned fm = __ballot_sync(0xffffffffu, finished);
+        if (fm) {
+            __threadfence();  // arena writes before the unit count
+            unsigned same = __match_any_sync(0xffffffffu, unit);
+            if (finished && lane == static_cast<unsigned>(__ffs(same) - 1))
+                atomicAdd(unit_done + unit, static_cast<uint32_t>(__popc(same)));
+            int leader = __ffs(fm) - 1;
+            uint32_t fbase = 0;
+            if (lane == static_cast<unsigned>(leader)) {
+                fbase = atomicAdd(&c->free_tail, static_cast<uint32_t>(__popc(fm)));
+                atomicAdd(&c->samples_done, static_cast<unsigned long long>(__popc(fm)));
+            }
+            fbase = __shfl_sync(0xffffffffu, fbase, leader);
+            if (finished) free_ring[(fbase + __popc(fm & ((1u << lane) - 1u))) % cap] = slot;
+        }
+        push_ray(alive, &c->q[nxt], slot, new_o, new_d, job, nslot, no, nd);
+    }
+}
+
+__global__ void k_eng_init_free(uint32_t* free_ring, uint32_t cap) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < cap) free_ring[i] = i;
+}
+
+int grid_for(const void* kernel, int block, size_t smem, uint32_t n) {
+    static int sm = device_sm_count();
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    uint32_t need = (n + block - 1) / block;
+    return static_cast<int>(std::max(1u, std::min(need, static_cast<uint32_t>(sm * per_sm))));
+}
+
+template <int W, int BS>
+gr_status launch_extend(EngineCtl* c, int cur, const DevJob* jobs, const float4* qo, const float4* qd, float4* qh,
+                        uint32_t cap, cudaStream_t st) {
+    size_t smem = step_stack_smem_bytes(BS);
+    int grid = grid_for(reinterpret_cast<const void*>(k_eng_extend<W, BS>), BS, smem, cap);
+    k_eng_extend<W, BS><<<grid, BS, smem, st>>>(c, cur, jobs, qo, qd, qh);
+    GR_CUDA_TRY(cudaGetLastError());
+    return GR_OK;
+}
+
+template <int W>
+gr_status launch_extend_w(uint32_t bs, EngineCtl* c, int cur, const DevJob* jobs, const float4* qo, const float4* qd,
+                          float4* qh, uint32_t cap, cudaStream_t st) {
+    switch (bs) {
+        case 64: return launch_extend<W, 64>(c, cur, jobs, qo, qd, qh, cap, st);
+        case 256: return launch_extend<W, 256>(c, cur, jobs, qo, qd, qh, cap, st);
+        default: return launch_extend<W, 128>(c, cur, jobs, qo, qd, qh, cap, st);
+    }
+}
+
+}  // namespace
+
+#define GR_ETRY(expr)                     \
+    do {                                  \
+        gr_status s__ = (expr);           \
+        if (s__ != GR_OK) return s__;     \
+    } while (0)
+
+constexpr uint32_t ENGINE_MAX_JOBS = 4096;
+constexpr uint32_t ENGINE_MAX_UNITS = 1u << 20;
+
+Engine::~Engine() {
+    if (st_) cudaStreamSynchronize(st_);
+    if (graph_) cudaGraphExecDestroy(graph_);
+    if (h_pinned_) cudaFreeHost(h_pinned_);
+    if (st_) cudaStreamDestroy(st_);
+}
+
+gr_status Engine::init(const EngineConfig& cfg, cudaStream_t) {
+    cfg_ = cfg;
+    if (cfg_.width != 2 && cfg_.width != 4 && cfg_.width != 8) {
+        set_error("engine: BVH width must be 2, 4 or 8");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    if (cfg_.block != 64 && cfg_.block != 128 && cfg_.block != 256) {
+        set_error("engine: block size must be 64, 128 or 256");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    if (cfg_.capacity < 1024) cfg_.capacity = 1024;
+    arena_ = cfg_.arena ? cfg_.arena : 2 * cfg_.capacity + (1u << 22);
+    GR_CUDA_TRY(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    const size_t C = cfg_.capacity;
+    auto alloc = [&](DevBuf& b, size_t bytes) -> cudaError_t {
+        bytes_ += bytes;
+        return b.ensure(bytes);
+    };
+    GR_CUDA_TRY(alloc(ctl_, sizeof(EngineCtl)));
+    GR_CUDA_TRY(alloc(jobs_, ENGINE_MAX_JOBS * sizeof(DevJob)));
+    GR_CUDA_TRY(alloc(units_, ENGINE_MAX_UNITS * sizeof(DevUnit)));
+    GR_CUDA_TRY(alloc(unit_done_, ENGINE_MAX_UNITS * sizeof(uint32_t)));
+    GR_CUDA_TRY(alloc(s_unit_, C * 4));
+    GR_CUDA_TRY(alloc(s_pixel_, C * 4));
+    GR_CUDA_TRY(alloc(s_depth_, C * 4));
+    GR_CUDA_TRY(alloc(s_tp_, C * 16));
+    GR_CUDA_TRY(alloc(s_L_, C * 16));
+    GR_CUDA_TRY(alloc(s_key_, C * 8));
+    GR_CUDA_TRY(alloc(s_st_, C * 8));
+    GR_CUDA_TRY(alloc(free_ring_, C * 4));
+    for (int k = 0; k < 2; ++k) {
+        GR_CUDA_TRY(alloc(q_slot_[k], C * 4));
+        GR_CUDA_TRY(alloc(q_o_[k], C * 16));
+        GR_CUDA_TRY(alloc(q_d_[k], C * 16));
+    }
+    GR_CUDA_TRY(alloc(q_hit_, C * 16));
+    GR_CUDA_TRY(alloc(a_st_, static_cast<size_t>(arena_) * 8));
+    GR_CUDA_TRY(alloc(a_c_, static_cast<size_t>(arena_) * 16));
+    GR_CUDA_TRY(cudaMemsetAsync(ctl_.ptr, 0, sizeof(EngineCtl), st_));
+    GR_CUDA_TRY(cudaMemsetAsync(unit_done_.ptr, 0, ENGINE_MAX_UNITS * sizeof(uint32_t), st_));
+    k_eng_init_free<<<(cfg_.capacity + 255) / 256, 256, 0, st_>>>(free_ring_.as<uint32_t>(), cfg_.capacity);
+    GR_CUDA_TRY(cudaGetLastError());
+    uint32_t tail = cfg_.capacity;
+    GR_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(EngineCtl, free_tail), &tail, 4,
+                                cudaMemcpyHostToDevice, st_));
+    GR_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&h_pinned_), 8 * sizeof(uint64_t), cudaHostAllocDefault));
+    GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    return record_pair();
+}
+
+gr_status Engine::enqueue_iteration(int cur) {
+    EngineCtl* c = ctl_.as<EngineCtl>();
+    const uint32_t C = cfg_.capacity;
+    const int nxt = cur ^ 1;
+    k_eng_plan<<<1, 1, 0, st_>>>(c, units_.as<DevUnit>(), unit_done_.as<uint32_t>(), arena_);
+    GR_CUDA_TRY(cudaGetLastError());
+    k_eng_gather<<<GATHER_BLOCKS, FILM_TILE * FILM_TILE, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(),
+                                                                   a_st_.as<float2>(), a_c_.as<float4>(), arena_);
+    GR_CUDA_TRY(cudaGetLastError());
+    int fgrid = grid_for(reinterpret_cast<const void*>(k_eng_fill), EBLOCK, 0, C);
+    k_eng_fill<<<fgrid, EBLOCK, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), free_ring_.as<uint32_t>(), C,
+                                          cur, s_unit_.as<uint32_t>(), s_pixel_.as<uint32_t>(),
+                                          s_depth_.as<uint32_t>(), s_tp_.as<float4>(), s_L_.as<float4>(),
+                                          s_key_.as<unsigned long long>(), s_st_.as<float2>(),
+                                          q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>());
+    GR_CUDA_TRY(cudaGetLastError());
+    switch (cfg_.width) {
+        case 2:
+            GR_ETRY(launch_extend_w<2>(cfg_.block, c, cur, jobs_.as<DevJob>(), q_o_[cur].as<float4>(),
+                                       q_d_[cur].as<float4>(), q_hit_.as<float4>(), C, st_));
+            break;
+        case 8:
+            GR_ETRY(launch_extend_w<8>(cfg_.block, c, cur, jobs_.as<DevJob>(), q_o_[cur].as<float4>(),
+                                       q_d_[cur].as<float4>(), q_hit_.as<float4>(), C, st_));
+            break;
+        default:
+            GR_ETRY(launch_extend_w<4>(cfg_.block, c, cur, jobs_.as<DevJob>(), q_o_[cur].as<float4>(),
+                                       q_d_[cur].as<float4>(), q_hit_.as<float4>(), C, st_));
+    }
+    GR_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(c) + offsetof(EngineCtl, q) + nxt * sizeof(uint32_t), 0, 4, st_));
+    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), EBLOCK, 0, C);
+    k_eng_shade<<<sgrid, EBLOCK, 0, st_>>>(
+        c, cur, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), free_ring_.as<uint32_t>(), C,
+        arena_, q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>(), q_hit_.as<float4>(),
+        s_unit_.as<uint32_t>(), s_pixel_.as<uint32_t>(), s_depth_.as<uint32_t>(), s_tp_.as<float4>(),
+        s_L_.as<float4>(), s_key_.as<unsigned long long>(), s_st_.as<float2>(), a_st_.as<float2>(),
+        a_c_.as<float4>(), q_slot_[nxt].as<uint32_t>(), q_o_[nxt].as<float4>(), q_d_[nxt].as<float4>());
+    GR_CUDA_TRY(cudaGetLastError());
+    return GR_OK;
+}
+
+// Captures two iterations (queues 0 -> 1, then 1 -> 0) as one graph.
+gr_status Engine::record_pair() {
+    cudaGraph_t g = nullptr;
+    GR_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+    gr_status s0 = enqueue_iteration(0);
+    gr_status s1 = s0 == GR_OK ? enqueue_iteration(1) : s0;
+    cudaError_t e = cudaStreamEndCapture(st_, &g);
+    if (s1 != GR_OK) {
+        if (g) cudaGraphDestroy(g);
+        return s1;
+    }
+    GR_CUDA_TRY(e);
+    cudaError_t ie = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    GR_CUDA_TRY(ie);
+    return GR_OK;
+}
+
+gr_status Engine::add_job(const DevJob& job, uint32_t first_pass, uint32_t passes, uint32_t& index) {
+    if (h_jobs_.size() >= ENGINE_MAX_JOBS) {
+        set_error("engine: too many jobs");
+        return GR_ERR_BUSY;
+    }
+    if (job.scene.width != cfg_.width) {
+        set_error("engine: every scene in one engine must have the engine's BVH width");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    if (static_cast<uint64_t>(job.npix) * 2 > arena_) {
+        set_error("engine: image too large for the sample arena");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    index = static_cast<uint32_t>(h_jobs_.size());
+    h_jobs_.push_back(job);
+    GR_CUDA_TRY(cudaMemcpyAsync(jobs_.as<DevJob>() + index, &h_jobs_.back(), sizeof(DevJob), cudaMemcpyHostToDevice,
+                                st_));
+    std::vector<std::pair<uint32_t, uint32_t>> u;
+    for (uint32_t k = 0; k < passes; ++k) u.emplace_back(index, first_pass + k);
+    if (!u.empty()) return append_units(u);
+    return GR_OK;
+}
+
+gr_status Engine::append_units(const std::vector<std::pair<uint32_t, uint32_t>>& units) {
+    if (h_units_.size() + units.size() > ENGINE_MAX_UNITS) {
+        set_error("engine: too many units");
+        return GR_ERR_BUSY;
+    }
+    uint64_t prefix = 0;
+    if (!h_units_.empty()) prefix = h_units_.back().prefix + h_units_.back().npix;
+    size_t first = h_units_.size();
+    for (auto& pu : units) {
+        DevUnit U;
+        U.prefix = prefix;
+        U.job = pu.first;
+        U.pass = pu.second;
+        U.npix = h_jobs_[pu.first].npix;
+        U.pad = 0;
+        prefix += U.npix;
+        h_units_.push_back(U);
+    }
+    GR_CUDA_TRY(cudaMemcpyAsync(units_.as<DevUnit>() + first, h_units_.data() + first, units.size() * sizeof(DevUnit),
+                                cudaMemcpyHostToDevice, st_));
+    // The kernels read units_count / paths_total from the control block.  Updating them
+    // from the host is stream-ordered after every launched iteration.
+    uint32_t count = static_cast<uint32_t>(h_units_.size());
+    unsigned long long total = prefix;
+    h_pinned_[6] = count;
+    h_pinned_[7] = total;
+    GR_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(EngineCtl, units_count), &h_pinned_[6],
+                                4, cudaMemcpyHostToDevice, st_));
+    GR_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(EngineCtl, paths_total), &h_pinned_[7],
+                                8, cudaMemcpyHostToDevice, st_));
+    GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    return GR_OK;
+}
+
+gr_status Engine::reset() {
+    GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    size_t used = h_units_.size();
+    GR_CUDA_TRY(cudaMemsetAsync(ctl_.ptr, 0, sizeof(EngineCtl), st_));
+    if (used) GR_CUDA_TRY(cudaMemsetAsync(unit_done_.ptr, 0, used * sizeof(uint32_t), st_));
+    k_eng_init_free<<<(cfg_.capacity + 255) / 256, 256, 0, st_>>>(free_ring_.as<uint32_t>(), cfg_.capacity);
+    GR_CUDA_TRY(cudaGetLastError());
+    h_pinned_[6] = cfg_.capacity;
+    GR_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(EngineCtl, free_tail), &h_pinned_[6], 4,
+                                cudaMemcpyHostToDevice, st_));
+    GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    h_jobs_.clear();
+    h_units_.clear();
+    return GR_OK;
+}
+
+gr_status Engine::cancel_job(uint32_t j) {
+    if (j >= h_jobs_.size()) {
+        set_error("engine: no such job");
+        return GR_ERR_NOT_FOUND;
+    }
+    h_jobs_[j].live = 0;
+    GR_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(jobs_.as<DevJob>() + j) + offsetof(DevJob, live),
+                                &h_jobs_[j].live, 4, cudaMemcpyHostToDevice, st_));
+    GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    return GR_OK;
+}
+
+gr_status Engine::run(uint32_t max_pairs, bool& done) {
+    done = false;
+    // Replays graph pairs; the done flag is copied back after each replay and read two
+    // replays behind, so the host never stalls the GPU.  Replays after completion are
+    // empty iterations.
+    cudaEvent_t ev[4];
+    for (auto& e : ev) GR_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    struct Free {
+        cudaEvent_t* e;
+        ~Free() {
+            for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
+        }
+    } fr{ev};
+    const char* done_ptr = reinterpret_cast<const char*>(ctl_.ptr) + offsetof(EngineCtl, done);
+    // Progress guard: every 256 replays the issued / gathered counters must have moved.
+    unsigned long long last_samples = ~0ull;
+    uint32_t last_glo = ~0u;
+    for (uint32_t k = 0; k < max_pairs; ++k) {
+        if (k && (k & 255) == 0) {
+            EngineCtl c;
+            GR_CUDA_TRY(cudaStreamSynchronize(st_));
+            GR_CUDA_TRY(cudaMemcpy(&c, ctl_.ptr, sizeof(EngineCtl), cudaMemcpyDeviceToHost));
+            if (c.done) break;
+            if (c.samples_done == last_samples && c.g_lo == last_glo) {
+                set_error("engine: no progress over 256 iterations");
+                return GR_ERR_INTERNAL;
+            }
+            last_samples = c.samples_done;
+            last_glo = c.g_lo;
+        }
+        GR_CUDA_TRY(cudaGraphLaunch(graph_, st_));
+        h_pinned_[k & 3] = 0;
+        GR_CUDA_TRY(cudaMemcpyAsync(&h_pinned_[k & 3], done_ptr, 4, cudaMemcpyDeviceToHost, st_));
+        GR_CUDA_TRY(cudaEventRecord(ev[k & 3], st_));
+        if (k >= 2) {
+            GR_CUDA_TRY(cudaEventSynchronize(ev[(k - 2) & 3]));
+            if (h_pinned_[(k - 2) & 3]) break;
+        }
+    }
+    GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    EngineCtl c;
+    GR_CUDA_TRY(cudaMemcpy(&c, ctl_.ptr, sizeof(EngineCtl), cudaMemcpyDeviceToHost));
+    done = c.done != 0;
+    last_rays_ = c.rays;
+    if (c.err == 2) {
+        set_error("engine: traversal step budget exceeded");
+        return GR_ERR_TIMEOUT;
+    }
+    if (c.err) {
+        set_error("engine: traversal stack bound exceeded");
+        return GR_ERR_STACK_OVERFLOW;
+    }
+    return GR_OK;
+}
+
+gr_status Engine::read_ctl(EngineCtl& c) {
+    GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    GR_CUDA_TRY(cudaMemcpy(&c, ctl_.ptr, sizeof(EngineCtl), cudaMemcpyDeviceToHost));
+    return GR_OK;
+}
+
+gr_status Engine::unit_done_counts(std::vector<uint32_t>& done) {
+    done.resize(h_units_.size());
+    if (done.empty()) return GR_OK;
+    GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    GR_CUDA_TRY(cudaMemcpy(done.data(), unit_done_.ptr, done.size() * 4, cudaMemcpyDeviceToHost));
+    return GR_OK;
+}
+
+DevJob make_job(gr_scene* scene, const gr_camera& cam, const gr_render_params& p, uint32_t width, uint32_t height,
+                float4* film) {
+    DevJob j;
+    std::memset(&j, 0, sizeof(j));
+    j.scene = scene->dev;
+    j.cam = make_camera(cam);
+    j.film = film;
+    j.seed = p.seed;
+    j.width = width;
+    j.height = height;
+    j.npix = width * height;
+    j.display = p.integrator == GR_INTEGRATOR_DISPLAY_COLOR ? 1 : 0;
+    j.max_depth = j.display ? 1 : p.max_depth;
+    j.rr_depth = p.rr_depth;
+    j.rr_aggr = p.rr_aggressive_depth;
+    j.live = 1;
+    return j;
+}
+
+}  // namespace gr

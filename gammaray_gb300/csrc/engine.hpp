@@ -1,0 +1,122 @@
+// Multi-job wavefront engine: the machinery behind gr_render_batch and gr_server_*.
+//
+// Many renders ("jobs": a scene, a camera, settings and a film) share one pool of path
+// slots.  Each job's work is a list of units, one per pass; units are issued in a global
+// order (round-robin over jobs, pass by pass).  Every iteration:
+//   plan    (1 thread) picks the finished units to gather (consecutive from the oldest,
+//           at most one per job) and how many new paths to issue into free slots
+//   gather  splats the picked units into their films (the deterministic tile gather)
+//   fill    turns free slots into new camera paths (jitter, camera ray)
+//   extend  closest hit for the queued rays of all jobs
+//   shade   path-tracer shading per job; finished paths write their sample into a ring
+//           arena, count their unit done and free their slot
+// All launches have fixed grids and read their sizes from device memory, so an
+// iteration pair is captured once in a CUDA graph and replayed until every unit is
+// gathered.  A job's passes are gathered in pass order, so each film is identical to the
+// film the job gets when it renders alone.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "runtime.hpp"
+
+namespace gr {
+
+struct alignas(16) DevJob {
+    DeviceScene scene;
+    DevCamera cam;
+    float4* film;
+    uint64_t seed;
+    uint32_t width, height, npix;
+    uint32_t display;  // display-colour integrator
+    uint32_t max_depth, rr_depth, rr_aggr;
+    uint32_t live;  // 0: cancelled, its paths are dropped
+};
+
+struct DevUnit {
+    uint64_t prefix;  // global index of the unit's first path
+    uint32_t job;
+    uint32_t pass;
+    uint32_t npix;
+    uint32_t pad;
+};
+
+constexpr int GATHER_MAX = 64;
+
+struct EngineCtl {
+    unsigned long long paths_total;  // paths of all units appended so far
+    unsigned long long gcur;         // next path to issue
+    unsigned long long gather_lo_prefix;
+    unsigned long long fill_base;
+    unsigned long long rays;
+    unsigned long long samples_done;
+    uint32_t units_count;
+    uint32_t g_lo;  // oldest unit not yet gathered
+    uint32_t free_head, free_tail;
+    uint32_t q[2];
+    uint32_t fill_n, fill_head;
+    uint32_t gather_n;
+    uint32_t done;
+    int32_t err;
+    uint32_t iter;
+    uint32_t gather_units[GATHER_MAX];
+};
+
+struct EngineConfig {
+    uint32_t capacity = 1u << 21;  // path slots
+    uint32_t width = 4;            // BVH width of every scene in the engine
+    uint32_t block = 128;          // extension kernel block size (64, 128, 256)
+    uint32_t arena = 0;            // samples; 0 = derived
+};
+
+class Engine {
+  public:
+    Engine() {}
+    ~Engine();
+    gr_status init(const EngineConfig& cfg, cudaStream_t st);
+    // Appends a job and its units (one per pass).  Returns the job index.
+    gr_status add_job(const DevJob& job, uint32_t first_pass, uint32_t passes, uint32_t& job_index);
+    // Appends units of several jobs round-robin by pass: units[k] = (job, pass).
+    gr_status append_units(const std::vector<std::pair<uint32_t, uint32_t>>& units);
+    gr_status cancel_job(uint32_t job_index);
+    // Forgets every job and unit (buffers and the captured graph are kept).
+    gr_status reset();
+    // Runs iteration pairs (graph replays) until every appended unit is gathered or
+    // `max_pairs` pairs ran.  Returns whether all work is done.
+    gr_status run(uint32_t max_pairs, bool& done);
+    // Host copies of the control block and unit progress (synchronises the stream).
+    gr_status read_ctl(EngineCtl& ctl);
+    gr_status unit_done_counts(std::vector<uint32_t>& done);
+    const std::vector<DevUnit>& units() const { return h_units_; }
+    const std::vector<DevJob>& jobs() const { return h_jobs_; }
+    uint32_t capacity() const { return cfg_.capacity; }
+    const EngineConfig& config() const { return cfg_; }
+    uint64_t rays() const { return last_rays_; }
+    uint64_t device_bytes() const { return bytes_; }
+    cudaStream_t stream() const { return st_; }
+
+  private:
+    gr_status record_pair();
+    gr_status enqueue_iteration(int cur);
+    EngineConfig cfg_;
+    cudaStream_t st_ = nullptr;
+    uint32_t arena_ = 0;
+    DevBuf ctl_, jobs_, units_, unit_done_;
+    DevBuf s_unit_, s_pixel_, s_depth_, s_tp_, s_L_, s_key_, s_st_, free_ring_;
+    DevBuf q_slot_[2], q_o_[2], q_d_[2], q_hit_;
+    DevBuf a_st_, a_c_;
+    std::vector<DevJob> h_jobs_;
+    std::vector<DevUnit> h_units_;
+    uint32_t jobs_cap_ = 0, units_cap_ = 0;
+    cudaGraphExec_t graph_ = nullptr;
+    uint64_t last_rays_ = 0;
+    uint64_t bytes_ = 0;
+    uint64_t* h_pinned_ = nullptr;
+};
+
+// DeviceScene + camera + settings of a render as an engine job.
+DevJob make_job(gr_scene* scene, const gr_camera& cam, const gr_render_params& p, uint32_t width, uint32_t height,
+                float4* film);
+
+}  // namespace gr

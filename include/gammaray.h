@@ -366,15 +366,22 @@ typedef struct gr_batch_options {
 } gr_batch_options;
 
 gr_status gr_render_batch(const gr_job* jobs, uint32_t n, const gr_batch_options* options);
+/* Picks path_capacity and block_size for these jobs by timing short trial runs on
+ * scratch films (the jobs' films are not touched). */
+gr_status gr_batch_autotune(const gr_job* jobs, uint32_t n, gr_batch_options* out);
+/* Counters of the last gr_render_batch on this thread. */
+gr_status gr_batch_last_stats(gr_render_stats* out);
 
 /* -------------------------------------------------------------------- serving */
 
 typedef struct gr_server gr_server;
 
 typedef struct gr_server_options {
-    uint64_t memory_budget_bytes; /* admission limit; 0 = 90% of free device memory */
+    uint64_t memory_budget_bytes; /* admission limit for films; 0 = 90% of free device memory */
     uint32_t max_active;          /* concurrent renders; 0 = unlimited */
-    uint32_t path_capacity;       /* paths in flight per wavefront; 0 = default */
+    uint32_t path_capacity;       /* paths in flight; 0 = default */
+    uint32_t bvh_width;           /* BVH width of the scenes served (2, 4, 8); 0 = 4 */
+    uint32_t block_size;          /* extension kernel block size; 0 = 128 */
 } gr_server_options;
 
 typedef struct gr_request {

@@ -513,6 +513,18 @@ gr_status gr_render_batch(const gr_job* jobs, uint32_t n, const gr_batch_options
     return GR_OK;
 }
 
+gr_status gr_batch_autotune(const gr_job*, uint32_t, gr_batch_options* out) {
+    if (!out) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    return GR_OK;
+}
+
+gr_status gr_batch_last_stats(gr_render_stats* out) {
+    if (!out) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    return GR_OK;
+}
+
 gr_status gr_server_create(const gr_server_options*, gr_server**) {
     return fail(GR_ERR_UNSUPPORTED, "serving is a device feature");
 }
