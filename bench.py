@@ -45,6 +45,10 @@ def parse():
     ap.add_argument("--height", type=int, default=1024)
     ap.add_argument("--spp", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-rate", type=float, default=3.0, help="Poisson arrival rate (requests/s)")
     ap.add_argument("--profile-case", action="store_true",
                     help="render the workload once (untimed, --spp passes) and exit: the small case for ncu")
     return ap.parse_args()
@@ -172,6 +176,122 @@ def config_of(w):
             "unit_of_step": "one complete render"}
 
 
+def percentiles(xs):
+    xs = np.asarray(xs, np.float64)
+    return {"p50": float(np.percentile(xs, 50)), "p95": float(np.percentile(xs, 95)),
+            "p99": float(np.percentile(xs, 99)), "mean": float(xs.mean())}
+
+
+def run_batched(lib):
+    """Config 4: 64 seeded scenes (1k-200k triangles, 0-8 spheres, random resolution, spp
+    4-64, depth 4-12) rendered (a) one gr_render per image and (b) in one batch."""
+    import gammaray_gb300 as g
+    from gammaray_gb300 import batch, scenes
+
+    ws = scenes.batch_scenes(64)
+    stages = [g.Stage(w.prims, lib=lib, environment=w.environment, seed=k) for k, w in enumerate(ws)]
+    samples = sum(w.width * w.height * w.spp for w in ws)
+
+    def jobs():
+        return [batch.Job(st, w.camera, w.integrator, g.Film(w.width, w.height, lib=lib), w.spp)
+                for st, w in zip(stages, ws)]
+
+    # plain per-image path (warm once, then timed)
+    warm = jobs()
+    batch.render_individually(warm[:4], lib)
+    pj = jobs()
+    t0 = time.perf_counter()
+    plain_dev = batch.render_individually(pj, lib)
+    plain_wall = time.perf_counter() - t0
+    qj = jobs()
+    t0 = time.perf_counter()
+    batch.render_per_pass(qj, lib)
+    per_pass_wall = time.perf_counter() - t0
+    opt = batch.autotune(jobs(), lib)
+    batch.render_batch(jobs()[:8], lib, opt.path_capacity, opt.block_size)  # warm
+    bj = jobs()
+    t0 = time.perf_counter()
+    st = batch.render_batch(bj, lib, opt.path_capacity, opt.block_size)
+    batch_wall = time.perf_counter() - t0
+    # same requests, same films (bit-identical is tested; spot-check one here)
+    a = bj[0].film.read()[0]
+    b = pj[0].film.read()[0]
+    same = bool(np.allclose(a, b, rtol=1e-6, atol=1e-7))
+    return {"workload": "batch_64_scenes", "samples": samples,
+            "msamples_per_s": samples / batch_wall / 1e6, "msamples_per_s_device": samples / (st.device_ms * 1e-3) / 1e6,
+            "plain_msamples_per_s": samples / plain_wall / 1e6,
+            "plain_msamples_per_s_device": samples / (plain_dev * 1e-3) / 1e6,
+            "speedup_vs_plain": plain_wall / batch_wall, "mrays_per_s": st.extension_rays / batch_wall / 1e6,
+            "plain_per_pass_msamples_per_s": samples / per_pass_wall / 1e6,
+            "speedup_vs_per_pass": per_pass_wall / batch_wall,
+            "autotuned": {"path_capacity": opt.path_capacity, "block_size": opt.block_size},
+            "films_equal_plain": same}
+
+
+def run_served(lib, n_req, rate, seed=11):
+    """Config 5: 16 resident scenes (10k-2M triangles); Poisson arrivals; random pose,
+    resolution 256^2..1920x1080, spp 1-256, depth 4-16.  Served by the continuous-
+    batching loop vs a FIFO timeline of one gr_render per request on the same GPU."""
+    import gammaray_gb300 as g
+    from gammaray_gb300 import scenes, serve
+
+    rng = np.random.default_rng(seed)
+    scs = scenes.serving_scenes(16)
+    stages = [g.Stage(p, lib=lib, environment=env, seed=k) for k, (p, env) in enumerate(scs)]
+    resolutions = [(256, 256), (512, 512), (640, 480), (1280, 720), (1920, 1080)]
+    reqs = []
+    t = 0.0
+    for k in range(n_req):
+        t += float(rng.exponential(1.0 / rate))
+        res = resolutions[int(rng.integers(0, len(resolutions)))]
+        reqs.append(dict(arrival=t, scene=int(rng.integers(0, 16)), res=res, spp=int(rng.integers(1, 257)),
+                         depth=int(rng.integers(4, 17)), cam=scenes.orbit_camera(rng, *res)))
+    samples = sum(r["res"][0] * r["res"][1] * r["spp"] for r in reqs)
+    # plain: one render per request, FIFO on one GPU
+    dur = []
+    for r in reqs:
+        f = g.Film(*r["res"], lib=lib)
+        integ = g.PathTracerIntegrator(max_depth=r["depth"])
+        t0 = time.perf_counter()
+        stages[r["scene"]].render(r["cam"], integ, f, r["spp"])
+        dur.append(time.perf_counter() - t0)
+        f.close()
+    finish, lat_plain = 0.0, []
+    for r, d in zip(reqs, dur):
+        start = max(finish, r["arrival"])
+        finish = start + d
+        lat_plain.append((finish - r["arrival"]) * 1e3)
+    plain_span = finish - reqs[0]["arrival"]
+    # served
+    srv = serve.Server(lib, max_active=16)
+    ids = {}
+    t0 = time.perf_counter()
+    nxt = 0
+    while nxt < len(reqs) or any(srv.poll(i).state < 2 for i in ids.values()):
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt]["arrival"] <= now:
+            r = reqs[nxt]
+            ids[nxt] = srv.submit(stages[r["scene"]], r["cam"], g.PathTracerIntegrator(max_depth=r["depth"]),
+                                  r["res"][0], r["res"][1], r["spp"])
+            nxt += 1
+        if nxt < len(reqs) and not any(srv.poll(i).state < 2 for i in ids.values()):
+            time.sleep(max(0.0, reqs[nxt]["arrival"] - now))
+            continue
+        srv.step(2.0)
+    span = time.perf_counter() - t0 - reqs[0]["arrival"]
+    lat = []
+    for k, rid in ids.items():
+        st = srv.poll(rid)
+        lat.append(st.finish_ms - st.submit_ms)
+        srv.take(rid)
+    srv.close()
+    return {"workload": "serve_16_scenes", "requests": n_req, "rate_per_s": rate, "samples": samples,
+            "msamples_per_s": samples / span / 1e6, "latency_ms": percentiles(lat),
+            "plain_fifo_msamples_per_s": samples / plain_span / 1e6, "plain_fifo_latency_ms": percentiles(lat_plain),
+            "plain_busy_msamples_per_s": samples / sum(dur) / 1e6,
+            "speedup_vs_plain_fifo": plain_span / span}
+
+
 def run_ours(args, rank, world, local):
     import ctypes as C
 
@@ -228,13 +348,12 @@ def run_ours(args, rank, world, local):
             launches += s.kernel_launches
         barrier()
         wall = time.perf_counter() - t0
-    total_ms = sum(dev_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps * samples_per_step / (total_ms * 1e-3) / 1e6
-    mrays = world * rays / (total_ms * 1e-3) / 1e6
+    from gammaray_gb300 import replicas
+
+    total_ms, all_samples = replicas.aggregate(sum(dev_ms), args.steps * samples_per_step)
+    _, all_rays = replicas.aggregate(0.0, rays)
+    value = all_samples / (total_ms * 1e-3) / 1e6
+    mrays = all_rays / (total_ms * 1e-3) / 1e6
 
     # End to end through the C ABI with host buffers: scene build + upload, render, read-back.
     e2e_ms, h2d, d2h = [], 0, 0
@@ -266,6 +385,7 @@ def run_ours(args, rank, world, local):
                 "peak_source": peak_kind,
                 "bytes_per_ray": b_ray, "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
                 "extend_share_of_device_time": ext_ms / total_ms if total_ms else None,
+                "shade_share_of_device_time": shade_ms / total_ms if total_ms else None,
                 "extend_ms_per_launch": ext_ms / max(1, ext_launch)}
     ncu_traffic = os.path.join(ROOT, "profiles", "extend_traffic.json")
     if os.path.exists(ncu_traffic):
@@ -277,6 +397,11 @@ def run_ours(args, rank, world, local):
         except Exception:
             pass
 
+    batched = served = None
+    if rank == 0 and not args.no_batch:
+        batched = run_batched(lib)
+    if rank == 0 and not args.no_serve:
+        served = run_served(lib, args.serve_requests, args.serve_rate)
     if rank == 0:
         cb = cpu_baseline(w, args.cpu_seconds) if world == 1 else None
         line = {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
@@ -284,6 +409,7 @@ def run_ours(args, rank, world, local):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": config_of(w), "mrays_per_s": mrays, "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
                 "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s": wall,
+                "batched": batched, "served": served,
                 "scene": {"components": int(info.num_components), "wide_nodes": int(info.num_wide_nodes),
                           "device_bytes": int(info.device_bytes), "build_s": info.build_seconds}}
         print(json.dumps(line), flush=True)

@@ -58,10 +58,28 @@ def autotune(jobs, lib) -> _abi.BatchOptions:
 def render_individually(jobs, lib) -> float:
     """The plain per-image path on the same requests: one gr_render per job.  Returns
     the summed CUDA-event time in ms."""
+    import ctypes as C
+
     total = 0.0
     for j in jobs:
-        j.stage.render(j.camera, j.integrator, j.film, j.spp)
+        p = j.stage.params(j.integrator, j.spp, first_pass=j.film.passes())
+        cam = j.camera.desc()
+        lib.call("gr_render", j.stage.handle, C.byref(cam), C.byref(p), j.film.handle)
         total += j.stage.last_stats().device_ms
+    return total
+
+
+def render_per_pass(jobs, lib) -> float:
+    """The drop-in path: one Stage::trace call (gr_render with spp = 1) per pass."""
+    import ctypes as C
+
+    total = 0.0
+    for j in jobs:
+        cam = j.camera.desc()
+        for k in range(j.spp):
+            p = j.stage.params(j.integrator, 1, first_pass=j.film.passes())
+            lib.call("gr_render", j.stage.handle, C.byref(cam), C.byref(p), j.film.handle)
+            total += j.stage.last_stats().device_ms
     return total
 
 

@@ -47,6 +47,7 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
                 "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", *inc]
     if ptxas_verbose:
         cu_flags += ["-Xptxas", "-v"]
+    cu_flags += os.environ.get("GR_NVCC_FLAGS", "").split()
     cpp_flags = ["g++", "-c", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
                  "-I" + os.path.join(cuda, "include"), *inc]
     jobs = []

@@ -70,10 +70,12 @@ gr_status run_engine_batch(const std::vector<const gr_job*>& jobs, const EngineC
         if (s != GR_OK) return s;
         max_spp = std::max(max_spp, j.params.spp);
     }
+    // Job-major order: a few scenes are live at a time, so their BVHs stay in L2; the
+    // pool still refills across job boundaries.
     std::vector<std::pair<uint32_t, uint32_t>> units;
-    for (uint32_t r = 0; r < max_spp; ++r)
-        for (size_t k = 0; k < jobs.size(); ++k)
-            if (r < jobs[k]->params.spp) units.emplace_back(idx[k], jobs[k]->params.first_pass + r);
+    for (size_t k = 0; k < jobs.size(); ++k)
+        for (uint32_t r = 0; r < jobs[k]->params.spp; ++r) units.emplace_back(idx[k], jobs[k]->params.first_pass + r);
+    (void)max_spp;
     s = e->append_units(units);
     if (s != GR_OK) return s;
     cudaEvent_t a, b;
@@ -253,8 +255,8 @@ struct gr_server {
 namespace {
 
 // Admits queued requests while films fit the budget, then tops up the engine's unit
-// backlog one pass per running request at a time (continuous batching: a request that
-// arrives joins the rotation at the next top-up).
+// backlog (continuous batching: a request that arrives is admitted and appended at the
+// next step, while the earlier ones are still on the GPU).
 gr_status schedule(gr_server* s) {
     uint32_t active = 0;
     for (auto& r : s->reqs) active += r->state == GR_REQUEST_RUNNING ? 1 : 0;
@@ -280,23 +282,33 @@ gr_status schedule(gr_server* s) {
     if (st != GR_OK) return st;
     uint64_t backlog = c.paths_total - c.gcur;
     const uint64_t want = 2ull * s->engine.capacity();
-    while (backlog < want) {
-        std::vector<std::pair<uint32_t, uint32_t>> round;
-        std::vector<ServerRequest*> owners;
-        for (auto& r : s->reqs) {
-            if (r->state != GR_REQUEST_RUNNING || r->appended >= r->req.params.spp) continue;
-            round.emplace_back(r->job, r->req.params.first_pass + r->appended);
-            owners.push_back(r.get());
+    // Shortest remaining work first: passes of the request with the fewest samples left
+    // are appended first, so short requests that arrive behind long ones start within
+    // one backlog (about two pools) of work.
+    std::vector<ServerRequest*> order;
+    for (auto& r : s->reqs)
+        if (r->state == GR_REQUEST_RUNNING && r->appended < r->req.params.spp) order.push_back(r.get());
+    std::stable_sort(order.begin(), order.end(), [](ServerRequest* a, ServerRequest* b) {
+        uint64_t ra = static_cast<uint64_t>(a->req.params.spp - a->appended) * a->req.width * a->req.height;
+        uint64_t rb = static_cast<uint64_t>(b->req.params.spp - b->appended) * b->req.width * b->req.height;
+        return ra < rb;
+    });
+    std::vector<std::pair<uint32_t, uint32_t>> batch;
+    std::vector<ServerRequest*> owners;
+    for (ServerRequest* r : order) {
+        while (backlog < want && r->appended < r->req.params.spp) {
+            batch.emplace_back(r->job, r->req.params.first_pass + r->appended);
+            owners.push_back(r);
+            r->appended += 1;
+            backlog += static_cast<uint64_t>(r->req.width) * r->req.height;
         }
-        if (round.empty()) break;
+        if (backlog >= want) break;
+    }
+    if (!batch.empty()) {
         size_t first = s->engine.units().size();
-        st = s->engine.append_units(round);
+        st = s->engine.append_units(batch);
         if (st != GR_OK) return st;
-        for (size_t k = 0; k < owners.size(); ++k) {
-            owners[k]->units.push_back(static_cast<uint32_t>(first + k));
-            owners[k]->appended += 1;
-            backlog += owners[k]->req.width * owners[k]->req.height;
-        }
+        for (size_t k = 0; k < owners.size(); ++k) owners[k]->units.push_back(static_cast<uint32_t>(first + k));
     }
     return GR_OK;
 }

@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams
     push_warp(light_alive, count_out, 2 * i + 1, lo, ld, nslot, no, nd);
 }
 
-__global__ void __launch_bounds__(BLOCK) k_bdpt_shade(DeviceScene s, BdptParams p, Verts vs,
+__global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts vs,
                                                       const uint32_t* __restrict__ count_in,
                                                       const uint32_t* __restrict__ q_slot,
                                                       const float4* __restrict__ q_o, const float4* __restrict__ q_d,

@@ -9,6 +9,16 @@
 
 namespace gr {
 
+// The lobe entry points are called from several places of the mixture (the chosen
+// lobe, then every other lobe's f and pdf).  Inlined everywhere they make the shading
+// kernels large enough to thrash the instruction cache; GR_LOBE_CALLS builds them as
+// real calls instead.
+#ifdef GR_LOBE_CALLS
+#define GR_LOBE static __device__ __noinline__
+#else
+#define GR_LOBE GR_D
+#endif
+
 GR_D V3 ld3(const float* p) { return V3{p[0], p[1], p[2]}; }
 
 // Local-frame trigonometry (core/vector.rs:137-213).
@@ -220,7 +230,7 @@ GR_D float microfacet_pdf(const DevLobe& L, V3 i, V3 h) {
 }
 
 // Lobe::f
-GR_D V3 lobe_f(const DevLobe& L, V3 i, V3 o, bool c2l) {
+GR_LOBE V3 lobe_f(const DevLobe& L, V3 i, V3 o, bool c2l) {
     switch (L.type) {
         case L_DISNEY_DIFFUSE: {  // lobes.rs:93-116
             V3 color = ld3(L.c0);
@@ -275,7 +285,7 @@ GR_D V3 lobe_f(const DevLobe& L, V3 i, V3 o, bool c2l) {
 }
 
 // Lobe::pdf
-GR_D float lobe_pdf(const DevLobe& L, V3 i, V3 o) {
+GR_LOBE float lobe_pdf(const DevLobe& L, V3 i, V3 o) {
     switch (L.type) {
         case L_GGX_DISNEY:
         case L_GTR1_SCHLICK: {  // lobes.rs:150-158
@@ -302,7 +312,7 @@ GR_D float lobe_pdf(const DevLobe& L, V3 i, V3 o) {
 }
 
 // Lobe::sample_f
-GR_D LobeSample lobe_sample(const DevLobe& L, V3 i, bool c2l, float u1, float u2) {
+GR_LOBE LobeSample lobe_sample(const DevLobe& L, V3 i, bool c2l, float u1, float u2) {
     LobeSample z{v3zero(), v3zero(), 0.0f};
     switch (L.type) {
         case L_GGX_DISNEY:

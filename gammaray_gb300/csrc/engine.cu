@@ -11,6 +11,9 @@ namespace gr {
 namespace {
 
 constexpr int EBLOCK = 128;
+#ifndef GR_SHADE_MIN_BLOCKS
+#define GR_SHADE_MIN_BLOCKS 6
+#endif
 constexpr int GATHER_BLOCKS = 512;
 
 GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t job,
@@ -31,64 +34,90 @@ GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, u
 }
 
 // Single thread: what to gather and how many paths to issue this iteration.
-__global__ void k_eng_plan(EngineCtl* c, const DevUnit* __restrict__ units, const uint32_t* __restrict__ unit_done,
-                           uint32_t arena) {
-    uint32_t u = c->g_lo, gn = 0;
-    uint32_t jobs_in[GATHER_MAX];
-    while (u < c->units_count && gn < GATHER_MAX) {
+__global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const DevUnit* __restrict__ units,
+                           const uint32_t* __restrict__ unit_done, uint32_t arena) {
+    // Finished units, consecutive from the oldest, grouped by job (pass order kept).
+    uint32_t u = c->g_lo, n = 0, groups = 0;
+    uint32_t gjob[GATHER_MAX];
+    uint32_t tmp[GATHER_MAX];
+    uint32_t tmp_group[GATHER_MAX];
+    while (u < c->units_count && n < GATHER_MAX) {
         DevUnit U = units[u];
         if (unit_done[u] < U.npix) break;
-        bool dup = false;
-        for (uint32_t k = 0; k < gn; ++k) dup |= jobs_in[k] == U.job;
-        if (dup) break;  // a job's passes are gathered one per iteration, in order
-        jobs_in[gn] = U.job;
-        c->gather_units[gn++] = u;
+        uint32_t g = 0;
+        while (g < groups && gjob[g] != U.job) ++g;
+        if (g == groups) {
+            gjob[groups] = U.job;
+            c->gather_group_count[groups] = 0;
+            ++groups;
+        }
+        c->gather_group_count[g] += 1;
+        tmp[n] = u;
+        tmp_group[n] = g;
+        ++n;
         ++u;
     }
-    c->gather_n = gn;
+    uint32_t first = 0, tiles = 0;
+    for (uint32_t g = 0; g < groups; ++g) {
+        c->gather_group_first[g] = first;
+        c->gather_group_tiles[g] = tiles;
+        const DevJob& J = jobs[gjob[g]];
+        tiles += ((J.width + FILM_TILE - 1) / FILM_TILE) * ((J.height + FILM_TILE - 1) / FILM_TILE);
+        first += c->gather_group_count[g];
+    }
+    uint32_t fill[GATHER_MAX];
+    for (uint32_t g = 0; g < groups; ++g) fill[g] = c->gather_group_first[g];
+    for (uint32_t k = 0; k < n; ++k) c->gather_units[fill[tmp_group[k]]++] = tmp[k];
+    c->gather_n = n;
+    c->gather_groups = groups;
+    c->gather_tiles = tiles;
     c->g_lo = u;
     c->gather_lo_prefix = u < c->units_count ? units[u].prefix : c->paths_total;
     unsigned long long freec = c->free_tail - c->free_head;
     unsigned long long rem = c->paths_total - c->gcur;
     unsigned long long lim = c->gather_lo_prefix + arena - c->gcur;  // arena slots not holding ungathered samples
-    unsigned long long n = min(freec, min(rem, lim));
-    c->fill_n = static_cast<uint32_t>(n);
+    unsigned long long nf = min(freec, min(rem, lim));
+    c->fill_n = static_cast<uint32_t>(nf);
     c->fill_base = c->gcur;
     c->fill_head = c->free_head;
-    c->gcur += n;
-    c->free_head += static_cast<uint32_t>(n);
+    c->gcur += nf;
+    c->free_head += static_cast<uint32_t>(nf);
     c->done = c->g_lo == c->units_count ? 1u : 0u;
     c->iter += 1;
 }
 
 struct ArenaIdx {
     unsigned long long prefix;
-    uint32_t width, arena;
+    uint32_t width, mask;
     GR_D size_t operator()(uint32_t r, uint32_t col) const {
-        return static_cast<size_t>((prefix + static_cast<unsigned long long>(r) * width + col) % arena);
+        return static_cast<size_t>((prefix + static_cast<unsigned long long>(r) * width + col) & mask);
     }
 };
 
 __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const EngineCtl* c, const DevJob* __restrict__ jobs,
                                                                     const DevUnit* __restrict__ units,
                                                                     const float2* __restrict__ a_st,
-                                                                    const float4* __restrict__ a_c, uint32_t arena) {
+                                                                    const float4* __restrict__ a_c, uint32_t mask) {
     __shared__ StagedSample sm[FILM_SPAN * FILM_SPAN];
-    const uint32_t gn = c->gather_n;
-    for (uint32_t g = 0; g < gn; ++g) {
-        DevUnit U = units[c->gather_units[g]];
-        const DevJob& J = jobs[U.job];
+    const uint32_t total = c->gather_tiles, groups = c->gather_groups;
+    for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
+        uint32_t g = 0;
+        while (g + 1 < groups && c->gather_group_tiles[g + 1] <= item) ++g;
+        const uint32_t t = item - c->gather_group_tiles[g];
+        const uint32_t first = c->gather_group_first[g], cnt = c->gather_group_count[g];
+        const DevJob& J = jobs[units[c->gather_units[first]].job];
         const uint32_t w = J.width, h = J.height;
-        const uint32_t tx = (w + FILM_TILE - 1) / FILM_TILE, tiles = tx * ((h + FILM_TILE - 1) / FILM_TILE);
-        for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
-            const int ox = static_cast<int>((t % tx) * FILM_TILE), oy = static_cast<int>((t / tx) * FILM_TILE);
-            const int x = ox + threadIdx.x % FILM_TILE, y = oy + threadIdx.x / FILM_TILE;
-            const bool inside = x < static_cast<int>(w) && y < static_cast<int>(h);
-            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (inside) acc = J.film[static_cast<size_t>(y) * w + x];
-            gather_tile(sm, a_st, a_c, w, h, ox, oy, acc, ArenaIdx{U.prefix, w, arena});
-            if (inside && J.live) J.film[static_cast<size_t>(y) * w + x] = acc;
+        const uint32_t tx = (w + FILM_TILE - 1) / FILM_TILE;
+        const int ox = static_cast<int>((t % tx) * FILM_TILE), oy = static_cast<int>((t / tx) * FILM_TILE);
+        const int x = ox + threadIdx.x % FILM_TILE, y = oy + threadIdx.x / FILM_TILE;
+        const bool inside = x < static_cast<int>(w) && y < static_cast<int>(h);
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (inside) acc = J.film[static_cast<size_t>(y) * w + x];
+        for (uint32_t k = 0; k < cnt; ++k) {  // the job's passes, in order
+            const DevUnit U = units[c->gather_units[first + k]];
+            gather_tile(sm, a_st, a_c, w, h, ox, oy, acc, ArenaIdx{U.prefix, w, mask});
         }
+        if (inside && J.live) J.film[static_cast<size_t>(y) * w + x] = acc;
     }
 }
 
@@ -174,7 +203,7 @@ __global__ void __launch_bounds__(BS) k_eng_extend(EngineCtl* c, int cur, const 
     }
 }
 
-__global__ void __launch_bounds__(EBLOCK) k_eng_shade(EngineCtl* c, int cur, const DevJob* __restrict__ jobs,
+__global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS) k_eng_shade(EngineCtl* c, int cur, const DevJob* __restrict__ jobs,
                                                       const DevUnit* __restrict__ units, uint32_t* unit_done,
                                                       uint32_t* free_ring, uint32_t cap, uint32_t arena,
                                                       const uint32_t* __restrict__ q_slot,
@@ -246,7 +275,7 @@ __global__ void __launch_bounds__(EBLOCK) k_eng_shade(EngineCtl* c, int cur, con
                 finished = true;
                 unit = s_unit[slot];
                 unsigned long long p = units[unit].prefix + s_pixel[slot];
-                size_t a = static_cast<size_t>(p % arena);
+                size_t a = static_cast<size_t>(p & (arena - 1));  // arena is a power of two
                 a_st[a] = s_st[slot];
                 a_c[a] = make_float4(L.x, L.y, L.z, 0.0f);
             }
@@ -335,7 +364,9 @@ gr_status Engine::init(const EngineConfig& cfg, cudaStream_t) {
         return GR_ERR_INVALID_ARGUMENT;
     }
     if (cfg_.capacity < 1024) cfg_.capacity = 1024;
-    arena_ = cfg_.arena ? cfg_.arena : 2 * cfg_.capacity + (1u << 22);
+    uint64_t want = cfg_.arena ? cfg_.arena : 2ull * cfg_.capacity + (1u << 22);
+    arena_ = 1u << 20;
+    while (arena_ < want && arena_ < (1u << 30)) arena_ <<= 1;  // power of two: the index is a mask
     GR_CUDA_TRY(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
     const size_t C = cfg_.capacity;
     auto alloc = [&](DevBuf& b, size_t bytes) -> cudaError_t {
@@ -378,10 +409,10 @@ gr_status Engine::enqueue_iteration(int cur) {
     EngineCtl* c = ctl_.as<EngineCtl>();
     const uint32_t C = cfg_.capacity;
     const int nxt = cur ^ 1;
-    k_eng_plan<<<1, 1, 0, st_>>>(c, units_.as<DevUnit>(), unit_done_.as<uint32_t>(), arena_);
+    k_eng_plan<<<1, 1, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), arena_);
     GR_CUDA_TRY(cudaGetLastError());
     k_eng_gather<<<GATHER_BLOCKS, FILM_TILE * FILM_TILE, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(),
-                                                                   a_st_.as<float2>(), a_c_.as<float4>(), arena_);
+                                                                   a_st_.as<float2>(), a_c_.as<float4>(), arena_ - 1);
     GR_CUDA_TRY(cudaGetLastError());
     int fgrid = grid_for(reinterpret_cast<const void*>(k_eng_fill), EBLOCK, 0, C);
     k_eng_fill<<<fgrid, EBLOCK, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), free_ring_.as<uint32_t>(), C,

@@ -3,9 +3,10 @@
 // Many renders ("jobs": a scene, a camera, settings and a film) share one pool of path
 // slots.  Each job's work is a list of units, one per pass; units are issued in a global
 // order (round-robin over jobs, pass by pass).  Every iteration:
-//   plan    (1 thread) picks the finished units to gather (consecutive from the oldest,
-//           at most one per job) and how many new paths to issue into free slots
-//   gather  splats the picked units into their films (the deterministic tile gather)
+//   plan    (1 thread) picks the finished units to gather (consecutive from the oldest)
+//           and how many new paths to issue into free slots
+//   gather  splats the picked units into their films (the deterministic tile gather);
+//           each film tile adds its job's units in pass order
 //   fill    turns free slots into new camera paths (jitter, camera ray)
 //   extend  closest hit for the queued rays of all jobs
 //   shade   path-tracer shading per job; finished paths write their sample into a ring
@@ -42,7 +43,7 @@ struct DevUnit {
     uint32_t pad;
 };
 
-constexpr int GATHER_MAX = 64;
+constexpr int GATHER_MAX = 256;
 
 struct EngineCtl {
     unsigned long long paths_total;  // paths of all units appended so far
@@ -56,11 +57,16 @@ struct EngineCtl {
     uint32_t free_head, free_tail;
     uint32_t q[2];
     uint32_t fill_n, fill_head;
-    uint32_t gather_n;
+    uint32_t gather_n;       // units to gather this iteration, grouped by job
+    uint32_t gather_groups;  // distinct jobs among them
     uint32_t done;
     int32_t err;
     uint32_t iter;
-    uint32_t gather_units[GATHER_MAX];
+    uint32_t gather_units[GATHER_MAX];      // unit indices, each job's units contiguous and in pass order
+    uint32_t gather_group_first[GATHER_MAX];  // per group: first entry in gather_units
+    uint32_t gather_group_count[GATHER_MAX];
+    uint32_t gather_group_tiles[GATHER_MAX];  // per group: cumulative film tiles (exclusive prefix)
+    uint32_t gather_tiles;                    // total film tiles of all groups
 };
 
 struct EngineConfig {

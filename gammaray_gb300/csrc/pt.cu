@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
     q_d[i] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
-__global__ void __launch_bounds__(BLOCK) k_shade(DeviceScene s, PTParams p, uint32_t depth,
+
+__global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t depth,
                                                  const uint32_t* __restrict__ count_in,
                                                  const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
                                                  const float4* __restrict__ q_d, const float4* __restrict__ q_hit,
