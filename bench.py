@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--height", type=int, default=1024)
     ap.add_argument("--spp", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--bvh-width", type=int, default=0, help="device BVH width (2, 4, 8); 0 = library default")
+    ap.add_argument("--leaf-size", type=int, default=0, help="primitives per wide leaf; 0 = library default")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-requests", type=int, default=24)
@@ -172,7 +174,7 @@ def run_reference(args, rank):
 def config_of(w):
     return {"workload": "pt_displaced_sphere_102k", "width": w.width, "height": w.height, "spp": w.spp,
             "max_depth": w.integrator.max_depth, "triangles": w.num_triangles(), "integrator": "path_tracer",
-            "bvh": "reference SAH, collapsed to width 4", "l2": "flushed (256 MiB write) between timed steps",
+            "bvh": "reference SAH, collapsed to a wide BVH", "l2": "flushed (256 MiB write) between timed steps",
             "unit_of_step": "one complete render"}
 
 
@@ -307,7 +309,8 @@ def run_ours(args, rank, world, local):
         dist.init_process_group("nccl")
     lib = g.load()
     w = workload(args)
-    st = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1)
+    st = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1, bvh_width=args.bvh_width,
+                 leaf_size=args.leaf_size)
     info = st.info()
     film = g.Film(w.width, w.height, lib=lib)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")

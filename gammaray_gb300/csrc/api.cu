@@ -22,6 +22,13 @@ static gr_status fail(gr_status s, const std::string& msg) {
     return s;
 }
 
+DeviceWork& device_work() {
+    static DeviceWork work[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return work[dev < 0 || dev >= 64 ? 0 : dev];
+}
+
 gr_status sync_check(cudaStream_t st, const char* what, uint32_t bounce, uint32_t n) {
     static const double limit = [] {
         const char* e = std::getenv("GR_SYNC_CHECK");
@@ -419,8 +426,9 @@ static gr_status run_render(gr_scene* s, const gr_camera* c, const gr_render_par
     job.samples_out = samples_out;
     cudaStream_t st = s->stream;
     std::memset(&s->stats, 0, sizeof(s->stats));
-    GR_CUDA_TRY(s->paths.ensure(1));
-    GR_CUDA_TRY(cudaMemsetAsync(s->paths.counters.ptr, 0, NUM_COUNTERS * sizeof(uint32_t), st));
+    GR_CUDA_TRY(s->counters.ensure(NUM_COUNTERS * sizeof(uint32_t)));
+    GR_CUDA_TRY(cudaMemsetAsync(s->counters.ptr, 0, NUM_COUNTERS * sizeof(uint32_t), st));
+    std::lock_guard<std::mutex> work_lock(device_work().mu);
     GR_CUDA_TRY(cudaEventRecord(s->ev0, st));
     gr_status r = p->integrator == GR_INTEGRATOR_BDPT ? render_bdpt(s, job, st) : render_pt(s, job, st);
     if (r != GR_OK) {
@@ -429,7 +437,7 @@ static gr_status run_render(gr_scene* s, const gr_camera* c, const gr_render_par
     }
     GR_CUDA_TRY(cudaEventRecord(s->ev1, st));
     uint32_t cnt[NUM_COUNTERS];
-    GR_CUDA_TRY(cudaMemcpyAsync(cnt, s->paths.counters.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+    GR_CUDA_TRY(cudaMemcpyAsync(cnt, s->counters.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, st));
     GR_CUDA_TRY(cudaStreamSynchronize(st));
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
@@ -494,8 +502,8 @@ gr_status gr_trace_rays(gr_scene* s, const float* rays, uint64_t n, gr_hit* hits
 
 gr_status gr_trace_rays_dev(gr_scene* s, const float* rays, uint64_t n, gr_hit* hits, void* stream) {
     if (!s || (n && (!rays || !hits))) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
-    GR_CUDA_TRY(s->paths.ensure(1));
-    int* err = reinterpret_cast<int*>(s->paths.counters.as<uint32_t>() + CNT_ERROR);
+    GR_CUDA_TRY(s->counters.ensure(NUM_COUNTERS * sizeof(uint32_t)));
+    int* err = reinterpret_cast<int*>(s->counters.as<uint32_t>() + CNT_ERROR);
     return launch_trace(s->dev, rays, n, hits, false, nullptr, err, static_cast<cudaStream_t>(stream));
 }
 

@@ -383,6 +383,16 @@ cudaError_t BdptState::ensure(size_t paths, uint32_t max_len) {
     size_t slots = 2 * paths;
     size_t pairs = static_cast<size_t>(max_pairs(max_len)) * paths;
     cudaError_t e;
+    for (int k = 0; k < 2; ++k) {
+        if ((e = q_slot[k].ensure(slots * sizeof(uint32_t))) != cudaSuccess) return e;
+        if ((e = q_o[k].ensure(slots * sizeof(float4))) != cudaSuccess) return e;
+        if ((e = q_d[k].ensure(slots * sizeof(float4))) != cudaSuccess) return e;
+    }
+    if ((e = q_hit.ensure(slots * sizeof(float4))) != cudaSuccess) return e;
+    if ((e = tp.ensure(slots * sizeof(float4))) != cudaSuccess) return e;
+    if ((e = key.ensure(paths * sizeof(unsigned long long))) != cudaSuccess) return e;
+    if ((e = st.ensure(paths * sizeof(float2))) != cudaSuccess) return e;
+    if ((e = light.ensure(paths * sizeof(float4))) != cudaSuccess) return e;
     if ((e = verts.ensure(slots * max_len * VREC * sizeof(float4))) != cudaSuccess) return e;
     if ((e = vcount.ensure(slots * sizeof(uint32_t))) != cudaSuccess) return e;
     if ((e = flags.ensure(paths * sizeof(uint32_t))) != cudaSuccess) return e;
@@ -407,11 +417,10 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     uint32_t target = env && std::atoi(env) > 0 ? static_cast<uint32_t>(std::atoi(env)) : (1u << 19);
     uint32_t group = std::max(1u, std::min(total, target / std::max(1u, npix)));
     const size_t npaths = static_cast<size_t>(group) * npix;
-    PathState& ps = sc->paths;
-    GR_CUDA_TRY(ps.ensure(2 * npaths));
-    GR_CUDA_TRY(sc->bdpt.ensure(npaths, max_len));
-    BdptState& bs = sc->bdpt;
-    uint32_t* cnt = ps.counters.as<uint32_t>();
+    BdptState& bs = device_work().bdpt;
+    GR_CUDA_TRY(bs.ensure(npaths, max_len));
+    BdptState& ps = bs;
+    uint32_t* cnt = sc->counters.as<uint32_t>();
     int* err = reinterpret_cast<int*>(cnt + CNT_ERROR);
     unsigned long long* rays = reinterpret_cast<unsigned long long*>(cnt + CNT_RAYS);
     unsigned long long* shadow = reinterpret_cast<unsigned long long*>(cnt + CNT_SHADOW);

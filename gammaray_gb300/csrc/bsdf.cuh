@@ -9,10 +9,9 @@
 
 namespace gr {
 
-// The lobe entry points are called from several places of the mixture (the chosen
-// lobe, then every other lobe's f and pdf).  Inlined everywhere they make the shading
-// kernels large enough to thrash the instruction cache; GR_LOBE_CALLS builds them as
-// real calls instead.
+// Lobe::f and Lobe::pdf are inlined; the sampling mixture calls each from one place
+// only, to keep the shading kernels small enough for the instruction cache.
+// GR_LOBE_CALLS builds them as real calls instead (measured slower).
 #ifdef GR_LOBE_CALLS
 #define GR_LOBE static __device__ __noinline__
 #else
@@ -54,6 +53,15 @@ GR_D V3 refract(V3 v, V3 n, float eta) {  // core/vector.rs:253-264
     return V3{a.x + n.x * k, a.y + n.y * k, a.z + n.z * k};
 }
 
+// cosf and sinf of one angle.  Out of line so that the full-range argument reduction
+// of both exists once in each shading kernel instead of at every sampler.
+// Returns (cos a, sin a) by value, in registers.  GR_TRIG_INLINE inlines it instead.
+#ifdef GR_TRIG_INLINE
+GR_D float2 cos_sin(float a) { return make_float2(cosf(a), sinf(a)); }
+#else
+static __device__ __noinline__ float2 cos_sin(float a) { return make_float2(cosf(a), sinf(a)); }
+#endif
+
 // core/random.rs:28-106
 GR_D void area_sample_disk(float u1, float u2, float& dx, float& dy) {
     float sx = -1.0f + 2.0f * u1;
@@ -71,8 +79,9 @@ GR_D void area_sample_disk(float u1, float u2, float& dx, float& dy) {
         r = sy;
         theta = FRAC_PI_2 - FRAC_PI_4 * (sx / sy);
     }
-    dx = r * cosf(theta);
-    dy = r * sinf(theta);
+    float2 cs = cos_sin(theta);
+    dx = r * cs.x;
+    dy = r * cs.y;
 }
 GR_D V3 cosine_sample_hemisphere(bool flipped, float u1, float u2) {
     float x, y;
@@ -141,8 +150,9 @@ GR_D void ggx_sample11(float cos_theta, float u1, float u2, float& sx, float& sy
     if (cos_theta > 0.9999f) {
         float r = sqrtf(u1 / (1.0f - u1));
         float phi = TWO_PI * u2;
-        sx = r * cosf(phi);
-        sy = r * sinf(phi);
+        float2 cs = cos_sin(phi);
+        sx = r * cs.x;
+        sy = r * cs.y;
         return;
     }
     float s = sqrtf(fmaxf(0.0f, 1.0f - cos_theta * cos_theta));
@@ -200,16 +210,12 @@ GR_D V3 gtr1_sample_half(float alpha, V3 i, float u1, float u2) {
     float phi = 2.0f * PI * u1;
     float c = sqrtf(clamp_unit(1.0f - powf(a2, 1.0f - u2) / (1.0f - a2)));
     float s = sqrtf(1.0f - c * c);  // Vec::from_spherical (core/vector.rs:21-24)
-    V3 h = V3{s * cosf(phi), s * sinf(phi), c};
+    float2 cs = cos_sin(phi);
+    V3 h = V3{s * cs.x, s * cs.y, c};
     return same_hemisphere(h, i) ? h : -h;
 }
 
 // -------------------------------------------------------------- lobe dispatch
-struct LobeSample {
-    V3 result, outgoing;
-    float pdf;
-};
-
 GR_D V3 microfacet_fresnel(const DevLobe& L, float c) {
     if (L.type == L_GGX_DISNEY) {  // DisneyFresnel (util.rs:72-78)
         V3 spec = ld3(L.c1);
@@ -311,38 +317,44 @@ GR_LOBE float lobe_pdf(const DevLobe& L, V3 i, V3 o) {
     }
 }
 
-// Lobe::sample_f
-GR_LOBE LobeSample lobe_sample(const DevLobe& L, V3 i, bool c2l, float u1, float u2) {
-    LobeSample z{v3zero(), v3zero(), 0.0f};
+// Lobe::sample_f, direction part.  Returns how the chosen lobe's value and pdf follow:
+// SAMPLE_NONE (the sampler gave up: value, direction and pdf are zero), SAMPLE_PDF_GIVEN
+// (microfacet reflection: the pdf is the sampler's, from the sampled half vector) or
+// SAMPLE_PDF_EVAL (the pdf is Lobe::pdf of the sampled direction).  The value is always
+// Lobe::f of the sampled direction, evaluated by the caller.
+enum : int { SAMPLE_NONE = 0, SAMPLE_PDF_GIVEN = 1, SAMPLE_PDF_EVAL = 2 };
+
+GR_D int lobe_direction(const DevLobe& L, V3 i, float u1, float u2, V3& o, float& pdf) {
+    o = v3zero();
+    pdf = 0.0f;
     switch (L.type) {
         case L_GGX_DISNEY:
         case L_GTR1_SCHLICK: {  // lobes.rs:160-184
-            if (i.z == 0.0f) return z;
+            if (i.z == 0.0f) return SAMPLE_NONE;
             V3 h = L.type == L_GGX_DISNEY ? ggx_sample_half(L.p[0], L.p[1], i, u1, u2)
                                           : gtr1_sample_half(L.p[0], i, u1, u2);
-            V3 o = reflect(i, h);
-            if (!same_hemisphere(i, o)) return z;
-            V3 r = lobe_f(L, i, o, c2l);
-            float p = microfacet_pdf(L, i, h) / (4.0f * dot(i, h));
-            return LobeSample{r, o, p};
+            V3 r = reflect(i, h);
+            if (!same_hemisphere(i, r)) return SAMPLE_NONE;
+            o = r;
+            pdf = microfacet_pdf(L, i, h) / (4.0f * dot(i, h));
+            return SAMPLE_PDF_GIVEN;
         }
         case L_SPECULAR_TRANS: {  // lobes.rs:351-388
-            if (i.z == 0.0f) return z;
+            if (i.z == 0.0f) return SAMPLE_NONE;
             V3 h = ggx_sample_half(L.p[0], L.p[1], i, u1, u2);
             float ior = L.p[2];
             float eta = i.z > 0.0f ? 1.0f / ior : ior;
-            V3 o = refract(i, h, eta);
-            if (is_zero(o)) return z;
-            return LobeSample{lobe_f(L, i, o, c2l), o, lobe_pdf(L, i, o)};
+            V3 r = refract(i, h, eta);
+            if (is_zero(r)) return SAMPLE_NONE;
+            o = r;
+            return SAMPLE_PDF_EVAL;
         }
-        case L_PERFECT_MIRROR: {  // lobes.rs:440-452
-            V3 o = V3{-i.x, -i.y, i.z};
-            return LobeSample{lobe_f(L, i, o, c2l), o, 1.0f};
-        }
-        default: {  // lobes.rs:54-68
-            V3 o = cosine_sample_hemisphere(i.z < 0.0f, u1, u2);
-            return LobeSample{lobe_f(L, i, o, c2l), o, lobe_pdf(L, i, o)};
-        }
+        case L_PERFECT_MIRROR:  // lobes.rs:440-452 (Lobe::pdf of a mirror is 1)
+            o = V3{-i.x, -i.y, i.z};
+            return SAMPLE_PDF_EVAL;
+        default:  // lobes.rs:54-68
+            o = cosine_sample_hemisphere(i.z < 0.0f, u1, u2);
+            return SAMPLE_PDF_EVAL;
     }
 }
 
@@ -357,6 +369,7 @@ GR_D V3 f_world(const DevMaterial& m, V3 wi, V3 wo, const Frame& f, bool c2l) { 
     V3 ol = world_to_local(wo, f.tangent, f.binormal, f.normal);
     bool refl = (dot(wi, f.geom_normal) * dot(wo, f.geom_normal)) > 0.0f;
     V3 r = v3zero();
+#pragma unroll 1
     for (int k = 0; k < m.n_lobes; ++k) {
         uint32_t kind = m.lobe[k].kind;
         if ((refl && (kind & LOBE_REFLECTION)) || (!refl && (kind & LOBE_TRANSMISSION)))
@@ -371,6 +384,7 @@ GR_D float pdf_world(const DevMaterial& m, V3 wi, V3 wo, const Frame& f) {  // m
     V3 ol = world_to_local(wo, f.tangent, f.binormal, f.normal);
     if (il.z == 0.0f) return 0.0f;
     float p = 0.0f;
+#pragma unroll 1
     for (int k = 0; k < m.n_lobes; ++k) p += lobe_pdf(m.lobe[k], il, ol);
     return p / static_cast<float>(m.n_lobes);
 }
@@ -389,6 +403,13 @@ struct MaterialSample {
 };
 
 // material.rs:140-235.  u0 picks the lobe, u1 and u2 feed the lobe's sampler.
+//
+// The reference sums the chosen lobe's value and pdf first, then every other lobe's in
+// index order.  One loop does all of it: step -1 is the chosen lobe, steps 0..n-1 the
+// others, so Lobe::f and Lobe::pdf each have a single call site.  Inlined at every place
+// the mixture uses them, they made the shading kernels too large for the instruction
+// cache.  The first term is assigned rather than added to zero, so the sums (and the
+// signs of zeros) are the reference's.
 GR_D MaterialSample sample_world(const DevMaterial& m, V3 wi, const Frame& f, bool c2l, float u0, float u1,
                                  float u2) {
     V3 il = world_to_local(wi, f.tangent, f.binormal, f.normal);
@@ -396,26 +417,33 @@ GR_D MaterialSample sample_world(const DevMaterial& m, V3 wi, const Frame& f, bo
     int n = m.n_lobes;
     if (n == 0) return MaterialSample{emission, v3zero(), v3zero(), 1.0f, LOBE_NONE};
     int r = static_cast<int>(range_index(u0, static_cast<uint32_t>(n)));
-    const DevLobe& L = m.lobe[r];
-    LobeSample s = lobe_sample(L, il, c2l, u1, u2);
-    V3 ow = local_to_world(s.outgoing, f.tangent, f.binormal, f.normal);
-    V3 radiance = s.result;
-    float pdf = s.pdf;
-    uint32_t kind = L.kind;
-    if (!(kind & LOBE_SPECULAR)) {
-        for (int k = 0; k < n; ++k)
-            if (k != r) pdf += lobe_pdf(m.lobe[k], il, s.outgoing);
-    }
-    pdf /= static_cast<float>(n);
-    if (!(kind & LOBE_SPECULAR)) {
+    uint32_t kind = m.lobe[r].kind;
+    V3 o;
+    float given_pdf;
+    int how = lobe_direction(m.lobe[r], il, u1, u2, o, given_pdf);
+    V3 ow = local_to_world(o, f.tangent, f.binormal, f.normal);
+    const bool mix = !(kind & LOBE_SPECULAR);
+    bool gate = false;
+    if (mix) {
         bool refl = (dot(wi, f.geom_normal) * dot(ow, f.geom_normal)) > 0.0f;
         // material.rs:203-206: the gate tests the chosen lobe's kind for every lobe (kept).
-        bool gate = (refl && (kind & LOBE_REFLECTION)) || (!refl && (kind & LOBE_TRANSMISSION));
-        if (gate) {
-            for (int k = 0; k < n; ++k)
-                if (k != r) radiance = radiance + lobe_f(m.lobe[k], il, s.outgoing, c2l);
+        gate = (refl && (kind & LOBE_REFLECTION)) || (!refl && (kind & LOBE_TRANSMISSION));
+    }
+    V3 radiance = v3zero();
+    float pdf = 0.0f;
+#pragma unroll 1
+    for (int j = -1; j < n; ++j) {
+        const bool first = j < 0;
+        if (first ? how == SAMPLE_NONE : (!mix || j == r)) continue;
+        const DevLobe& L = m.lobe[first ? r : j];
+        float pk = first && how == SAMPLE_PDF_GIVEN ? given_pdf : lobe_pdf(L, il, o);
+        pdf = first ? pk : pdf + pk;
+        if (first || gate) {
+            V3 fk = lobe_f(L, il, o, c2l);
+            radiance = first ? fk : radiance + fk;
         }
     }
+    pdf /= static_cast<float>(n);
     if (pdf == 0.0f) return MaterialSample{emission, v3zero(), ow, 1.0f, LOBE_NONE};
     return MaterialSample{emission, radiance, ow, pdf, kind};
 }

@@ -66,6 +66,27 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
 }
 
 
+// Material-sorted shading.  Each block takes the queue in chunks of SHADE_CHUNK entries,
+// gives every entry a bucket (0: the ray escaped; else a hash of the hit's material and
+// the lobe its sample will pick), counting-sorts the chunk by bucket in shared memory
+// and shades it in that order.  Warps then run one material's one lobe sampler instead
+// of a mix of all of them.  The order only decides which thread shades which path:
+// every path's arithmetic and its queue slot are unchanged.
+constexpr uint32_t SHADE_PER_THREAD = 4;
+constexpr uint32_t SHADE_CHUNK = BLOCK * SHADE_PER_THREAD;
+constexpr uint32_t SHADE_BUCKETS = 32;
+static_assert(SHADE_CHUNK <= 65536, "chunk positions are 16-bit");
+
+GR_D uint32_t shade_bucket(const DeviceScene& s, float4 h, uint64_t key, uint32_t dim) {
+    int32_t k = __float_as_int(h.y);
+    if (k < 0) return 0;
+    uint32_t prim = __float_as_uint(__ldg(s.prims + 3 * static_cast<size_t>(k)).w);
+    uint32_t mat = __ldg(s.prim_material + prim);
+    uint32_t nl = static_cast<uint32_t>(s.materials[mat].n_lobes);
+    uint32_t r = nl ? range_index(uniform01(key, dim), nl) : 0;
+    return 1 + (mat * MAX_LOBES + r) % (SHADE_BUCKETS - 1);
+}
+
 __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t depth,
                                                  const uint32_t* __restrict__ count_in,
                                                  const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
@@ -74,48 +95,88 @@ __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t dept
                                                  const unsigned long long* __restrict__ key_buf, uint32_t* count_out,
                                                  uint32_t* __restrict__ nslot, float4* __restrict__ no,
                                                  float4* __restrict__ nd) {
+    __shared__ uint32_t s_start[SHADE_BUCKETS];
+    __shared__ uint16_t s_order[SHADE_CHUNK];
     const uint32_t n = *count_in;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    // Warp-uniform trip count so every lane reaches the ballot in push_warp.
-    for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
-        uint32_t q = b + (threadIdx.x & 31u);
-        bool alive = false;
-        uint32_t slot = 0;
-        V3 new_o = v3zero(), new_d = v3zero();
-        if (q < n) {
-            slot = q_slot[q];
-            float4 h = q_hit[q];
-            float4 o4 = q_o[q], d4 = q_d[q];
-            V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
-            float4 tp4 = tp_buf[slot], L4 = L_buf[slot];
-            V3 tp = V3{tp4.x, tp4.y, tp4.z}, L = V3{L4.x, L4.y, L4.z};
-            int32_t k = __float_as_int(h.y);
-            if (k < 0) {
-                if (s.has_env) L = L + mul(tp, V3{s.env[0], s.env[1], s.env[2]});
-            } else {
-                uint32_t prim;
-                Frame f = hit_frame(s, k, o, d, h.x, h.z, h.w, prim);
-                const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
-                uint64_t key = key_buf[slot];
-                uint32_t base = DIM_CAMERA_WALK + 4 * depth;
-                MaterialSample ms = sample_world(m, -d, f, true, uniform01(key, base), uniform01(key, base + 1),
-                                                 uniform01(key, base + 2));
-                L = L + mul(tp, ms.emission);
-                tp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
-                new_o = nudge(o + (d * h.x), ms.outgoing);
-                new_d = ms.outgoing;
-                if (depth > p.rr_depth || nearly_zero(tp)) {
-                    float rv = uniform01(key, base + 3);
-                    float lum = luminance(tp);
-                    float prob = depth > p.rr_aggr ? clamped_lerp(0.10f, 0.75f, lum) : clamped_lerp(0.25f, 1.00f, lum);
-                    tp = rv < prob ? tp / prob : v3zero();
-                }
-                alive = !is_zero(tp) && (p.max_depth == 0 || depth + 1 < p.max_depth);
-                if (alive) tp_buf[slot] = make_float4(tp.x, tp.y, tp.z, 0.0f);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t base = DIM_CAMERA_WALK + 4 * depth;
+    // Block-uniform chunk loop (the barriers below need every thread).
+    for (uint32_t c0 = blockIdx.x * SHADE_CHUNK; c0 < n; c0 += gridDim.x * SHADE_CHUNK) {
+        const uint32_t cn = min(SHADE_CHUNK, n - c0);
+        if (tid < SHADE_BUCKETS) s_start[tid] = 0;
+        __syncthreads();
+        uint32_t bucket[SHADE_PER_THREAD], rank[SHADE_PER_THREAD];
+#pragma unroll
+        for (uint32_t e = 0; e < SHADE_PER_THREAD; ++e) {
+            uint32_t i = e * BLOCK + tid;
+            bucket[e] = 0;
+            rank[e] = 0;
+            if (i < cn) {
+                uint32_t q = c0 + i;
+                bucket[e] = shade_bucket(s, q_hit[q], key_buf[q_slot[q]], base);
+                rank[e] = atomicAdd(&s_start[bucket[e]], 1u);
             }
-            L_buf[slot] = make_float4(L.x, L.y, L.z, 0.0f);
         }
-        push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
+        __syncthreads();
+        if (tid < 32) {  // exclusive scan of the bucket counts (SHADE_BUCKETS == 32)
+            uint32_t c = s_start[tid], x = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (static_cast<int>(tid) >= o) x += y;
+            }
+            s_start[tid] = x - c;
+        }
+        __syncthreads();
+#pragma unroll
+        for (uint32_t e = 0; e < SHADE_PER_THREAD; ++e) {
+            uint32_t i = e * BLOCK + tid;
+            if (i < cn) s_order[s_start[bucket[e]] + rank[e]] = static_cast<uint16_t>(i);
+        }
+        __syncthreads();
+        // Every lane runs every step so that all of them reach the ballot in push_warp.
+        for (uint32_t e = 0; e < SHADE_PER_THREAD; ++e) {
+            uint32_t i = e * BLOCK + tid;
+            bool alive = false;
+            uint32_t slot = 0;
+            V3 new_o = v3zero(), new_d = v3zero();
+            if (i < cn) {
+                uint32_t q = c0 + s_order[i];
+                slot = q_slot[q];
+                float4 h = q_hit[q];
+                float4 o4 = q_o[q], d4 = q_d[q];
+                V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
+                float4 tp4 = tp_buf[slot], L4 = L_buf[slot];
+                V3 tp = V3{tp4.x, tp4.y, tp4.z}, L = V3{L4.x, L4.y, L4.z};
+                int32_t k = __float_as_int(h.y);
+                if (k < 0) {
+                    if (s.has_env) L = L + mul(tp, V3{s.env[0], s.env[1], s.env[2]});
+                } else {
+                    uint32_t prim;
+                    Frame f = hit_frame(s, k, o, d, h.x, h.z, h.w, prim);
+                    const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
+                    uint64_t key = key_buf[slot];
+                    MaterialSample ms = sample_world(m, -d, f, true, uniform01(key, base), uniform01(key, base + 1),
+                                                     uniform01(key, base + 2));
+                    L = L + mul(tp, ms.emission);
+                    tp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
+                    new_o = nudge(o + (d * h.x), ms.outgoing);
+                    new_d = ms.outgoing;
+                    if (depth > p.rr_depth || nearly_zero(tp)) {
+                        float rv = uniform01(key, base + 3);
+                        float lum = luminance(tp);
+                        float prob =
+                            depth > p.rr_aggr ? clamped_lerp(0.10f, 0.75f, lum) : clamped_lerp(0.25f, 1.00f, lum);
+                        tp = rv < prob ? tp / prob : v3zero();
+                    }
+                    alive = !is_zero(tp) && (p.max_depth == 0 || depth + 1 < p.max_depth);
+                    if (alive) tp_buf[slot] = make_float4(tp.x, tp.y, tp.z, 0.0f);
+                }
+                L_buf[slot] = make_float4(L.x, L.y, L.z, 0.0f);
+            }
+            push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
+        }
+        __syncthreads();  // s_start and s_order are reused by the next chunk
     }
 }
 
@@ -151,13 +212,15 @@ __global__ void k_samples_out(uint32_t n, const float2* __restrict__ st, const f
 uint32_t paths_in_flight_target() {
     const char* e = std::getenv("GR_PATHS_IN_FLIGHT");
     if (e && std::atoi(e) > 0) return static_cast<uint32_t>(std::atoi(e));
-    return 1u << 21;
+    // 64 M paths (about 9 GB): a 64-spp megapixel render is one group with one tail;
+    // measured faster than 16 M (4 groups) and 32 M on that workload.
+    return 1u << 26;
 }
 
 }  // namespace
 
 cudaError_t PathState::ensure(size_t n) {
-    if (n <= capacity && counters.ptr) return cudaSuccess;
+    if (n <= capacity && q_hit.ptr) return cudaSuccess;
     cudaError_t e;
 #define GR_ENS(buf, bytes)                  \
     if ((e = (buf).ensure(bytes)) != cudaSuccess) return e;
@@ -171,7 +234,6 @@ cudaError_t PathState::ensure(size_t n) {
         GR_ENS(q_d[k], n * sizeof(float4));
     }
     GR_ENS(q_hit, n * sizeof(float4));
-    GR_ENS(counters, NUM_COUNTERS * sizeof(uint32_t));
 #undef GR_ENS
     capacity = n;
     return cudaSuccess;
@@ -185,9 +247,9 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     if (total == 0) return GR_OK;
     uint32_t group = std::max(1u, std::min(total, paths_in_flight_target() / std::max(1u, npix)));
     if (static_cast<uint64_t>(group) * npix > 0xFFFFFFFFull / 2) group = 1;
-    PathState& ps = sc->paths;
+    PathState& ps = device_work().paths;
     GR_CUDA_TRY(ps.ensure(static_cast<size_t>(group) * npix));
-    uint32_t* cnt = ps.counters.as<uint32_t>();
+    uint32_t* cnt = sc->counters.as<uint32_t>();
     int* err = reinterpret_cast<int*>(cnt + CNT_ERROR);
     unsigned long long* rays = reinterpret_cast<unsigned long long*>(cnt + CNT_RAYS);
     uint32_t* host_cnt = nullptr;
@@ -272,7 +334,7 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
             if (timed) GR_TRY_S(mark(e0));
-            int grid = resident_grid(k_shade, 0, n);
+            int grid = resident_grid(k_shade, 0, (n + SHADE_PER_THREAD - 1) / SHADE_PER_THREAD);
             k_shade<<<grid, BLOCK, 0, st>>>(job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                             ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
                                             ps.q_hit.as<float4>(), ps.tp.as<float4>(), ps.light.as<float4>(),
@@ -473,7 +535,7 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
                 break;
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            int grid = resident_grid(k_shade, 0, n);
+            int grid = resident_grid(k_shade, 0, (n + SHADE_PER_THREAD - 1) / SHADE_PER_THREAD);
             k_shade<<<grid, BLOCK, 0, st>>>(sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit, tp,
                                             light, key, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt]);
             GR_CUDA_TRY(cudaGetLastError());

@@ -52,20 +52,30 @@ struct DevBuf {
     }
 };
 
-// Wavefront path state, reused across renders of a scene (grown on demand).
+// Path-tracer wavefront state, reused across renders of a scene (grown on demand).
 struct PathState {
-    DevBuf tp, light, key, st;       // per slot: throughput, radiance, random key, film (s, t)
-    DevBuf q_slot[2], q_o[2], q_d[2], q_hit;  // ping-pong queues
-    DevBuf counters;                 // [0..1] queue counts, [2] error flag, [3..] stats
+    DevBuf tp, light, key, st;                // per slot: throughput, radiance, random key, film (s, t)
+    DevBuf q_slot[2], q_o[2], q_d[2], q_hit;  // ping-pong queues of live slots and their rays
     size_t capacity = 0;
     cudaError_t ensure(size_t n);
 };
 
-// BDPT vertex storage, strategy entries and the shadow queue (grown on demand).
+// BDPT walk queues, vertex storage, strategy entries and the shadow queue (grown on
+// demand).  Walks are addressed by slot (2 per path: camera, light).
 struct BdptState {
+    DevBuf q_slot[2], q_o[2], q_d[2], q_hit, tp, key, st, light;
     DevBuf verts, vcount, flags, escape, entry_base, entries, shadow;
     cudaError_t ensure(size_t paths, uint32_t max_len);
 };
+
+// The large wavefront buffers are shared by every scene on a device (renders on one
+// GPU run one after another anyway); a scene keeps only its small counter block.
+struct DeviceWork {
+    std::mutex mu;
+    PathState paths;
+    BdptState bdpt;
+};
+DeviceWork& device_work();  // of the current device
 
 constexpr int CNT_QUEUE0 = 0;
 constexpr int CNT_QUEUE1 = 1;
@@ -87,8 +97,7 @@ struct gr_scene {
     gr::HostBuild host;
     gr::SceneBuffers buf;
     gr::DeviceScene dev{};
-    gr::PathState paths;
-    gr::BdptState bdpt;
+    gr::DevBuf counters;  // [0..1] queue counts, [2] error flag, [3..] stats (gr::CNT_*)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     gr_render_stats stats{};

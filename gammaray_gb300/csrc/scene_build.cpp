@@ -384,7 +384,7 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
         err = "bvh_width must be 2, 4 or 8";
         return false;
     }
-    uint32_t L = desc.leaf_size ? desc.leaf_size : 4;
+    uint32_t L = desc.leaf_size ? desc.leaf_size : 2;  // 2 measured fastest (width 4) on the bench workload
     if (L < 1 || L > static_cast<uint32_t>(MAX_LEAF_PRIMS)) {
         err = "leaf_size must be in [1, 16]";
         return false;
