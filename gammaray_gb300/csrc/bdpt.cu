@@ -18,6 +18,7 @@
 #include <cstdlib>
 
 #include "runtime.hpp"
+#include "shade_sort.cuh"
 #include "wavefront.cuh"
 
 namespace gr {
@@ -168,6 +169,9 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams
     push_warp(light_alive, count_out, 2 * i + 1, lo, ld, nslot, no, nd);
 }
 
+constexpr uint32_t BSHADE_PER_THREAD = 4;
+constexpr uint32_t BSHADE_CHUNK = BLOCK * BSHADE_PER_THREAD;
+
 __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts vs,
                                                       const uint32_t* __restrict__ count_in,
                                                       const uint32_t* __restrict__ q_slot,
@@ -178,62 +182,76 @@ __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts 
                                                       uint32_t* __restrict__ flags, float4* __restrict__ escape,
                                                       uint32_t* count_out, uint32_t* __restrict__ nslot,
                                                       float4* __restrict__ no, float4* __restrict__ nd) {
+    __shared__ SortSmem<BLOCK, BSHADE_PER_THREAD> sm;
     const uint32_t n = *count_in;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
-        uint32_t q = b + (threadIdx.x & 31u);
-        bool alive = false;
-        uint32_t slot = 0;
-        V3 new_o = v3zero(), new_d = v3zero();
-        if (q < n) {
-            slot = q_slot[q];
-            const uint32_t walk = slot & 1u, path = slot >> 1;
-            const bool c2l = walk == 0;
-            float4 h = q_hit[q];
-            float4 o4 = q_o[q], d4 = q_d[q];
-            V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
-            float4 t4 = tp_buf[slot];
-            V3 tp = V3{t4.x, t4.y, t4.z};
-            uint32_t k = vcount[slot];
-            int32_t pk = __float_as_int(h.y);
-            if (pk < 0) {
-                // As if a black infinite light was hit (integrators.rs:210-225).  The
-                // throughput at the escape is kept for the environment extension.
-                Frame z{v3zero(), v3zero(), v3zero(), v3zero()};
-                store_vertex(vs, k, slot, v3zero(), NO_INDEX, -d, false, z, tp, 0, v3zero());
-                vcount[slot] = k + 1;
-                if (walk == 0) {
-                    escape[path] = make_float4(tp.x, tp.y, tp.z, 0.0f);
-                    flags[path] |= F_ESCAPE;
+    // Material-sorted shading (shade_sort.cuh), by (walk, material, chosen lobe).
+    // Block-uniform chunk loop.
+    for (uint32_t c0 = blockIdx.x * BSHADE_CHUNK; c0 < n; c0 += gridDim.x * BSHADE_CHUNK) {
+        const uint32_t cn = min(BSHADE_CHUNK, n - c0);
+        sort_chunk(sm, cn, [&](uint32_t i) {
+            uint32_t q = c0 + i;
+            uint32_t sl = q_slot[q];
+            uint32_t w = sl & 1u;
+            uint32_t dim = (w ? DIM_LIGHT_WALK : DIM_CAMERA_WALK) + 4 * vcount[sl];
+            return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(key_buf[sl >> 1], dim), w);
+        });
+        for (uint32_t e = 0; e < BSHADE_PER_THREAD; ++e) {
+            uint32_t i = e * BLOCK + threadIdx.x;
+            bool alive = false;
+            uint32_t slot = 0;
+            V3 new_o = v3zero(), new_d = v3zero();
+            if (i < cn) {
+                uint32_t q = c0 + sm.order[i];
+                slot = q_slot[q];
+                const uint32_t walk = slot & 1u, path = slot >> 1;
+                const bool c2l = walk == 0;
+                float4 h = q_hit[q];
+                float4 o4 = q_o[q], d4 = q_d[q];
+                V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
+                float4 t4 = tp_buf[slot];
+                V3 tp = V3{t4.x, t4.y, t4.z};
+                uint32_t k = vcount[slot];
+                int32_t pk = __float_as_int(h.y);
+                if (pk < 0) {
+                    // As if a black infinite light was hit (integrators.rs:210-225).  The
+                    // throughput at the escape is kept for the environment extension.
+                    Frame z{v3zero(), v3zero(), v3zero(), v3zero()};
+                    store_vertex(vs, k, slot, v3zero(), NO_INDEX, -d, false, z, tp, 0, v3zero());
+                    vcount[slot] = k + 1;
+                    if (walk == 0) {
+                        escape[path] = make_float4(tp.x, tp.y, tp.z, 0.0f);
+                        flags[path] |= F_ESCAPE;
+                    }
+                } else {
+                    uint32_t prim;
+                    Frame f = hit_frame(s, pk, o, d, h.x, h.z, h.w, prim);
+                    uint32_t mi = __ldg(s.prim_material + prim);
+                    const DevMaterial& m = s.materials[mi];
+                    uint64_t key = key_buf[path];
+                    uint32_t base = (walk ? DIM_LIGHT_WALK : DIM_CAMERA_WALK) + 4 * k;
+                    V3 incoming = -d;
+                    V3 hit_point = o + (d * h.x);
+                    MaterialSample ms = sample_world(m, incoming, f, c2l, uniform01(key, base), uniform01(key, base + 1),
+                                                     uniform01(key, base + 2));
+                    bool connectible = count_lobes(m, LOBE_DIFFUSE | LOBE_GLOSSY) != 0;
+                    V3 ntp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
+                    ntp = ntp * correct_shading_normal(incoming, ms.outgoing, f, c2l);
+                    store_vertex(vs, k, slot, hit_point, prim, incoming, connectible, f, tp, mi, ms.emission);
+                    vcount[slot] = k + 1;
+                    if (k + 1 >= p.rr_len || nearly_zero(ntp)) {
+                        float rv = uniform01(key, base + 3);
+                        float prob = clamped_lerp(0.25f, 0.75f, luminance(ntp));
+                        ntp = rv < prob ? ntp / prob : v3zero();
+                    }
+                    alive = !is_zero(ntp) && k + 1 < p.max_len;
+                    new_o = nudge(hit_point, ms.outgoing);
+                    new_d = ms.outgoing;
+                    if (alive) tp_buf[slot] = make_float4(ntp.x, ntp.y, ntp.z, 0.0f);
                 }
-            } else {
-                uint32_t prim;
-                Frame f = hit_frame(s, pk, o, d, h.x, h.z, h.w, prim);
-                uint32_t mi = __ldg(s.prim_material + prim);
-                const DevMaterial& m = s.materials[mi];
-                uint64_t key = key_buf[path];
-                uint32_t base = (walk ? DIM_LIGHT_WALK : DIM_CAMERA_WALK) + 4 * k;
-                V3 incoming = -d;
-                V3 hit_point = o + (d * h.x);
-                MaterialSample ms = sample_world(m, incoming, f, c2l, uniform01(key, base), uniform01(key, base + 1),
-                                                 uniform01(key, base + 2));
-                bool connectible = count_lobes(m, LOBE_DIFFUSE | LOBE_GLOSSY) != 0;
-                V3 ntp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
-                ntp = ntp * correct_shading_normal(incoming, ms.outgoing, f, c2l);
-                store_vertex(vs, k, slot, hit_point, prim, incoming, connectible, f, tp, mi, ms.emission);
-                vcount[slot] = k + 1;
-                if (k + 1 >= p.rr_len || nearly_zero(ntp)) {
-                    float rv = uniform01(key, base + 3);
-                    float prob = clamped_lerp(0.25f, 0.75f, luminance(ntp));
-                    ntp = rv < prob ? ntp / prob : v3zero();
-                }
-                alive = !is_zero(ntp) && k + 1 < p.max_len;
-                new_o = nudge(hit_point, ms.outgoing);
-                new_d = ms.outgoing;
-                if (alive) tp_buf[slot] = make_float4(ntp.x, ntp.y, ntp.z, 0.0f);
             }
+            push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
         }
-        push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
+        __syncthreads();  // sm is reused by the next chunk
     }
 }
 
@@ -456,7 +474,7 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             if (s1 != GR_OK) return s1;
             GR_CUDA_TRY(cudaGetLastError());
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            int grid = resident_grid(k_bdpt_shade, 0, p.nslots);
+            int grid = resident_grid(k_bdpt_shade, 0, (p.nslots + BSHADE_PER_THREAD - 1) / BSHADE_PER_THREAD);
             k_bdpt_shade<<<grid, BLOCK, 0, st>>>(job.scene, p, vs, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                                  ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
                                                  ps.q_hit.as<float4>(), bs.vcount.as<uint32_t>(), ps.tp.as<float4>(),

@@ -4,6 +4,7 @@
 
 #include "engine.hpp"
 #include "film_gather.cuh"
+#include "shade_sort.cuh"
 #include "traverse.cuh"
 
 namespace gr {
@@ -11,12 +12,25 @@ namespace gr {
 namespace {
 
 constexpr int EBLOCK = 128;
+constexpr uint32_t ESHADE_PER_THREAD = 4;
+constexpr uint32_t ESHADE_CHUNK = EBLOCK * ESHADE_PER_THREAD;
 #ifndef GR_SHADE_MIN_BLOCKS
 #define GR_SHADE_MIN_BLOCKS 6
 #endif
 constexpr int GATHER_BLOCKS = 512;
 
-GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t job,
+// Path state.  The queue entry of a live path carries its ray, its job (o.w) and its
+// depth (d.w).  Global path p (the paths of all units, in unit order) keeps its state in
+// ring slot p & (ring - 1):
+//   s_hot[2 * slot]     = (throughput.xyz, radiance.x)
+//   s_hot[2 * slot + 1] = (radiance.y, radiance.z, key low 32 bits, key high 32 bits)
+//   s_cold[slot]        = (unit, 0, film s bits, film t bits)
+// The hot record is read and written at every bounce and holds the finished sample's
+// radiance; the cold record is written when the path starts.  The gather reads a
+// finished unit's samples straight from its slots, so a slot is reused only once the
+// unit of its previous path is gathered: paths are issued up to `ring` past the oldest
+// ungathered one.  At most `capacity` paths are live (the queues' size).
+GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t job, uint32_t depth,
                    uint32_t* __restrict__ nslot, float4* __restrict__ no, float4* __restrict__ nd) {
     const unsigned lane = threadIdx.x & 31;
     unsigned m = __ballot_sync(0xffffffffu, alive);
@@ -29,13 +43,23 @@ GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, u
         uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
         nslot[pos] = slot;
         no[pos] = make_float4(o.x, o.y, o.z, __uint_as_float(job));
-        nd[pos] = make_float4(d.x, d.y, d.z, 0.0f);
+        nd[pos] = make_float4(d.x, d.y, d.z, __uint_as_float(depth));
     }
+}
+
+// The unit holding global path p: the last unit whose prefix is <= p.
+GR_D uint32_t find_unit(const DevUnit* __restrict__ units, uint32_t lo, uint32_t hi, unsigned long long p) {
+    while (hi - lo > 1) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        if (units[mid].prefix <= p) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
 // Single thread: what to gather and how many paths to issue this iteration.
 __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const DevUnit* __restrict__ units,
-                           const uint32_t* __restrict__ unit_done, uint32_t arena) {
+                           const uint32_t* __restrict__ unit_done, uint32_t cap, uint32_t ring) {
     // Finished units, consecutive from the oldest, grouped by job (pass order kept).
     uint32_t u = c->g_lo, n = 0, groups = 0;
     uint32_t gjob[GATHER_MAX];
@@ -73,31 +97,41 @@ __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const 
     c->gather_tiles = tiles;
     c->g_lo = u;
     c->gather_lo_prefix = u < c->units_count ? units[u].prefix : c->paths_total;
-    unsigned long long freec = c->free_tail - c->free_head;
+    unsigned long long live = c->gcur - c->samples_done;
+    unsigned long long room = cap > live ? cap - live : 0;
     unsigned long long rem = c->paths_total - c->gcur;
-    unsigned long long lim = c->gather_lo_prefix + arena - c->gcur;  // arena slots not holding ungathered samples
-    unsigned long long nf = min(freec, min(rem, lim));
+    unsigned long long lim = c->gather_lo_prefix + ring - c->gcur;  // ring slots free of ungathered samples
+    unsigned long long nf = min(room, min(rem, lim));
     c->fill_n = static_cast<uint32_t>(nf);
     c->fill_base = c->gcur;
-    c->fill_head = c->free_head;
+    if (nf) {  // every unit before g_lo is issued, so the fill starts at or after it
+        c->fill_ulo = find_unit(units, c->g_lo, c->units_count, c->gcur);
+        c->fill_uhi = find_unit(units, c->fill_ulo, c->units_count, c->gcur + nf - 1);
+    }
     c->gcur += nf;
-    c->free_head += static_cast<uint32_t>(nf);
     c->done = c->g_lo == c->units_count ? 1u : 0u;
     c->iter += 1;
 }
 
-struct ArenaIdx {
+// A unit's samples in their ring slots.
+struct RingSamples {
+    const float4* __restrict__ hot;
+    const uint4* __restrict__ cold;
     unsigned long long prefix;
     uint32_t width, mask;
-    GR_D size_t operator()(uint32_t r, uint32_t col) const {
-        return static_cast<size_t>((prefix + static_cast<unsigned long long>(r) * width + col) & mask);
+    GR_D void operator()(uint32_t r, uint32_t col, float2& st, V3& rgb) const {
+        size_t slot = static_cast<size_t>((prefix + static_cast<unsigned long long>(r) * width + col) & mask);
+        float4 a = hot[2 * slot], b = hot[2 * slot + 1];
+        uint4 cd = cold[slot];
+        st = make_float2(__uint_as_float(cd.z), __uint_as_float(cd.w));
+        rgb = V3{a.w, b.x, b.y};
     }
 };
 
 __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const EngineCtl* c, const DevJob* __restrict__ jobs,
                                                                     const DevUnit* __restrict__ units,
-                                                                    const float2* __restrict__ a_st,
-                                                                    const float4* __restrict__ a_c, uint32_t mask) {
+                                                                    const float4* __restrict__ s_hot,
+                                                                    const uint4* __restrict__ s_cold, uint32_t mask) {
     __shared__ StagedSample sm[FILM_SPAN * FILM_SPAN];
     const uint32_t total = c->gather_tiles, groups = c->gather_groups;
     for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
@@ -115,33 +149,22 @@ __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const Engin
         if (inside) acc = J.film[static_cast<size_t>(y) * w + x];
         for (uint32_t k = 0; k < cnt; ++k) {  // the job's passes, in order
             const DevUnit U = units[c->gather_units[first + k]];
-            gather_tile(sm, a_st, a_c, w, h, ox, oy, acc, ArenaIdx{U.prefix, w, mask});
+            gather_tile(sm, w, h, ox, oy, acc, RingSamples{s_hot, s_cold, U.prefix, w, mask});
         }
         if (inside && J.live) J.film[static_cast<size_t>(y) * w + x] = acc;
     }
 }
 
-// The unit holding global path p: the last unit whose prefix is <= p.
-GR_D uint32_t find_unit(const DevUnit* __restrict__ units, uint32_t lo, uint32_t hi, unsigned long long p) {
-    while (hi - lo > 1) {
-        uint32_t mid = lo + (hi - lo) / 2;
-        if (units[mid].prefix <= p) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
+// Starts the next fill_n paths in their ring slots (coalesced: consecutive paths,
+// consecutive slots) and queues their camera rays.
 __global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob* __restrict__ jobs,
-                                                     const DevUnit* __restrict__ units,
-                                                     const uint32_t* __restrict__ free_ring, uint32_t cap, int cur,
-                                                     uint32_t* __restrict__ s_unit, uint32_t* __restrict__ s_pixel,
-                                                     uint32_t* __restrict__ s_depth, float4* __restrict__ s_tp,
-                                                     float4* __restrict__ s_L, unsigned long long* __restrict__ s_key,
-                                                     float2* __restrict__ s_st, uint32_t* __restrict__ q_slot,
-                                                     float4* __restrict__ q_o, float4* __restrict__ q_d) {
+                                                     const DevUnit* __restrict__ units, uint32_t mask, int cur,
+                                                     float4* __restrict__ s_hot, uint4* __restrict__ s_cold,
+                                                     uint32_t* __restrict__ q_slot, float4* __restrict__ q_o,
+                                                     float4* __restrict__ q_d) {
     const uint32_t n = c->fill_n;
     const unsigned long long base = c->fill_base;
-    const uint32_t head = c->fill_head, lo = c->g_lo, hi = c->units_count;
+    const uint32_t ulo = c->fill_ulo, uhi = c->fill_uhi + 1;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
         uint32_t i = b + (threadIdx.x & 31u);
@@ -149,9 +172,9 @@ __global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob*
         uint32_t slot = 0, job = 0;
         V3 o = v3zero(), d = v3zero();
         if (i < n) {
-            slot = free_ring[(head + i) % cap];
             unsigned long long p = base + i;
-            uint32_t u = find_unit(units, lo, hi, p);
+            slot = static_cast<uint32_t>(p & mask);
+            uint32_t u = find_unit(units, ulo, uhi, p);
             DevUnit U = units[u];
             uint32_t pixel = static_cast<uint32_t>(p - U.prefix);
             job = U.job;
@@ -161,16 +184,14 @@ __global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob*
             float s, t;
             film_sample_point(J.width, J.height, row, col, key, s, t);
             camera_ray(J.cam, s, t, o, d);
-            s_unit[slot] = u;
-            s_pixel[slot] = pixel;
-            s_depth[slot] = 0;
-            s_tp[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-            s_L[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            s_key[slot] = key;
-            s_st[slot] = make_float2(s, t);
+            s_hot[2 * static_cast<size_t>(slot)] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            s_hot[2 * static_cast<size_t>(slot) + 1] =
+                make_float4(0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(key)),
+                            __uint_as_float(static_cast<uint32_t>(key >> 32)));
+            s_cold[slot] = make_uint4(u, 0, __float_as_uint(s), __float_as_uint(t));
             alive = true;
         }
-        push_ray(alive, &c->q[cur], slot, o, d, job, q_slot, q_o, q_d);
+        push_ray(alive, &c->q[cur], slot, o, d, job, 0, q_slot, q_o, q_d);
     }
 }
 
@@ -203,107 +224,103 @@ __global__ void __launch_bounds__(BS) k_eng_extend(EngineCtl* c, int cur, const 
     }
 }
 
-__global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS) k_eng_shade(EngineCtl* c, int cur, const DevJob* __restrict__ jobs,
-                                                      const DevUnit* __restrict__ units, uint32_t* unit_done,
-                                                      uint32_t* free_ring, uint32_t cap, uint32_t arena,
-                                                      const uint32_t* __restrict__ q_slot,
-                                                      const float4* __restrict__ q_o, const float4* __restrict__ q_d,
-                                                      const float4* __restrict__ q_hit, uint32_t* __restrict__ s_unit,
-                                                      const uint32_t* __restrict__ s_pixel,
-                                                      uint32_t* __restrict__ s_depth, float4* __restrict__ s_tp,
-                                                      float4* __restrict__ s_L,
-                                                      const unsigned long long* __restrict__ s_key,
-                                                      const float2* __restrict__ s_st, float2* __restrict__ a_st,
-                                                      float4* __restrict__ a_c, uint32_t* __restrict__ nslot,
-                                                      float4* __restrict__ no, float4* __restrict__ nd) {
+__global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
+    k_eng_shade(EngineCtl* c, int cur, const DevJob* __restrict__ jobs, uint32_t* unit_done,
+                const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
+                const float4* __restrict__ q_d, const float4* __restrict__ q_hit, float4* __restrict__ s_hot,
+                const uint4* __restrict__ s_cold, uint32_t* __restrict__ nslot, float4* __restrict__ no,
+                float4* __restrict__ nd) {
+    __shared__ SortSmem<EBLOCK, ESHADE_PER_THREAD> sm;
     const int nxt = cur ^ 1;
     const uint32_t n = c->q[cur];
-    const uint32_t stride = gridDim.x * blockDim.x;
     const unsigned lane = threadIdx.x & 31u;
-    for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
-        uint32_t q = b + lane;
-        bool alive = false, finished = false;
-        uint32_t slot = 0, job = 0, unit = 0xFFFFFFFFu;
-        V3 new_o = v3zero(), new_d = v3zero();
-        if (q < n) {
-            slot = q_slot[q];
-            float4 h = q_hit[q];
-            float4 o4 = q_o[q], d4 = q_d[q];
-            job = __float_as_uint(o4.w);
-            const DevJob& J = jobs[job];
-            const DeviceScene& s = J.scene;
-            V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
-            float4 tp4 = s_tp[slot], L4 = s_L[slot];
-            V3 tp = V3{tp4.x, tp4.y, tp4.z}, L = V3{L4.x, L4.y, L4.z};
-            uint32_t depth = s_depth[slot];
-            int32_t k = __float_as_int(h.y);
-            if (!J.live) {
-                // cancelled: drop the path
-            } else if (k < 0) {
-                // DisplayColorIntegrator returns black on a miss (render/integrators.rs:29-31).
-                if (s.has_env && !J.display) L = L + mul(tp, V3{s.env[0], s.env[1], s.env[2]});
-            } else if (J.display) {
-                uint32_t prim = __float_as_uint(__ldg(s.prims + 3 * static_cast<size_t>(k)).w);
-                const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
-                L = V3{m.display[0], m.display[1], m.display[2]};
-            } else {
-                // PathTracerIntegrator::integrate (render/integrators.rs:42-100), one segment.
-                uint32_t prim;
-                Frame f = hit_frame(s, k, o, d, h.x, h.z, h.w, prim);
-                const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
-                uint64_t key = s_key[slot];
-                uint32_t base = DIM_CAMERA_WALK + 4 * depth;
-                MaterialSample ms = sample_world(m, -d, f, true, uniform01(key, base), uniform01(key, base + 1),
-                                                 uniform01(key, base + 2));
-                L = L + mul(tp, ms.emission);
-                tp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
-                new_o = nudge(o + (d * h.x), ms.outgoing);
-                new_d = ms.outgoing;
-                if (depth > J.rr_depth || nearly_zero(tp)) {
-                    float rv = uniform01(key, base + 3);
-                    float lum = luminance(tp);
-                    float prob = depth > J.rr_aggr ? clamped_lerp(0.10f, 0.75f, lum) : clamped_lerp(0.25f, 1.00f, lum);
-                    tp = rv < prob ? tp / prob : v3zero();
+    // Material-sorted shading (shade_sort.cuh), by (job, material, chosen lobe); misses,
+    // cancelled and display-colour jobs share bucket 0.  Block-uniform chunk loop.
+    for (uint32_t c0 = blockIdx.x * ESHADE_CHUNK; c0 < n; c0 += gridDim.x * ESHADE_CHUNK) {
+        const uint32_t cn = min(ESHADE_CHUNK, n - c0);
+        sort_chunk(sm, cn, [&](uint32_t i) {
+            uint32_t q = c0 + i;
+            uint32_t jb = __float_as_uint(q_o[q].w);
+            const DevJob& J = jobs[jb];
+            int32_t k = __float_as_int(q_hit[q].y);
+            if (!J.live || J.display || k < 0) return 0u;
+            float4 kb = s_hot[2 * static_cast<size_t>(q_slot[q]) + 1];
+            uint64_t key = (static_cast<uint64_t>(__float_as_uint(kb.w)) << 32) | __float_as_uint(kb.z);
+            return shade_bucket(J.scene, k, uniform01(key, DIM_CAMERA_WALK + 4 * __float_as_uint(q_d[q].w)), jb);
+        });
+        for (uint32_t e = 0; e < ESHADE_PER_THREAD; ++e) {
+            uint32_t i = e * EBLOCK + threadIdx.x;
+            bool alive = false, finished = false;
+            uint32_t slot = 0, job = 0, unit = 0xFFFFFFFFu, depth = 0;
+            V3 new_o = v3zero(), new_d = v3zero();
+            if (i < cn) {
+                uint32_t q = c0 + sm.order[i];
+                slot = q_slot[q];
+                float4 h = q_hit[q];
+                float4 o4 = q_o[q], d4 = q_d[q];
+                job = __float_as_uint(o4.w);
+                depth = __float_as_uint(d4.w);
+                const DevJob& J = jobs[job];
+                const DeviceScene& s = J.scene;
+                V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
+                const size_t hs = 2 * static_cast<size_t>(slot);
+                float4 ha = s_hot[hs], hb = s_hot[hs + 1];
+                V3 tp = V3{ha.x, ha.y, ha.z}, L = V3{ha.w, hb.x, hb.y};
+                int32_t k = __float_as_int(h.y);
+                if (!J.live) {
+                    // cancelled: drop the path
+                } else if (k < 0) {
+                    // DisplayColorIntegrator returns black on a miss (render/integrators.rs:29-31).
+                    if (s.has_env && !J.display) L = L + mul(tp, V3{s.env[0], s.env[1], s.env[2]});
+                } else if (J.display) {
+                    uint32_t prim = __float_as_uint(__ldg(s.prims + 3 * static_cast<size_t>(k)).w);
+                    const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
+                    L = V3{m.display[0], m.display[1], m.display[2]};
+                } else {
+                    // PathTracerIntegrator::integrate (render/integrators.rs:42-100), one segment.
+                    uint32_t prim;
+                    Frame f = hit_frame(s, k, o, d, h.x, h.z, h.w, prim);
+                    const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
+                    uint64_t key = (static_cast<uint64_t>(__float_as_uint(hb.w)) << 32) | __float_as_uint(hb.z);
+                    uint32_t base = DIM_CAMERA_WALK + 4 * depth;
+                    MaterialSample ms = sample_world(m, -d, f, true, uniform01(key, base), uniform01(key, base + 1),
+                                                     uniform01(key, base + 2));
+                    L = L + mul(tp, ms.emission);
+                    tp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
+                    new_o = nudge(o + (d * h.x), ms.outgoing);
+                    new_d = ms.outgoing;
+                    if (depth > J.rr_depth || nearly_zero(tp)) {
+                        float rv = uniform01(key, base + 3);
+                        float lum = luminance(tp);
+                        float prob =
+                            depth > J.rr_aggr ? clamped_lerp(0.10f, 0.75f, lum) : clamped_lerp(0.25f, 1.00f, lum);
+                        tp = rv < prob ? tp / prob : v3zero();
+                    }
+                    alive = !is_zero(tp) && (J.max_depth == 0 || depth + 1 < J.max_depth);
                 }
-                alive = !is_zero(tp) && (J.max_depth == 0 || depth + 1 < J.max_depth);
+                // The hot record keeps the radiance of a finished path: the gather reads it.
+                s_hot[hs] = make_float4(tp.x, tp.y, tp.z, L.x);
+                s_hot[hs + 1] = make_float4(L.y, L.z, hb.z, hb.w);
+                if (!alive) {
+                    finished = true;
+                    unit = s_cold[slot].x;
+                }
             }
-            if (alive) {
-                s_tp[slot] = make_float4(tp.x, tp.y, tp.z, 0.0f);
-                s_L[slot] = make_float4(L.x, L.y, L.z, 0.0f);
-                s_depth[slot] = depth + 1;
-            } else {
-                finished = true;
-                unit = s_unit[slot];
-                unsigned long long p = units[unit].prefix + s_pixel[slot];
-                size_t a = static_cast<size_t>(p & (arena - 1));  // arena is a power of two
-                a_st[a] = s_st[slot];
-                a_c[a] = make_float4(L.x, L.y, L.z, 0.0f);
+            // Finished paths count their unit done: one atomic per unit per warp, and one
+            // per warp for the engine total.  The plan and gather kernels that read the
+            // counts and the samples are later launches on the same stream.
+            unsigned fm = __ballot_sync(0xffffffffu, finished);
+            if (fm) {
+                unsigned same = __match_any_sync(0xffffffffu, unit);
+                if (finished && lane == static_cast<unsigned>(__ffs(same) - 1))
+                    atomicAdd(unit_done + unit, static_cast<uint32_t>(__popc(same)));
+                if (lane == static_cast<unsigned>(__ffs(fm) - 1))
+                    atomicAdd(&c->samples_done, static_cast<unsigned long long>(__popc(fm)));
             }
+            push_ray(alive, &c->q[nxt], slot, new_o, new_d, job, depth + 1, nslot, no, nd);
         }
-        // Finished paths: count their unit done (one atomic per unit per warp) and free
-        // their slot (one atomic per warp).
-        unsigned fm = __ballot_sync(0xffffffffu, finished);
-        if (fm) {
-            __threadfence();  // arena writes before the unit count
-            unsigned same = __match_any_sync(0xffffffffu, unit);
-            if (finished && lane == static_cast<unsigned>(__ffs(same) - 1))
-                atomicAdd(unit_done + unit, static_cast<uint32_t>(__popc(same)));
-            int leader = __ffs(fm) - 1;
-            uint32_t fbase = 0;
-            if (lane == static_cast<unsigned>(leader)) {
-                fbase = atomicAdd(&c->free_tail, static_cast<uint32_t>(__popc(fm)));
-                atomicAdd(&c->samples_done, static_cast<unsigned long long>(__popc(fm)));
-            }
-            fbase = __shfl_sync(0xffffffffu, fbase, leader);
-            if (finished) free_ring[(fbase + __popc(fm & ((1u << lane) - 1u))) % cap] = slot;
-        }
-        push_ray(alive, &c->q[nxt], slot, new_o, new_d, job, nslot, no, nd);
+        __syncthreads();  // sm is reused by the next chunk
     }
-}
-
-__global__ void k_eng_init_free(uint32_t* free_ring, uint32_t cap) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < cap) free_ring[i] = i;
 }
 
 int grid_for(const void* kernel, int block, size_t smem, uint32_t n) {
@@ -364,9 +381,9 @@ gr_status Engine::init(const EngineConfig& cfg, cudaStream_t) {
         return GR_ERR_INVALID_ARGUMENT;
     }
     if (cfg_.capacity < 1024) cfg_.capacity = 1024;
-    uint64_t want = cfg_.arena ? cfg_.arena : 2ull * cfg_.capacity + (1u << 22);
-    arena_ = 1u << 20;
-    while (arena_ < want && arena_ < (1u << 30)) arena_ <<= 1;  // power of two: the index is a mask
+    uint64_t want = cfg_.ring ? cfg_.ring : 2ull * cfg_.capacity + (1u << 22);
+    ring_ = 1u << 20;
+    while (ring_ < want && ring_ < (1u << 30)) ring_ <<= 1;  // power of two: the slot is a mask
     GR_CUDA_TRY(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
     const size_t C = cfg_.capacity;
     auto alloc = [&](DevBuf& b, size_t bytes) -> cudaError_t {
@@ -377,29 +394,16 @@ gr_status Engine::init(const EngineConfig& cfg, cudaStream_t) {
     GR_CUDA_TRY(alloc(jobs_, ENGINE_MAX_JOBS * sizeof(DevJob)));
     GR_CUDA_TRY(alloc(units_, ENGINE_MAX_UNITS * sizeof(DevUnit)));
     GR_CUDA_TRY(alloc(unit_done_, ENGINE_MAX_UNITS * sizeof(uint32_t)));
-    GR_CUDA_TRY(alloc(s_unit_, C * 4));
-    GR_CUDA_TRY(alloc(s_pixel_, C * 4));
-    GR_CUDA_TRY(alloc(s_depth_, C * 4));
-    GR_CUDA_TRY(alloc(s_tp_, C * 16));
-    GR_CUDA_TRY(alloc(s_L_, C * 16));
-    GR_CUDA_TRY(alloc(s_key_, C * 8));
-    GR_CUDA_TRY(alloc(s_st_, C * 8));
-    GR_CUDA_TRY(alloc(free_ring_, C * 4));
+    GR_CUDA_TRY(alloc(s_hot_, static_cast<size_t>(ring_) * 32));
+    GR_CUDA_TRY(alloc(s_cold_, static_cast<size_t>(ring_) * 16));
     for (int k = 0; k < 2; ++k) {
         GR_CUDA_TRY(alloc(q_slot_[k], C * 4));
         GR_CUDA_TRY(alloc(q_o_[k], C * 16));
         GR_CUDA_TRY(alloc(q_d_[k], C * 16));
     }
     GR_CUDA_TRY(alloc(q_hit_, C * 16));
-    GR_CUDA_TRY(alloc(a_st_, static_cast<size_t>(arena_) * 8));
-    GR_CUDA_TRY(alloc(a_c_, static_cast<size_t>(arena_) * 16));
     GR_CUDA_TRY(cudaMemsetAsync(ctl_.ptr, 0, sizeof(EngineCtl), st_));
     GR_CUDA_TRY(cudaMemsetAsync(unit_done_.ptr, 0, ENGINE_MAX_UNITS * sizeof(uint32_t), st_));
-    k_eng_init_free<<<(cfg_.capacity + 255) / 256, 256, 0, st_>>>(free_ring_.as<uint32_t>(), cfg_.capacity);
-    GR_CUDA_TRY(cudaGetLastError());
-    uint32_t tail = cfg_.capacity;
-    GR_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(EngineCtl, free_tail), &tail, 4,
-                                cudaMemcpyHostToDevice, st_));
     GR_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&h_pinned_), 8 * sizeof(uint64_t), cudaHostAllocDefault));
     GR_CUDA_TRY(cudaStreamSynchronize(st_));
     return record_pair();
@@ -409,17 +413,15 @@ gr_status Engine::enqueue_iteration(int cur) {
     EngineCtl* c = ctl_.as<EngineCtl>();
     const uint32_t C = cfg_.capacity;
     const int nxt = cur ^ 1;
-    k_eng_plan<<<1, 1, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), arena_);
+    k_eng_plan<<<1, 1, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), C, ring_);
     GR_CUDA_TRY(cudaGetLastError());
     k_eng_gather<<<GATHER_BLOCKS, FILM_TILE * FILM_TILE, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(),
-                                                                   a_st_.as<float2>(), a_c_.as<float4>(), arena_ - 1);
+                                                                   s_hot_.as<float4>(), s_cold_.as<uint4>(), ring_ - 1);
     GR_CUDA_TRY(cudaGetLastError());
     int fgrid = grid_for(reinterpret_cast<const void*>(k_eng_fill), EBLOCK, 0, C);
-    k_eng_fill<<<fgrid, EBLOCK, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), free_ring_.as<uint32_t>(), C,
-                                          cur, s_unit_.as<uint32_t>(), s_pixel_.as<uint32_t>(),
-                                          s_depth_.as<uint32_t>(), s_tp_.as<float4>(), s_L_.as<float4>(),
-                                          s_key_.as<unsigned long long>(), s_st_.as<float2>(),
-                                          q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>());
+    k_eng_fill<<<fgrid, EBLOCK, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), ring_ - 1, cur,
+                                          s_hot_.as<float4>(), s_cold_.as<uint4>(), q_slot_[cur].as<uint32_t>(),
+                                          q_o_[cur].as<float4>(), q_d_[cur].as<float4>());
     GR_CUDA_TRY(cudaGetLastError());
     switch (cfg_.width) {
         case 2:
@@ -435,13 +437,12 @@ gr_status Engine::enqueue_iteration(int cur) {
                                        q_d_[cur].as<float4>(), q_hit_.as<float4>(), C, st_));
     }
     GR_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(c) + offsetof(EngineCtl, q) + nxt * sizeof(uint32_t), 0, 4, st_));
-    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), EBLOCK, 0, C);
-    k_eng_shade<<<sgrid, EBLOCK, 0, st_>>>(
-        c, cur, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), free_ring_.as<uint32_t>(), C,
-        arena_, q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>(), q_hit_.as<float4>(),
-        s_unit_.as<uint32_t>(), s_pixel_.as<uint32_t>(), s_depth_.as<uint32_t>(), s_tp_.as<float4>(),
-        s_L_.as<float4>(), s_key_.as<unsigned long long>(), s_st_.as<float2>(), a_st_.as<float2>(),
-        a_c_.as<float4>(), q_slot_[nxt].as<uint32_t>(), q_o_[nxt].as<float4>(), q_d_[nxt].as<float4>());
+    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), EBLOCK, 0, (C + ESHADE_PER_THREAD - 1) / ESHADE_PER_THREAD);
+    k_eng_shade<<<sgrid, EBLOCK, 0, st_>>>(c, cur, jobs_.as<DevJob>(), unit_done_.as<uint32_t>(),
+                                           q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>(),
+                                           q_hit_.as<float4>(), s_hot_.as<float4>(), s_cold_.as<uint4>(),
+                                           q_slot_[nxt].as<uint32_t>(), q_o_[nxt].as<float4>(),
+                                           q_d_[nxt].as<float4>());
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }
@@ -473,8 +474,8 @@ gr_status Engine::add_job(const DevJob& job, uint32_t first_pass, uint32_t passe
         set_error("engine: every scene in one engine must have the engine's BVH width");
         return GR_ERR_INVALID_ARGUMENT;
     }
-    if (static_cast<uint64_t>(job.npix) * 2 > arena_) {
-        set_error("engine: image too large for the sample arena");
+    if (static_cast<uint64_t>(job.npix) * 2 > ring_) {
+        set_error("engine: image too large for the path ring");
         return GR_ERR_INVALID_ARGUMENT;
     }
     index = static_cast<uint32_t>(h_jobs_.size());
@@ -526,11 +527,6 @@ gr_status Engine::reset() {
     size_t used = h_units_.size();
     GR_CUDA_TRY(cudaMemsetAsync(ctl_.ptr, 0, sizeof(EngineCtl), st_));
     if (used) GR_CUDA_TRY(cudaMemsetAsync(unit_done_.ptr, 0, used * sizeof(uint32_t), st_));
-    k_eng_init_free<<<(cfg_.capacity + 255) / 256, 256, 0, st_>>>(free_ring_.as<uint32_t>(), cfg_.capacity);
-    GR_CUDA_TRY(cudaGetLastError());
-    h_pinned_[6] = cfg_.capacity;
-    GR_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(EngineCtl, free_tail), &h_pinned_[6], 4,
-                                cudaMemcpyHostToDevice, st_));
     GR_CUDA_TRY(cudaStreamSynchronize(st_));
     h_jobs_.clear();
     h_units_.clear();

@@ -1,16 +1,17 @@
 // Multi-job wavefront engine: the machinery behind gr_render_batch and gr_server_*.
 //
-// Many renders ("jobs": a scene, a camera, settings and a film) share one pool of path
-// slots.  Each job's work is a list of units, one per pass; units are issued in a global
-// order (round-robin over jobs, pass by pass).  Every iteration:
+// Many renders ("jobs": a scene, a camera, settings and a film) share one wavefront.
+// Each job's work is a list of units, one per pass; units are issued in a global order
+// (round-robin over jobs, pass by pass), and global path p keeps its state in slot
+// p mod ring of a ring of path records.  Every iteration:
 //   plan    (1 thread) picks the finished units to gather (consecutive from the oldest)
-//           and how many new paths to issue into free slots
-//   gather  splats the picked units into their films (the deterministic tile gather);
-//           each film tile adds its job's units in pass order
-//   fill    turns free slots into new camera paths (jitter, camera ray)
+//           and how many new paths to issue (queue room, ring slots already gathered)
+//   gather  splats the picked units into their films from their ring slots (the
+//           deterministic tile gather); each film tile adds its job's units in pass order
+//   fill    starts the next paths in their slots (jitter, camera ray) and queues them
 //   extend  closest hit for the queued rays of all jobs
-//   shade   path-tracer shading per job; finished paths write their sample into a ring
-//           arena, count their unit done and free their slot
+//   shade   path-tracer shading per job, material-sorted; finished paths leave their
+//           radiance in their slot and count their unit done
 // All launches have fixed grids and read their sizes from device memory, so an
 // iteration pair is captured once in a CUDA graph and replayed until every unit is
 // gathered.  A job's passes are gathered in pass order, so each film is identical to the
@@ -54,9 +55,9 @@ struct EngineCtl {
     unsigned long long samples_done;
     uint32_t units_count;
     uint32_t g_lo;  // oldest unit not yet gathered
-    uint32_t free_head, free_tail;
     uint32_t q[2];
-    uint32_t fill_n, fill_head;
+    uint32_t fill_n;
+    uint32_t fill_ulo, fill_uhi;  // units holding the paths of this fill: [fill_ulo, fill_uhi]
     uint32_t gather_n;       // units to gather this iteration, grouped by job
     uint32_t gather_groups;  // distinct jobs among them
     uint32_t done;
@@ -73,7 +74,7 @@ struct EngineConfig {
     uint32_t capacity = 1u << 21;  // path slots
     uint32_t width = 4;            // BVH width of every scene in the engine
     uint32_t block = 128;          // extension kernel block size (64, 128, 256)
-    uint32_t arena = 0;            // samples; 0 = derived
+    uint32_t ring = 0;             // path state slots (power of two); 0 = derived
 };
 
 class Engine {
@@ -107,11 +108,10 @@ class Engine {
     gr_status enqueue_iteration(int cur);
     EngineConfig cfg_;
     cudaStream_t st_ = nullptr;
-    uint32_t arena_ = 0;
+    uint32_t ring_ = 0;
     DevBuf ctl_, jobs_, units_, unit_done_;
-    DevBuf s_unit_, s_pixel_, s_depth_, s_tp_, s_L_, s_key_, s_st_, free_ring_;
+    DevBuf s_hot_, s_cold_;  // path state ring (see engine.cu)
     DevBuf q_slot_[2], q_o_[2], q_d_[2], q_hit_;
-    DevBuf a_st_, a_c_;
     std::vector<DevJob> h_jobs_;
     std::vector<DevUnit> h_units_;
     uint32_t jobs_cap_ = 0, units_cap_ = 0;

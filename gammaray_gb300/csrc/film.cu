@@ -7,12 +7,6 @@ namespace gr {
 
 namespace {
 
-struct LinearIdx {
-    size_t base;
-    uint32_t width;
-    GR_D size_t operator()(uint32_t r, uint32_t c) const { return base + static_cast<size_t>(r) * width + c; }
-};
-
 __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_film_gather(const float2* __restrict__ st,
                                                                      const float4* __restrict__ color, uint32_t width,
                                                                      uint32_t height, uint32_t passes, float4* film) {
@@ -24,7 +18,7 @@ __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_film_gather(const floa
     if (inside) acc = film[static_cast<size_t>(y) * width + x];
     const size_t npix = static_cast<size_t>(width) * height;
     for (uint32_t pass = 0; pass < passes; ++pass)
-        gather_tile(sm, st, color, width, height, ox, oy, acc, LinearIdx{pass * npix, width});
+        gather_tile(sm, width, height, ox, oy, acc, LinearSamples{st, color, pass * npix, width});
     if (inside) film[static_cast<size_t>(y) * width + x] = acc;
 }
 

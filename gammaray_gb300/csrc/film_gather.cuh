@@ -39,12 +39,11 @@ struct StagedSample {
     float r, g, b;
 };
 
-// Adds the samples of one pass to the tile (ox, oy) of `film`.  `idx(row, col)` is the
-// index of that pixel's sample in `st` / `color`.  Every thread of the block (256 =
-// FILM_TILE^2) must call it; `sm` holds FILM_SPAN^2 entries.
-template <class Idx>
-GR_D void gather_tile(StagedSample* sm, const float2* __restrict__ st, const float4* __restrict__ color,
-                      uint32_t width, uint32_t height, int ox, int oy, float4& acc, const Idx& idx) {
+// Adds the samples of one pass to the tile (ox, oy) of `film`.  `src(row, col, st, rgb)`
+// loads that pixel's sample: its film position (s, t) and its radiance.  Every thread of
+// the block (256 = FILM_TILE^2) must call it; `sm` holds FILM_SPAN^2 entries.
+template <class Src>
+GR_D void gather_tile(StagedSample* sm, uint32_t width, uint32_t height, int ox, int oy, float4& acc, const Src& src) {
     const int tx = threadIdx.x % FILM_TILE, ty = threadIdx.x / FILM_TILE;
     const int x = ox + tx, y = oy + ty;
     const bool inside = x < static_cast<int>(width) && y < static_cast<int>(height);
@@ -61,9 +60,9 @@ GR_D void gather_tile(StagedSample* sm, const float2* __restrict__ st, const flo
         e.cd = e.rd = 0.0f;
         e.r = e.g = e.b = 0.0f;
         if (sr >= 0 && sc >= 0 && sr < static_cast<int>(height) && sc < static_cast<int>(width)) {
-            size_t i = idx(static_cast<uint32_t>(sr), static_cast<uint32_t>(sc));
-            float2 s = st[i];
-            float4 c = color[i];
+            float2 s;
+            V3 c;
+            src(static_cast<uint32_t>(sr), static_cast<uint32_t>(sc), s, c);
             // film.rs:82-97
             float col_cont = lerp(0.0f, wf, 0.5f * (s.x + 1.0f));
             float row_cont = lerp(0.0f, hf, 0.5f * (s.y + 1.0f));
@@ -107,5 +106,20 @@ GR_D void gather_tile(StagedSample* sm, const float2* __restrict__ st, const flo
         }
     }
 }
+
+// Samples of one pass stored linearly: sample (row, col) at base + row * width + col of
+// `st` (film position) and `color` (radiance in xyz).
+struct LinearSamples {
+    const float2* __restrict__ st;
+    const float4* __restrict__ color;
+    size_t base;
+    uint32_t width;
+    GR_D void operator()(uint32_t r, uint32_t c, float2& s, V3& rgb) const {
+        size_t i = base + static_cast<size_t>(r) * width + c;
+        s = st[i];
+        float4 v = color[i];
+        rgb = V3{v.x, v.y, v.z};
+    }
+};
 
 }  // namespace gr

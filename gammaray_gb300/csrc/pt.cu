@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "runtime.hpp"
+#include "shade_sort.cuh"
 #include "wavefront.cuh"
 
 #define GR_TRY_S(expr)                \
@@ -66,26 +67,10 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
 }
 
 
-// Material-sorted shading.  Each block takes the queue in chunks of SHADE_CHUNK entries,
-// gives every entry a bucket (0: the ray escaped; else a hash of the hit's material and
-// the lobe its sample will pick), counting-sorts the chunk by bucket in shared memory
-// and shades it in that order.  Warps then run one material's one lobe sampler instead
-// of a mix of all of them.  The order only decides which thread shades which path:
-// every path's arithmetic and its queue slot are unchanged.
+// Material-sorted shading (shade_sort.cuh): each block sorts its SHADE_CHUNK-entry chunk
+// of the queue by (material, chosen lobe), then shades it in that order.
 constexpr uint32_t SHADE_PER_THREAD = 4;
 constexpr uint32_t SHADE_CHUNK = BLOCK * SHADE_PER_THREAD;
-constexpr uint32_t SHADE_BUCKETS = 32;
-static_assert(SHADE_CHUNK <= 65536, "chunk positions are 16-bit");
-
-GR_D uint32_t shade_bucket(const DeviceScene& s, float4 h, uint64_t key, uint32_t dim) {
-    int32_t k = __float_as_int(h.y);
-    if (k < 0) return 0;
-    uint32_t prim = __float_as_uint(__ldg(s.prims + 3 * static_cast<size_t>(k)).w);
-    uint32_t mat = __ldg(s.prim_material + prim);
-    uint32_t nl = static_cast<uint32_t>(s.materials[mat].n_lobes);
-    uint32_t r = nl ? range_index(uniform01(key, dim), nl) : 0;
-    return 1 + (mat * MAX_LOBES + r) % (SHADE_BUCKETS - 1);
-}
 
 __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t depth,
                                                  const uint32_t* __restrict__ count_in,
@@ -95,53 +80,24 @@ __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t dept
                                                  const unsigned long long* __restrict__ key_buf, uint32_t* count_out,
                                                  uint32_t* __restrict__ nslot, float4* __restrict__ no,
                                                  float4* __restrict__ nd) {
-    __shared__ uint32_t s_start[SHADE_BUCKETS];
-    __shared__ uint16_t s_order[SHADE_CHUNK];
+    __shared__ SortSmem<BLOCK, SHADE_PER_THREAD> sm;
     const uint32_t n = *count_in;
-    const uint32_t tid = threadIdx.x;
     const uint32_t base = DIM_CAMERA_WALK + 4 * depth;
-    // Block-uniform chunk loop (the barriers below need every thread).
+    // Block-uniform chunk loop (sort_chunk's barriers need every thread).
     for (uint32_t c0 = blockIdx.x * SHADE_CHUNK; c0 < n; c0 += gridDim.x * SHADE_CHUNK) {
         const uint32_t cn = min(SHADE_CHUNK, n - c0);
-        if (tid < SHADE_BUCKETS) s_start[tid] = 0;
-        __syncthreads();
-        uint32_t bucket[SHADE_PER_THREAD], rank[SHADE_PER_THREAD];
-#pragma unroll
-        for (uint32_t e = 0; e < SHADE_PER_THREAD; ++e) {
-            uint32_t i = e * BLOCK + tid;
-            bucket[e] = 0;
-            rank[e] = 0;
-            if (i < cn) {
-                uint32_t q = c0 + i;
-                bucket[e] = shade_bucket(s, q_hit[q], key_buf[q_slot[q]], base);
-                rank[e] = atomicAdd(&s_start[bucket[e]], 1u);
-            }
-        }
-        __syncthreads();
-        if (tid < 32) {  // exclusive scan of the bucket counts (SHADE_BUCKETS == 32)
-            uint32_t c = s_start[tid], x = c;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                if (static_cast<int>(tid) >= o) x += y;
-            }
-            s_start[tid] = x - c;
-        }
-        __syncthreads();
-#pragma unroll
-        for (uint32_t e = 0; e < SHADE_PER_THREAD; ++e) {
-            uint32_t i = e * BLOCK + tid;
-            if (i < cn) s_order[s_start[bucket[e]] + rank[e]] = static_cast<uint16_t>(i);
-        }
-        __syncthreads();
+        sort_chunk(sm, cn, [&](uint32_t i) {
+            uint32_t q = c0 + i;
+            return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(key_buf[q_slot[q]], base), 0);
+        });
         // Every lane runs every step so that all of them reach the ballot in push_warp.
         for (uint32_t e = 0; e < SHADE_PER_THREAD; ++e) {
-            uint32_t i = e * BLOCK + tid;
+            uint32_t i = e * BLOCK + threadIdx.x;
             bool alive = false;
             uint32_t slot = 0;
             V3 new_o = v3zero(), new_d = v3zero();
             if (i < cn) {
-                uint32_t q = c0 + s_order[i];
+                uint32_t q = c0 + sm.order[i];
                 slot = q_slot[q];
                 float4 h = q_hit[q];
                 float4 o4 = q_o[q], d4 = q_d[q];
@@ -176,7 +132,7 @@ __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t dept
             }
             push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
         }
-        __syncthreads();  // s_start and s_order are reused by the next chunk
+        __syncthreads();  // sm is reused by the next chunk
     }
 }
 
