@@ -265,7 +265,8 @@ class Mesh:
             if xf is not None:
                 nn = xf.transform_normals(n)
                 mag2 = (n * n).sum(axis=1)
-                unit = nn / np.sqrt((nn * nn).sum(axis=1, keepdims=True))
+                with np.errstate(divide="ignore", invalid="ignore"):  # nearly-zero rows are kept raw
+                    unit = nn / np.sqrt((nn * nn).sum(axis=1, keepdims=True))
                 n = np.where((mag2 < np.finfo(np.float32).eps)[:, None], n, unit).astype(np.float32)
             self.normals = np.ascontiguousarray(n)
             self.tri_normals = np.ascontiguousarray(tri_normals, dtype=np.uint32).reshape(-1, 3)
