@@ -169,8 +169,7 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams
     push_warp(light_alive, count_out, 2 * i + 1, lo, ld, nslot, no, nd);
 }
 
-constexpr uint32_t BSHADE_PER_THREAD = 4;
-constexpr uint32_t BSHADE_CHUNK = BLOCK * BSHADE_PER_THREAD;
+constexpr uint32_t BSHADE_PER_THREAD = SHADE_PER_THREAD;
 
 __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts vs,
                                                       const uint32_t* __restrict__ count_in,
@@ -182,20 +181,23 @@ __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts 
                                                       uint32_t* __restrict__ flags, float4* __restrict__ escape,
                                                       uint32_t* count_out, uint32_t* __restrict__ nslot,
                                                       float4* __restrict__ no, float4* __restrict__ nd) {
-    __shared__ SortSmem<BLOCK, BSHADE_PER_THREAD> sm;
+    extern __shared__ unsigned char dsmem[];
+    const SortView sm = sort_view<BLOCK, BSHADE_PER_THREAD>(dsmem);
     const uint32_t n = *count_in;
     // Material-sorted shading (shade_sort.cuh), by (walk, material, chosen lobe).
     // Block-uniform chunk loop.
-    for (uint32_t c0 = blockIdx.x * BSHADE_CHUNK; c0 < n; c0 += gridDim.x * BSHADE_CHUNK) {
-        const uint32_t cn = min(BSHADE_CHUNK, n - c0);
-        sort_chunk(sm, cn, [&](uint32_t i) {
+    const uint32_t per = chunk_per_thread<BLOCK, BSHADE_PER_THREAD>(n, gridDim.x);
+    const uint32_t chunk = BLOCK * per;
+    for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
+        const uint32_t cn = min(chunk, n - c0);
+        sort_chunk<BLOCK, SHADE_PER_THREAD>(sm, cn, per, [&](uint32_t i) {
             uint32_t q = c0 + i;
             uint32_t sl = q_slot[q];
             uint32_t w = sl & 1u;
             uint32_t dim = (w ? DIM_LIGHT_WALK : DIM_CAMERA_WALK) + 4 * vcount[sl];
             return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(key_buf[sl >> 1], dim), w);
         });
-        for (uint32_t e = 0; e < BSHADE_PER_THREAD; ++e) {
+        for (uint32_t e = 0; e < per; ++e) {
             uint32_t i = e * BLOCK + threadIdx.x;
             bool alive = false;
             uint32_t slot = 0;
@@ -474,8 +476,10 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             if (s1 != GR_OK) return s1;
             GR_CUDA_TRY(cudaGetLastError());
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            int grid = resident_grid(k_bdpt_shade, 0, (p.nslots + BSHADE_PER_THREAD - 1) / BSHADE_PER_THREAD);
-            k_bdpt_shade<<<grid, BLOCK, 0, st>>>(job.scene, p, vs, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
+            const size_t ssmem = sort_smem_bytes(BLOCK, BSHADE_PER_THREAD);
+            GR_CUDA_TRY(allow_sort_smem(k_bdpt_shade, ssmem));
+            int grid = resident_grid(k_bdpt_shade, ssmem, (p.nslots + BSHADE_PER_THREAD - 1) / BSHADE_PER_THREAD);
+            k_bdpt_shade<<<grid, BLOCK, ssmem, st>>>(job.scene, p, vs, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                                  ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
                                                  ps.q_hit.as<float4>(), bs.vcount.as<uint32_t>(), ps.tp.as<float4>(),
                                                  ps.key.as<unsigned long long>(), bs.flags.as<uint32_t>(),

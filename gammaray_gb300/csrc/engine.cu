@@ -12,8 +12,7 @@ namespace gr {
 namespace {
 
 constexpr int EBLOCK = 128;
-constexpr uint32_t ESHADE_PER_THREAD = 4;
-constexpr uint32_t ESHADE_CHUNK = EBLOCK * ESHADE_PER_THREAD;
+constexpr uint32_t ESHADE_PER_THREAD = SHADE_PER_THREAD;
 #ifndef GR_SHADE_MIN_BLOCKS
 #define GR_SHADE_MIN_BLOCKS 6
 #endif
@@ -230,15 +229,18 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
                 const float4* __restrict__ q_d, const float4* __restrict__ q_hit, float4* __restrict__ s_hot,
                 const uint4* __restrict__ s_cold, uint32_t* __restrict__ nslot, float4* __restrict__ no,
                 float4* __restrict__ nd) {
-    __shared__ SortSmem<EBLOCK, ESHADE_PER_THREAD> sm;
+    extern __shared__ unsigned char dsmem[];
+    const SortView sm = sort_view<EBLOCK, ESHADE_PER_THREAD>(dsmem);
     const int nxt = cur ^ 1;
     const uint32_t n = c->q[cur];
     const unsigned lane = threadIdx.x & 31u;
     // Material-sorted shading (shade_sort.cuh), by (job, material, chosen lobe); misses,
     // cancelled and display-colour jobs share bucket 0.  Block-uniform chunk loop.
-    for (uint32_t c0 = blockIdx.x * ESHADE_CHUNK; c0 < n; c0 += gridDim.x * ESHADE_CHUNK) {
-        const uint32_t cn = min(ESHADE_CHUNK, n - c0);
-        sort_chunk(sm, cn, [&](uint32_t i) {
+    const uint32_t per = chunk_per_thread<EBLOCK, ESHADE_PER_THREAD>(n, gridDim.x);
+    const uint32_t chunk = EBLOCK * per;
+    for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
+        const uint32_t cn = min(chunk, n - c0);
+        sort_chunk<EBLOCK, ESHADE_PER_THREAD>(sm, cn, per, [&](uint32_t i) {
             uint32_t q = c0 + i;
             uint32_t jb = __float_as_uint(q_o[q].w);
             const DevJob& J = jobs[jb];
@@ -248,7 +250,7 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
             uint64_t key = (static_cast<uint64_t>(__float_as_uint(kb.w)) << 32) | __float_as_uint(kb.z);
             return shade_bucket(J.scene, k, uniform01(key, DIM_CAMERA_WALK + 4 * __float_as_uint(q_d[q].w)), jb);
         });
-        for (uint32_t e = 0; e < ESHADE_PER_THREAD; ++e) {
+        for (uint32_t e = 0; e < per; ++e) {
             uint32_t i = e * EBLOCK + threadIdx.x;
             bool alive = false, finished = false;
             uint32_t slot = 0, job = 0, unit = 0xFFFFFFFFu, depth = 0;
@@ -406,6 +408,7 @@ gr_status Engine::init(const EngineConfig& cfg, cudaStream_t) {
     GR_CUDA_TRY(cudaMemsetAsync(unit_done_.ptr, 0, ENGINE_MAX_UNITS * sizeof(uint32_t), st_));
     GR_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&h_pinned_), 8 * sizeof(uint64_t), cudaHostAllocDefault));
     GR_CUDA_TRY(cudaStreamSynchronize(st_));
+    GR_CUDA_TRY(allow_sort_smem(k_eng_shade, sort_smem_bytes(EBLOCK, ESHADE_PER_THREAD)));
     return record_pair();
 }
 
@@ -437,8 +440,10 @@ gr_status Engine::enqueue_iteration(int cur) {
                                        q_d_[cur].as<float4>(), q_hit_.as<float4>(), C, st_));
     }
     GR_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(c) + offsetof(EngineCtl, q) + nxt * sizeof(uint32_t), 0, 4, st_));
-    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), EBLOCK, 0, (C + ESHADE_PER_THREAD - 1) / ESHADE_PER_THREAD);
-    k_eng_shade<<<sgrid, EBLOCK, 0, st_>>>(c, cur, jobs_.as<DevJob>(), unit_done_.as<uint32_t>(),
+    const size_t ssmem = sort_smem_bytes(EBLOCK, ESHADE_PER_THREAD);
+    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), EBLOCK, ssmem,
+                         (C + ESHADE_PER_THREAD - 1) / ESHADE_PER_THREAD);
+    k_eng_shade<<<sgrid, EBLOCK, ssmem, st_>>>(c, cur, jobs_.as<DevJob>(), unit_done_.as<uint32_t>(),
                                            q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>(),
                                            q_hit_.as<float4>(), s_hot_.as<float4>(), s_cold_.as<uint4>(),
                                            q_slot_[nxt].as<uint32_t>(), q_o_[nxt].as<float4>(),

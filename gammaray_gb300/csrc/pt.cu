@@ -67,10 +67,8 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
 }
 
 
-// Material-sorted shading (shade_sort.cuh): each block sorts its SHADE_CHUNK-entry chunk
-// of the queue by (material, chosen lobe), then shades it in that order.
-constexpr uint32_t SHADE_PER_THREAD = 4;
-constexpr uint32_t SHADE_CHUNK = BLOCK * SHADE_PER_THREAD;
+// Material-sorted shading (shade_sort.cuh): each block sorts its chunk of the queue by
+// (material, chosen lobe), then shades it in that order.
 
 __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t depth,
                                                  const uint32_t* __restrict__ count_in,
@@ -80,18 +78,21 @@ __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t dept
                                                  const unsigned long long* __restrict__ key_buf, uint32_t* count_out,
                                                  uint32_t* __restrict__ nslot, float4* __restrict__ no,
                                                  float4* __restrict__ nd) {
-    __shared__ SortSmem<BLOCK, SHADE_PER_THREAD> sm;
+    extern __shared__ unsigned char dsmem[];
+    const SortView sm = sort_view<BLOCK, SHADE_PER_THREAD>(dsmem);
     const uint32_t n = *count_in;
     const uint32_t base = DIM_CAMERA_WALK + 4 * depth;
     // Block-uniform chunk loop (sort_chunk's barriers need every thread).
-    for (uint32_t c0 = blockIdx.x * SHADE_CHUNK; c0 < n; c0 += gridDim.x * SHADE_CHUNK) {
-        const uint32_t cn = min(SHADE_CHUNK, n - c0);
-        sort_chunk(sm, cn, [&](uint32_t i) {
+    const uint32_t per = chunk_per_thread<BLOCK, SHADE_PER_THREAD>(n, gridDim.x);
+    const uint32_t chunk = BLOCK * per;
+    for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
+        const uint32_t cn = min(chunk, n - c0);
+        sort_chunk<BLOCK, SHADE_PER_THREAD>(sm, cn, per, [&](uint32_t i) {
             uint32_t q = c0 + i;
             return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(key_buf[q_slot[q]], base), 0);
         });
         // Every lane runs every step so that all of them reach the ballot in push_warp.
-        for (uint32_t e = 0; e < SHADE_PER_THREAD; ++e) {
+        for (uint32_t e = 0; e < per; ++e) {
             uint32_t i = e * BLOCK + threadIdx.x;
             bool alive = false;
             uint32_t slot = 0;
@@ -205,6 +206,8 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     if (static_cast<uint64_t>(group) * npix > 0xFFFFFFFFull / 2) group = 1;
     PathState& ps = device_work().paths;
     GR_CUDA_TRY(ps.ensure(static_cast<size_t>(group) * npix));
+    const size_t shade_smem = sort_smem_bytes(BLOCK, SHADE_PER_THREAD);
+    GR_CUDA_TRY(allow_sort_smem(k_shade, shade_smem));
     uint32_t* cnt = sc->counters.as<uint32_t>();
     int* err = reinterpret_cast<int*>(cnt + CNT_ERROR);
     unsigned long long* rays = reinterpret_cast<unsigned long long*>(cnt + CNT_RAYS);
@@ -290,8 +293,8 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
             if (timed) GR_TRY_S(mark(e0));
-            int grid = resident_grid(k_shade, 0, (n + SHADE_PER_THREAD - 1) / SHADE_PER_THREAD);
-            k_shade<<<grid, BLOCK, 0, st>>>(job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
+            int grid = resident_grid(k_shade, shade_smem, (n + SHADE_PER_THREAD - 1) / SHADE_PER_THREAD);
+            k_shade<<<grid, BLOCK, shade_smem, st>>>(job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                             ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
                                             ps.q_hit.as<float4>(), ps.tp.as<float4>(), ps.light.as<float4>(),
                                             ps.key.as<unsigned long long>(), cnt + nxt,
@@ -433,6 +436,8 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
     void* base = nullptr;
     GR_TRY_S(static_scratch(&base));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t shade_smem = sort_smem_bytes(BLOCK, SHADE_PER_THREAD);
+    GR_CUDA_TRY(allow_sort_smem(k_shade, shade_smem));
     const uint32_t npix = static_cast<uint32_t>(npix64);
     const size_t cap = STATIC_MAX_PATHS;
     // Carve the array (same layout for every call; every region is 16-byte aligned).
@@ -491,8 +496,8 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
                 break;
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            int grid = resident_grid(k_shade, 0, (n + SHADE_PER_THREAD - 1) / SHADE_PER_THREAD);
-            k_shade<<<grid, BLOCK, 0, st>>>(sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit, tp,
+            int grid = resident_grid(k_shade, shade_smem, (n + SHADE_PER_THREAD - 1) / SHADE_PER_THREAD);
+            k_shade<<<grid, BLOCK, shade_smem, st>>>(sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit, tp,
                                             light, key, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt]);
             GR_CUDA_TRY(cudaGetLastError());
             if (p.max_depth == 0 && (depth & 3) == 3) {

@@ -12,49 +12,84 @@ namespace gr {
 
 constexpr uint32_t SORT_BUCKETS = 32;
 
-template <uint32_t NT, uint32_t PER>
-struct SortSmem {
-    uint32_t start[SORT_BUCKETS];
-    uint16_t order[NT * PER];
+// Most queue entries each thread of a shading block sorts and shades per chunk.  Larger
+// chunks give fuller warps per bucket and amortise the sort's barriers; on the
+// path-tracer workload 4 -> 8 -> 16 entries per thread measured 937 -> 1011 -> 1070
+// Msamples/s.  The entries per thread of a launch are chosen from the queue length
+// (chunk_per_thread) so that small queues still spread over every block.
+#ifndef GR_SHADE_PER_THREAD
+#define GR_SHADE_PER_THREAD 64
+#endif
+constexpr uint32_t SHADE_PER_THREAD = GR_SHADE_PER_THREAD;
+
+// The sort's shared memory (dynamic, sort_smem_bytes(NT, PER) bytes at the start of the
+// block's dynamic shared memory): bucket sizes, then per-entry bucket and sorted order.
+struct SortView {
+    uint32_t* count;  // SORT_BUCKETS: bucket sizes, then running positions
+    uint8_t* bucket;
+    uint16_t* order;
 };
 
-// Sorts positions 0..cn-1 (cn <= NT * PER) by bucket_of(i) < SORT_BUCKETS into
-// sm.order.  Every thread of an NT-thread block must call it.  It ends with a barrier;
-// the caller needs one more before the next call reuses `sm`.  Within a bucket the order
-// is unspecified.
+inline size_t sort_smem_bytes(uint32_t nt, uint32_t per) {
+    return SORT_BUCKETS * sizeof(uint32_t) + static_cast<size_t>(nt) * per * (sizeof(uint8_t) + sizeof(uint16_t));
+}
+
+// Lets `kernel` use `bytes` of dynamic shared memory (needed above 48 KB).  Call it
+// before the first launch (and before a graph capture that contains one).
+template <class K>
+cudaError_t allow_sort_smem(K kernel, size_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+template <uint32_t NT, uint32_t PER>
+GR_D SortView sort_view(unsigned char* smem) {
+    uint32_t* count = reinterpret_cast<uint32_t*>(smem);
+    uint16_t* order = reinterpret_cast<uint16_t*>(count + SORT_BUCKETS);
+    uint8_t* bucket = reinterpret_cast<uint8_t*>(order + NT * PER);
+    return SortView{count, bucket, order};
+}
+
+// Entries per thread for a queue of n entries over `blocks` blocks of NT threads: about
+// one chunk per block, at most PER.
+template <uint32_t NT, uint32_t PER>
+GR_D uint32_t chunk_per_thread(uint32_t n, uint32_t blocks) {
+    uint32_t per = (n + blocks * NT - 1) / (blocks * NT);
+    return per < 1 ? 1 : (per > PER ? PER : per);
+}
+
+// Sorts positions 0..cn-1 (cn <= NT * per, per <= PER) by bucket_of(i) < SORT_BUCKETS
+// into sm.order.  Every thread of an NT-thread block must call it with the same cn and
+// per.  It ends with a barrier; the caller needs one more before the next call reuses
+// `sm`.  Within a bucket the order is unspecified.
 template <uint32_t NT, uint32_t PER, class F>
-GR_D void sort_chunk(SortSmem<NT, PER>& sm, uint32_t cn, F bucket_of) {
+GR_D void sort_chunk(const SortView& sm, uint32_t cn, uint32_t per, F bucket_of) {
     static_assert(NT * PER <= 65536, "chunk positions are 16-bit");
     static_assert(SORT_BUCKETS == 32, "the scan below is one warp");
     const uint32_t tid = threadIdx.x;
-    if (tid < SORT_BUCKETS) sm.start[tid] = 0;
+    if (tid < SORT_BUCKETS) sm.count[tid] = 0;
     __syncthreads();
-    uint32_t bucket[PER], rank[PER];
-#pragma unroll
-    for (uint32_t e = 0; e < PER; ++e) {
+    for (uint32_t e = 0; e < per; ++e) {
         uint32_t i = e * NT + tid;
-        bucket[e] = 0;
-        rank[e] = 0;
         if (i < cn) {
-            bucket[e] = bucket_of(i);
-            rank[e] = atomicAdd(&sm.start[bucket[e]], 1u);
+            uint32_t b = bucket_of(i);
+            sm.bucket[i] = static_cast<uint8_t>(b);
+            atomicAdd(&sm.count[b], 1u);
         }
     }
     __syncthreads();
-    if (tid < 32) {  // exclusive scan of the bucket counts
-        uint32_t c = sm.start[tid], x = c;
+    if (tid < 32) {  // exclusive scan of the bucket sizes
+        uint32_t c = sm.count[tid], x = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
             if (static_cast<int>(tid) >= o) x += y;
         }
-        sm.start[tid] = x - c;
+        sm.count[tid] = x - c;
     }
     __syncthreads();
-#pragma unroll
-    for (uint32_t e = 0; e < PER; ++e) {
+    for (uint32_t e = 0; e < per; ++e) {
         uint32_t i = e * NT + tid;
-        if (i < cn) sm.order[sm.start[bucket[e]] + rank[e]] = static_cast<uint16_t>(i);
+        if (i < cn) sm.order[atomicAdd(&sm.count[sm.bucket[i]], 1u)] = static_cast<uint16_t>(i);
     }
     __syncthreads();
 }

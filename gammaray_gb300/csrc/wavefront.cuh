@@ -25,8 +25,18 @@ constexpr int BLOCK = 128;
 // launches never depend on a host read of the queue length.  Each thread traverses one
 // ray at a time with the step function and the shared/local hybrid stack; a ray that
 // needs more steps than the tree could ever require is abandoned and flagged (err = 2).
+// GR_EXTEND_MIN_BLOCKS caps registers for that many resident blocks per SM (0: uncapped).
+#ifndef GR_EXTEND_MIN_BLOCKS
+#define GR_EXTEND_MIN_BLOCKS 0
+#endif
+#if GR_EXTEND_MIN_BLOCKS > 0
+#define GR_EXTEND_BOUNDS __launch_bounds__(BLOCK, GR_EXTEND_MIN_BLOCKS)
+#else
+#define GR_EXTEND_BOUNDS __launch_bounds__(BLOCK)
+#endif
+
 template <int W, bool COUNT>
-__global__ void __launch_bounds__(BLOCK) k_extend(DeviceScene s, const uint32_t* __restrict__ count,
+__global__ void GR_EXTEND_BOUNDS k_extend(DeviceScene s, const uint32_t* __restrict__ count,
                                                      const float4* __restrict__ q_o, const float4* __restrict__ q_d,
                                                      float4* __restrict__ q_hit, int* err,
                                                      unsigned long long* rays) {
