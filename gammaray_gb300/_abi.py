@@ -277,6 +277,7 @@ SIGNATURES = {
     "gr_film_resolve": (C.c_int, [_VP, _PF]),
     "gr_film_write_exr": (C.c_int, [_VP, C.c_char_p]),
     "gr_film_passes": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
+    "gr_film_read_splat": (C.c_int, [_VP, _PF]),
     "gr_render_params_default": (None, [C.c_int32, C.POINTER(RenderParams)]),
     "gr_render": (C.c_int, [_VP, C.POINTER(CameraDesc), C.POINTER(RenderParams), _VP]),
     "gr_render_samples": (

@@ -340,7 +340,10 @@ class PathTracerIntegrator:
 
 @dataclass
 class BdptIntegrator:
-    """render/integrators.rs:102-418 (BDPT_MAX_DEPTH = 16, roulette from length 4)."""
+    """render/integrators.rs:102-418 (BDPT_MAX_DEPTH = 16, roulette from length 4).
+
+    Extensions, off by default: mis = 1 weights the strategies by the power heuristic;
+    light_tracing = 1 adds the light-walk-to-camera strategy, splatted into the film."""
 
     max_depth: int = 16
     rr_depth: int = 4
@@ -423,6 +426,13 @@ class Film:
         n = C.c_uint32()
         self.lib.call("gr_film_passes", self.handle, C.byref(n))
         return n.value
+
+    def read_splat(self) -> np.ndarray:
+        """Light-tracing splat sums (H,W,3) — the BDPT extension's splat buffer; resolve()
+        adds them divided by passes()."""
+        sp = np.empty((self.height, self.width, 3), np.float32)
+        self.lib.call("gr_film_read_splat", self.handle, fptr(sp))
+        return sp
 
 
 def scene_desc(prims, environment=(0.0, 0.0, 0.0), bvh_width: int = 0, leaf_size: int = 0):

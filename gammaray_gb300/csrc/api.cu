@@ -300,7 +300,23 @@ gr_status gr_film_destroy(gr_film* f) {
 gr_status gr_film_clear(gr_film* f) {
     if (!f) return fail(GR_ERR_INVALID_ARGUMENT, "null film");
     GR_CUDA_TRY(cudaMemset(f->pixels.ptr, 0, static_cast<size_t>(f->width) * f->height * sizeof(float4)));
+    if (f->splat.ptr) GR_CUDA_TRY(cudaMemset(f->splat.ptr, 0, static_cast<size_t>(f->width) * f->height * sizeof(float4)));
     f->passes = 0;
+    return GR_OK;
+}
+
+static float splat_scale(const gr_film* f) { return f->passes ? 1.0f / static_cast<float>(f->passes) : 0.0f; }
+
+gr_status gr_film_read_splat(const gr_film* f, float* splat) {
+    if (!f || !splat) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
+    size_t n = static_cast<size_t>(f->width) * f->height;
+    std::vector<float4> px(n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    if (f->splat.ptr) GR_CUDA_TRY(cudaMemcpy(px.data(), f->splat.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) {
+        splat[3 * i] = px[i].x;
+        splat[3 * i + 1] = px[i].y;
+        splat[3 * i + 2] = px[i].z;
+    }
     return GR_OK;
 }
 
@@ -325,7 +341,7 @@ gr_status gr_film_resolve(const gr_film* f, float* rgb) {
     uint32_t n = f->width * f->height;
     DevBuf out;
     GR_CUDA_TRY(out.ensure(static_cast<size_t>(n) * 3 * sizeof(float)));
-    GR_TRY(film_resolve(f->pixels.as<float4>(), n, out.as<float>(), 0));
+    GR_TRY(film_resolve(f->pixels.as<float4>(), f->splat.as<float4>(), splat_scale(f), n, out.as<float>(), 0));
     GR_CUDA_TRY(cudaMemcpy(rgb, out.ptr, static_cast<size_t>(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost));
     return GR_OK;
 }
@@ -399,7 +415,8 @@ gr_status gr_film_write_exr(const gr_film* f, const char* path) {
     size_t data_bytes = line * f->height;
     DevBuf dev;
     GR_CUDA_TRY(dev.ensure(data_bytes));
-    GR_TRY(film_exr_pack(f->pixels.as<float4>(), f->width, f->height, dev.as<unsigned char>(), 0, 0));
+    GR_TRY(film_exr_pack(f->pixels.as<float4>(), f->splat.as<float4>(), splat_scale(f), f->width, f->height,
+                         dev.as<unsigned char>(), 0, 0));
     b.resize(data_offset + data_bytes);
     GR_CUDA_TRY(cudaMemcpy(b.data() + data_offset, dev.ptr, data_bytes, cudaMemcpyDeviceToHost));
     std::ofstream os(path, std::ios::binary);
@@ -415,7 +432,7 @@ gr_status gr_film_passes(const gr_film* f, uint32_t* p) {
 }
 
 static gr_status run_render(gr_scene* s, const gr_camera* c, const gr_render_params* p, uint32_t w, uint32_t h,
-                            float4* film, float* samples_out) {
+                            float4* film, float* samples_out, float4* splat = nullptr) {
     RenderJob job;
     job.scene = s->dev;
     job.camera = make_camera(*c);
@@ -423,6 +440,7 @@ static gr_status run_render(gr_scene* s, const gr_camera* c, const gr_render_par
     job.width = w;
     job.height = h;
     job.film = film;
+    job.splat = splat;
     job.samples_out = samples_out;
     cudaStream_t st = s->stream;
     std::memset(&s->stats, 0, sizeof(s->stats));
@@ -459,7 +477,16 @@ gr_status gr_render(gr_scene* s, const gr_camera* c, const gr_render_params* p, 
     if (!s || !c || !f) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
     GR_TRY(check_params(p));
     std::lock_guard<std::mutex> g(s->mu);
-    GR_TRY(run_render(s, c, p, f->width, f->height, f->pixels.as<float4>(), nullptr));
+    float4* splat = nullptr;
+    if (p->integrator == GR_INTEGRATOR_BDPT && p->light_tracing) {
+        if (!f->splat.ptr) {
+            size_t bytes = static_cast<size_t>(f->width) * f->height * sizeof(float4);
+            GR_CUDA_TRY(f->splat.ensure(bytes));
+            GR_CUDA_TRY(cudaMemset(f->splat.ptr, 0, bytes));
+        }
+        splat = f->splat.as<float4>();
+    }
+    GR_TRY(run_render(s, c, p, f->width, f->height, f->pixels.as<float4>(), nullptr, splat));
     f->passes += p->spp;
     return GR_OK;
 }

@@ -1,5 +1,7 @@
 // Wavefront BDPT: BdptIntegrator::integrate (render/integrators.rs:357-418) with the
-// reference's uniform strategy weights 1 / (c + l) (integrators.rs:345-354).
+// reference's uniform strategy weights 1 / (c + l) (integrators.rs:345-354), and two
+// extensions (off by default): power-heuristic MIS weights and the light-tracing
+// strategy (light-walk vertex -> pinhole camera, splatted with atomics).
 //
 //   raygen    per path: jitter + camera ray (camera walk, slot 2i) and Bvh::sample_light
 //             + the light vertex (light walk, slot 2i+1), both pushed to one queue
@@ -8,11 +10,13 @@
 //             throughput, shading-normal correction on light paths, roulette from
 //             length rr_len; each vertex is stored SoA, the escape vertex too
 //   connect   per path, every strategy (c >= 1, l >= 0, c + l <= max) in the reference's
-//             loop order: connect() (integrators.rs:269-343) without the visibility test;
-//             terms that need one queue a shadow ray
+//             loop order: connect() (integrators.rs:269-343) without the visibility test,
+//             times its weight; terms that need one queue a shadow ray.  With light
+//             tracing, every light-walk vertex inside the image also gets a camera term.
 //   shadow    Bvh::visibility (bvh.rs:460-477) as an any-hit query
-//   gather    per path, sums the strategy terms in loop order (deterministic, same
-//             order as the reference)
+//   gather    per path, sums the weighted strategy terms in loop order (deterministic,
+//             same order as the reference); visible light-tracing terms are added to
+//             the film's splat buffer with atomics
 //   film      the deterministic splat of film.cu
 #include <algorithm>
 #include <cstdlib>
@@ -25,7 +29,7 @@ namespace gr {
 
 namespace {
 
-constexpr int VREC = 7;            // float4 per stored vertex
+constexpr int VREC = 8;            // float4 per stored vertex
 constexpr uint32_t F_SKIP = 1;     // light sample had a zero pdf: the reference returns early
 constexpr uint32_t F_ESCAPE = 2;   // the camera walk escaped (environment term)
 constexpr float E_NO_TEST = 0.0f;  // entry flags (float in .w)
@@ -35,18 +39,54 @@ constexpr float E_OCCLUDED = 3.0f;
 constexpr int CNT_ENTRIES = 12;
 constexpr int CNT_SHADOWQ = 13;
 
+// The pinhole camera seen from the scene (light-tracing and MIS extensions): position,
+// world directions of its x, y, z axes (the camera matrix is a rotation and a
+// translation, camera.rs:42-61) and the [-1, 1]^2 window on the plane at distance 1.
+struct PinholeView {
+    V3 pos, axis[3];
+    float wx, wy, area;
+    // Film position (s, t) of p, its distance and the cosine between the viewing axis
+    // and the direction to p; false when p is behind the camera or outside the window.
+    GR_D bool project(V3 p, float& s, float& t, float& dist, float& cos_view) const {
+        V3 v = p - pos;
+        float cx = dot(v, axis[0]), cy = dot(v, axis[1]), cz = dot(v, axis[2]);
+        if (!(cz < 0.0f)) return false;
+        s = (cx / -cz) / wx;
+        t = (cy / -cz) / wy;
+        dist = magnitude(v);
+        cos_view = -cz / dist;
+        return s >= -1.0f && s <= 1.0f && t >= -1.0f && t <= 1.0f;
+    }
+    // Solid-angle pdf of a camera ray spread uniformly over the window: 1 / (area cos^3).
+    GR_D float dir_pdf(float cos_view) const { return 1.0f / (area * cos_view * cos_view * cos_view); }
+};
+
 struct BdptParams {
     DevCamera cam;
+    PinholeView view;
     uint32_t width, height, npix, first_pass;
     uint64_t seed;
     uint32_t max_len, rr_len;
     uint32_t n;       // paths in this group
     uint32_t nslots;  // 2 n
+    uint32_t mis;     // power-heuristic weights (else uniform)
+    uint32_t lt;      // light-tracing strategy
 };
 
-// Stored vertex (BdptVertex, integrators.rs:107-130) as 7 float4, field-major:
+// Solid-angle pdf at `from` of the direction toward `to`, as an area density at `to`
+// (geometric normal ng).
+GR_D float to_area(float pdf, V3 from, V3 to, V3 ng) {
+    V3 v = to - from;
+    float d2 = dot(v, v);
+    if (d2 == 0.0f) return 0.0f;
+    return pdf * (fabsf(dot(ng, v)) / sqrtf(d2)) / d2;
+}
+
+// Stored vertex (BdptVertex, integrators.rs:107-130) as 8 float4, field-major:
 //   0: point, prim     1: incoming, connectible   2: normal, tp.x   3: tangent, tp.y
 //   4: binormal, tp.z  5: geom_normal, material   6: emission
+//   7: MIS extension: area pdf of the vertex from its predecessor on its walk (afwd) and
+//      from its successor (arev), specular-sample flag
 struct Verts {
     float4* v;
     uint32_t nslots;
@@ -89,6 +129,15 @@ GR_D void store_vertex(const Verts& vs, uint32_t k, uint32_t slot, V3 point, uin
     vs.at(k, 4, slot) = make_float4(f.binormal.x, f.binormal.y, f.binormal.z, tp.z);
     vs.at(k, 5, slot) = make_float4(f.geom_normal.x, f.geom_normal.y, f.geom_normal.z, __uint_as_float(material));
     vs.at(k, 6, slot) = make_float4(emission.x, emission.y, emission.z, 0.0f);
+}
+
+struct VPdf {
+    float afwd, arev;
+    bool delta;
+};
+GR_D VPdf load_pdf(const Verts& vs, uint32_t k, uint32_t slot) {
+    float4 f7 = vs.at(k, 7, slot);
+    return VPdf{f7.x, f7.y, f7.z != 0.0f};
 }
 
 // Warp-aggregated counter increment for divergent code (the lanes active here).
@@ -140,7 +189,9 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams
         escape[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         uint32_t fl = 0;
         vcount[2 * i] = 0;
-        tp_buf[2 * i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        // .w carries the solid-angle pdf of the walk's next direction (MIS extension).
+        float cam_pdf = (p.mis || p.lt) ? p.view.dir_pdf(dot(cd, -p.view.axis[2])) : 0.0f;
+        tp_buf[2 * i] = make_float4(1.0f, 1.0f, 1.0f, cam_pdf);
         cam_alive = p.max_len > 0;
         vcount[2 * i + 1] = 0;
         if (s.num_lights > 0) {
@@ -156,8 +207,9 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams
                         (fabsf(dot(ls.frame.geom_normal, ls.direction)) / (ls.point_pdf * ls.dir_pdf));
                 store_vertex(vs, 0, 2 * i + 1, ls.origin, ls.prim, v3zero(), true, ls.frame, v3one() / ls.point_pdf,
                              mi, v3zero());
+                vs.at(0, 7, 2 * i + 1) = make_float4(ls.point_pdf, 0.0f, 0.0f, 0.0f);
                 vcount[2 * i + 1] = 1;
-                tp_buf[2 * i + 1] = make_float4(ie.x, ie.y, ie.z, 0.0f);
+                tp_buf[2 * i + 1] = make_float4(ie.x, ie.y, ie.z, ls.dir_pdf);
                 light_alive = !is_zero(ie) && 1 < p.max_len;
                 lo = nudge(ls.origin, ls.direction);
                 ld = ls.direction;
@@ -219,6 +271,7 @@ __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts 
                     // throughput at the escape is kept for the environment extension.
                     Frame z{v3zero(), v3zero(), v3zero(), v3zero()};
                     store_vertex(vs, k, slot, v3zero(), NO_INDEX, -d, false, z, tp, 0, v3zero());
+                    vs.at(k, 7, slot) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     vcount[slot] = k + 1;
                     if (walk == 0) {
                         escape[path] = make_float4(tp.x, tp.y, tp.z, 0.0f);
@@ -239,6 +292,25 @@ __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts 
                     V3 ntp = mul(tp, ms.radiance * (fabsf(dot(f.normal, ms.outgoing)) / ms.pdf));
                     ntp = ntp * correct_shading_normal(incoming, ms.outgoing, f, c2l);
                     store_vertex(vs, k, slot, hit_point, prim, incoming, connectible, f, tp, mi, ms.emission);
+                    const bool delta = (ms.kind & LOBE_SPECULAR) != 0;
+                    if (p.mis || p.lt) {
+                        // Area pdfs (MIS extension): this vertex from its predecessor, and the
+                        // predecessor from this vertex (reverse BSDF pdf; zero after a
+                        // specular sample, PBRT 3e section 16.3.2).
+                        const bool has_prev = walk == 1 || k > 0;
+                        V3 prev = p.view.pos;
+                        if (has_prev) {
+                            float4 pp = vs.at(k - 1, 0, slot);
+                            prev = V3{pp.x, pp.y, pp.z};
+                        }
+                        float afwd = to_area(t4.w, prev, hit_point, f.geom_normal);
+                        vs.at(k, 7, slot) = make_float4(afwd, 0.0f, delta ? 1.0f : 0.0f, 0.0f);
+                        if (has_prev) {
+                            float4 pn = vs.at(k - 1, 5, slot);
+                            float rev = delta ? 0.0f : pdf_world(m, ms.outgoing, incoming, f);
+                            vs.at(k - 1, 7, slot).y = to_area(rev, hit_point, prev, V3{pn.x, pn.y, pn.z});
+                        }
+                    }
                     vcount[slot] = k + 1;
                     if (k + 1 >= p.rr_len || nearly_zero(ntp)) {
                         float rv = uniform01(key, base + 3);
@@ -248,7 +320,7 @@ __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts 
                     alive = !is_zero(ntp) && k + 1 < p.max_len;
                     new_o = nudge(hit_point, ms.outgoing);
                     new_d = ms.outgoing;
-                    if (alive) tp_buf[slot] = make_float4(ntp.x, ntp.y, ntp.z, 0.0f);
+                    if (alive) tp_buf[slot] = make_float4(ntp.x, ntp.y, ntp.z, delta ? 0.0f : ms.pdf);
                 }
             }
             push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
@@ -263,12 +335,108 @@ GR_D uint32_t num_entries(uint32_t cs, uint32_t ls, uint32_t max_len) {
     return e;
 }
 
-// connect() for every strategy of one path, in the reference's loop order.
+// ---------------------------------------------------- MIS extension (power heuristic)
+// Veach 1997 eq. 10.9 with beta = 2, in the ratio form of PBRT 3e section 16.3.4: per
+// vertex the area pdfs of generating it along its own walk (afwd) and from the other
+// side (arev), ratios of neighbouring strategies' pdfs chained outwards from the
+// connection, delta (specular) vertices skipped and zero pdfs counted as 1.  The
+// strategies are (c camera-walk, l light-walk vertices), c + l <= max_len, and with
+// light tracing also c = 0.  The oracle states the same function (orender.hpp).
+
+// Area pdf with which Bvh::sample_light picks a point of light prim `prim`
+// (bvh.rs:481-496, mesh.rs:310-327, sphere.rs:103-111).
+GR_D float light_point_pdf(const DeviceScene& s, uint32_t prim) {
+    for (uint32_t k = 0; k < s.num_lights; ++k) {
+        const LightRec& L = s.lights[k];
+        if (L.prim != prim) continue;
+        float pdf = L.type == PRIM_SPHERE ? 1.0f / (4.0f * PI * L.radius * L.radius) : 1.0f / L.area;
+        return pdf / static_cast<float>(s.num_lights);
+    }
+    return 0.0f;
+}
+
+// Pdf of a light emitting toward w: cosine about the geometric normal (prim.rs:37-51).
+GR_D float light_dir_pdf(const Frame& f, V3 w) {
+    float c = dot(f.geom_normal, w);
+    return c > 0.0f ? c * FRAC_1_PI : 0.0f;
+}
+
+GR_D float remap0(float x) { return x != 0.0f ? x : 1.0f; }
+
+constexpr int MAX_WALK = 16;
+
+// Weight of strategy (c, l) from both walks' vertex pdfs, with the reverse pdfs the
+// connection implies for the last vertex of each walk and the one before it.
+// lt_possible: the light-tracing strategy can produce this path.
+GR_D float mis_weight(const VPdf* cp, const VPdf* lp, uint32_t c, uint32_t l, float z_rev, float zm_rev, float y_rev,
+                      float ym_rev, bool lt_possible) {
+    float sum = 0.0f, r = 1.0f;
+    for (uint32_t k = c; k-- > 0;) {
+        float rev = k + 1 == c ? z_rev : (k + 2 == c ? zm_rev : cp[k].arev);
+        r *= remap0(rev) / remap0(cp[k].afwd);
+        bool here = k + 1 == c ? false : cp[k].delta;
+        bool before = k == 0 ? false : cp[k - 1].delta;
+        if (k == 0 && !lt_possible) continue;
+        if (!here && !before) sum += r * r;
+    }
+    r = 1.0f;
+    for (uint32_t k = l; k-- > 0;) {
+        float rev = k + 1 == l ? y_rev : (k + 2 == l ? ym_rev : lp[k].arev);
+        r *= remap0(rev) / remap0(lp[k].afwd);
+        bool here = k + 1 == l ? false : lp[k].delta;
+        bool before = k == 0 ? false : lp[k - 1].delta;
+        if (!here && !before) sum += r * r;
+    }
+    return 1.0f / (1.0f + sum);
+}
+
+struct VPos {
+    V3 point, ng;
+};
+GR_D VPos load_pos(const Verts& vs, uint32_t k, uint32_t slot) {
+    float4 f0 = vs.at(k, 0, slot), f5 = vs.at(k, 5, slot);
+    return VPos{V3{f0.x, f0.y, f0.z}, V3{f5.x, f5.y, f5.z}};
+}
+
+// MIS weight of camera strategy (c >= 1, l >= 0) with a non-zero connection.
+GR_D float strategy_weight(const DeviceScene& s, const Verts& vs, uint32_t i, const VPdf* cp, const VPdf* lp,
+                           uint32_t c, uint32_t l, const Vtx& z, const Vtx* y, bool lt_possible) {
+    const DevMaterial& zm = s.materials[z.material];
+    float z_rev = 0.0f, zm_rev = 0.0f, y_rev = 0.0f, ym_rev = 0.0f;
+    if (l == 0) {  // the camera walk hit a light
+        z_rev = light_point_pdf(s, z.prim);
+        if (c >= 2) {
+            VPos zp = load_pos(vs, c - 2, 2 * i);
+            zm_rev = to_area(light_dir_pdf(z.frame, z.incoming), z.point, zp.point, zp.ng);
+        }
+    } else {
+        const DevMaterial& ym = s.materials[y->material];
+        V3 w_yz = normalized(z.point - y->point);
+        float pz = l == 1 ? light_dir_pdf(y->frame, w_yz) : pdf_world(ym, y->incoming, w_yz, y->frame);
+        z_rev = to_area(pz, y->point, z.point, z.frame.geom_normal);
+        if (c >= 2) {
+            VPos zp = load_pos(vs, c - 2, 2 * i);
+            zm_rev = to_area(pdf_world(zm, -w_yz, z.incoming, z.frame), z.point, zp.point, zp.ng);
+        }
+        y_rev = to_area(pdf_world(zm, z.incoming, -w_yz, z.frame), z.point, y->point, y->frame.geom_normal);
+        if (l >= 2) {
+            VPos yp = load_pos(vs, l - 2, 2 * i + 1);
+            ym_rev = to_area(pdf_world(ym, w_yz, y->incoming, y->frame), y->point, yp.point, yp.ng);
+        }
+    }
+    return mis_weight(cp, lp, c, l, z_rev, zm_rev, y_rev, ym_rev, lt_possible);
+}
+
+// connect() for every strategy of one path, in the reference's loop order, each term
+// times its weight (uniform or MIS).  With light tracing, each light-walk vertex inside
+// the image gets a camera term in lt[i * max_len + l - 1] (value, flag) and its film
+// pixel in lt_pixel.
 __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParams p, Verts vs,
                                                         const uint32_t* __restrict__ vcount,
                                                         const uint32_t* __restrict__ flags, uint32_t* counters,
                                                         uint32_t* __restrict__ entry_base, float4* __restrict__ entries,
-                                                        uint4* __restrict__ shadow_q) {
+                                                        uint4* __restrict__ shadow_q, float4* __restrict__ lt,
+                                                        uint32_t* __restrict__ lt_pixel) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     uint32_t fl = flags[i];
@@ -277,6 +445,19 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParam
     uint32_t ne = num_entries(cs, ls, p.max_len);
     uint32_t base = ne ? atomicAdd(counters + CNT_ENTRIES, ne) : 0;
     entry_base[i] = base;
+    VPdf cp[MAX_WALK], lp[MAX_WALK];
+    bool lt_possible = false;
+    if (p.mis) {
+        for (uint32_t k = 0; k < cs; ++k) cp[k] = load_pdf(vs, k, 2 * i);
+        for (uint32_t k = 0; k < ls; ++k) lp[k] = load_pdf(vs, k, 2 * i + 1);
+    }
+    if (p.lt && cs > 0) {
+        VPos z1 = load_pos(vs, 0, 2 * i);
+        float4 f0 = vs.at(0, 0, 2 * i);
+        float ss, tt, dd, cv;
+        lt_possible = __float_as_uint(f0.w) != NO_INDEX && p.view.project(z1.point, ss, tt, dd, cv);
+    }
+    const uint32_t extra = p.lt ? 1u : 0u;
     uint32_t j = base;
     for (uint32_t c = 1; c <= cs; ++c) {
         Vtx cv = load_vertex(vs, c - 1, 2 * i);
@@ -284,10 +465,11 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParam
             if (c + l > p.max_len) continue;
             V3 term = v3zero();
             float flag = E_NO_TEST;
+            Vtx lv;
             if (l == 0) {
                 if (cv.prim != NO_INDEX) term = mul(cv.tp, cv.emission);
             } else {
-                Vtx lv = load_vertex(vs, l - 1, 2 * i + 1);
+                lv = load_vertex(vs, l - 1, 2 * i + 1);
                 if (cv.prim != NO_INDEX && lv.prim != NO_INDEX && cv.connectible && lv.connectible) {
                     V3 c2l = normalized(lv.point - cv.point);
                     V3 l2c = -c2l;
@@ -307,17 +489,67 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParam
                     }
                 }
             }
+            float w;
+            if (!p.mis) w = 1.0f / static_cast<float>(c + l + extra);  // integrators.rs:345-354
+            else w = is_zero(term) ? 0.0f : strategy_weight(s, vs, i, cp, lp, c, l, cv, l ? &lv : nullptr, lt_possible);
+            term = term * w;
             entries[j] = make_float4(term.x, term.y, term.z, flag);
             ++j;
         }
     }
+    if (!p.lt) return;
+    // Light tracing: light-walk vertex y -> camera.  We / pdf of a pinhole camera is
+    // 1 / (area cos^3 dist^2) (PBRT 3e section 16.1.1).
+    const uint32_t lmax = min(ls, p.max_len);
+    for (uint32_t l = 1; l <= p.max_len; ++l) {
+        size_t e = static_cast<size_t>(i) * p.max_len + (l - 1);
+        float4 out = make_float4(0.0f, 0.0f, 0.0f, E_NO_TEST);
+        uint32_t pix = 0;
+        if (l <= lmax) {
+            Vtx y = load_vertex(vs, l - 1, 2 * i + 1);
+            float ss, tt, dist, cvw;
+            if (y.prim != NO_INDEX && y.connectible && p.view.project(y.point, ss, tt, dist, cvw)) {
+                V3 w_yc = (p.view.pos - y.point) / dist;
+                const DevMaterial& ym = s.materials[y.material];
+                V3 F = l == 1 ? light_world(ym, w_yc, y.frame) : f_world(ym, y.incoming, w_yc, y.frame, false);
+                float g = fabsf(dot(y.frame.normal, w_yc)) / (p.view.area * cvw * cvw * cvw * dist * dist);
+                V3 L = mul(y.tp, F) * g;
+                if (!nearly_zero(L)) {
+                    float w;
+                    if (!p.mis) {
+                        w = 1.0f / static_cast<float>(l + 1);
+                    } else {
+                        float y_rev = to_area(p.view.dir_pdf(cvw), p.view.pos, y.point, y.frame.geom_normal);
+                        float ym_rev = 0.0f;
+                        if (l >= 2) {
+                            VPos yp = load_pos(vs, l - 2, 2 * i + 1);
+                            ym_rev = to_area(pdf_world(ym, w_yc, y.incoming, y.frame), y.point, yp.point, yp.ng);
+                        }
+                        w = mis_weight(cp, lp, 0, l, 0.0f, 0.0f, y_rev, ym_rev, true);
+                    }
+                    L = L * w;
+                    uint32_t col = min(p.width - 1, static_cast<uint32_t>(floorf(0.5f * (ss + 1.0f) * p.width)));
+                    uint32_t row = min(p.height - 1, static_cast<uint32_t>(floorf(0.5f * (tt + 1.0f) * p.height)));
+                    pix = row * p.width + col;
+                    out = make_float4(L.x, L.y, L.z, E_PENDING);
+                    uint32_t sq = agg_inc(counters + CNT_SHADOWQ);
+                    shadow_q[sq] = make_uint4(static_cast<uint32_t>(e), (l - 1) * VREC * p.nslots + 2 * i + 1, 0, 1);
+                }
+            }
+        }
+        lt[e] = out;
+        lt_pixel[e] = pix;
+    }
 }
 
+// Shadow query entries: (entry, float4 index of vertex a's point, of vertex b's point,
+// kind).  Kind 0 connects two walk vertices (their strategy entry); kind 1 connects the
+// camera to vertex a (a light-tracing entry in lt).
 template <int W>
 __global__ void __launch_bounds__(BLOCK) k_bdpt_shadow(DeviceScene s, const uint32_t* __restrict__ count,
                                                        const uint4* __restrict__ shadow_q, const float4* __restrict__ v0,
-                                                       float4* __restrict__ entries, int* err,
-                                                       unsigned long long* shadow_rays) {
+                                                       float4* __restrict__ entries, float4* __restrict__ lt,
+                                                       float3 cam, int* err, unsigned long long* shadow_rays) {
     extern __shared__ unsigned char smem[];
     int32_t* sref = reinterpret_cast<int32_t*>(smem);
     float* stt = reinterpret_cast<float*>(smem + sizeof(int32_t) * s.stack_depth * blockDim.x);
@@ -325,8 +557,16 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_shadow(DeviceScene s, const uint
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(shadow_rays, static_cast<unsigned long long>(n));
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         uint4 e = shadow_q[q];
-        float4 a4 = v0[e.y], b4 = v0[e.z];
-        V3 a = V3{a4.x, a4.y, a4.z}, b = V3{b4.x, b4.y, b4.z};
+        V3 a, b;
+        if (e.w == 1) {  // Bvh::visibility(camera, y), as the oracle's light-tracing test
+            float4 y4 = v0[e.y];
+            a = V3{cam.x, cam.y, cam.z};
+            b = V3{y4.x, y4.y, y4.z};
+        } else {
+            float4 a4 = v0[e.y], b4 = v0[e.z];
+            a = V3{a4.x, a4.y, a4.z};
+            b = V3{b4.x, b4.y, b4.z};
+        }
         bool visible;
         if (fabsf(a.x - b.x) < 1e-3f && fabsf(a.y - b.y) < 1e-3f && fabsf(a.z - b.z) < 1e-3f) {
             visible = false;
@@ -338,16 +578,20 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_shadow(DeviceScene s, const uint
                                                blockDim.x, err);
             visible = r.k < 0;
         }
-        entries[e.x].w = visible ? E_VISIBLE : E_OCCLUDED;
+        (e.w == 1 ? lt : entries)[e.x].w = visible ? E_VISIBLE : E_OCCLUDED;
     }
 }
 
+// Sums each path's weighted strategy terms in loop order; adds visible light-tracing
+// terms to `splat` (atomics; null: dropped, as for per-path sample output).
 __global__ void __launch_bounds__(BLOCK) k_bdpt_gather(DeviceScene s, BdptParams p,
                                                        const uint32_t* __restrict__ vcount,
                                                        const uint32_t* __restrict__ flags,
                                                        const float4* __restrict__ escape,
                                                        const uint32_t* __restrict__ entry_base,
-                                                       const float4* __restrict__ entries, float4* __restrict__ L_out) {
+                                                       const float4* __restrict__ entries, float4* __restrict__ L_out,
+                                                       const float4* __restrict__ lt,
+                                                       const uint32_t* __restrict__ lt_pixel, float4* splat) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     uint32_t fl = flags[i];
@@ -364,8 +608,19 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_gather(DeviceScene s, BdptParams
                 if (c + l > p.max_len) continue;
                 float4 e = entries[j++];
                 V3 term = (e.w == E_NO_TEST || e.w == E_VISIBLE) ? V3{e.x, e.y, e.z} : v3zero();
-                float w = 1.0f / static_cast<float>(c + l);
-                light = light + (term * w);
+                light = light + term;  // weighted in k_bdpt_connect
+            }
+        }
+        if (p.lt && splat) {
+            const uint32_t lmax = min(ls, p.max_len);
+            for (uint32_t l = 1; l <= lmax; ++l) {
+                size_t e = static_cast<size_t>(i) * p.max_len + (l - 1);
+                float4 v = lt[e];
+                if (v.w != E_VISIBLE) continue;
+                float* d = reinterpret_cast<float*>(splat + lt_pixel[e]);
+                atomicAdd(d, v.x);
+                atomicAdd(d + 1, v.y);
+                atomicAdd(d + 2, v.z);
             }
         }
     }
@@ -387,12 +642,13 @@ uint32_t max_pairs(uint32_t max_len) { return max_len * (max_len + 1) / 2; }
 
 template <int W>
 gr_status shadow_launch(const DeviceScene& s, uint32_t cap, const uint32_t* count, const uint4* q, const float4* v0,
-                        float4* entries, int* err, unsigned long long* shadow_rays, cudaStream_t st) {
+                        float4* entries, float4* lt, float3 cam, int* err, unsigned long long* shadow_rays,
+                        cudaStream_t st) {
     size_t smem = stack_smem_bytes(s.stack_depth, BLOCK);
     GR_CUDA_TRY(
         cudaFuncSetAttribute(k_bdpt_shadow<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int grid = resident_grid(k_bdpt_shadow<W>, smem, cap);
-    k_bdpt_shadow<W><<<grid, BLOCK, smem, st>>>(s, count, q, v0, entries, err, shadow_rays);
+    k_bdpt_shadow<W><<<grid, BLOCK, smem, st>>>(s, count, q, v0, entries, lt, cam, err, shadow_rays);
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }
@@ -419,16 +675,15 @@ cudaError_t BdptState::ensure(size_t paths, uint32_t max_len) {
     if ((e = escape.ensure(paths * sizeof(float4))) != cudaSuccess) return e;
     if ((e = entry_base.ensure(paths * sizeof(uint32_t))) != cudaSuccess) return e;
     if ((e = entries.ensure(pairs * sizeof(float4))) != cudaSuccess) return e;
-    if ((e = shadow.ensure(pairs * sizeof(uint4))) != cudaSuccess) return e;
+    const size_t lt_n = paths * max_len;  // light-tracing terms
+    if ((e = shadow.ensure((pairs + lt_n) * sizeof(uint4))) != cudaSuccess) return e;
+    if ((e = lt.ensure(lt_n * sizeof(float4))) != cudaSuccess) return e;
+    if ((e = lt_pixel.ensure(lt_n * sizeof(uint32_t))) != cudaSuccess) return e;
     return cudaSuccess;
 }
 
 gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     const gr_render_params& rp = job.params;
-    if (rp.mis || rp.light_tracing) {
-        set_error("BDPT: only the reference's uniform strategy weights are implemented (mis = 0, light_tracing = 0)");
-        return GR_ERR_UNSUPPORTED;
-    }
     const uint32_t npix = job.width * job.height;
     const uint32_t total = job.samples_out ? 1u : rp.spp;
     if (total == 0) return GR_OK;
@@ -454,6 +709,17 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     p.seed = rp.seed;
     p.max_len = max_len;
     p.rr_len = rp.rr_depth;
+    p.mis = rp.mis ? 1u : 0u;
+    p.lt = rp.light_tracing ? 1u : 0u;
+    {  // the camera seen from the scene (rotation rows and translation of the camera matrix)
+        const DevCamera& c = job.camera;
+        p.view.pos = V3{c.m[3][0] / c.m[3][3], c.m[3][1] / c.m[3][3], c.m[3][2] / c.m[3][3]};
+        for (int k = 0; k < 3; ++k) p.view.axis[k] = V3{c.m[k][0], c.m[k][1], c.m[k][2]};
+        p.view.wx = c.wx;
+        p.view.wy = c.wy;
+        p.view.area = 4.0f * c.wx * c.wy;
+    }
+    const float3 cam_pos = make_float3(p.view.pos.x, p.view.pos.y, p.view.pos.z);
     for (uint32_t done = 0; done < total; done += group) {
         uint32_t g = std::min(group, total - done);
         p.n = g * npix;
@@ -490,22 +756,23 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         }
         k_bdpt_connect<<<(p.n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(
             job.scene, p, vs, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), cnt, bs.entry_base.as<uint32_t>(),
-            bs.entries.as<float4>(), bs.shadow.as<uint4>());
+            bs.entries.as<float4>(), bs.shadow.as<uint4>(), bs.lt.as<float4>(), bs.lt_pixel.as<uint32_t>());
         GR_CUDA_TRY(cudaGetLastError());
-        uint32_t cap = p.n * max_pairs(max_len);
+        uint32_t cap = p.n * (max_pairs(max_len) + (p.lt ? max_len : 0u));
         gr_status s2;
         switch (job.scene.width) {
             case 2: s2 = shadow_launch<2>(job.scene, cap, cnt + CNT_SHADOWQ, bs.shadow.as<uint4>(),
-                                          bs.verts.as<float4>(), bs.entries.as<float4>(), err, shadow, st); break;
+                                          bs.verts.as<float4>(), bs.entries.as<float4>(), bs.lt.as<float4>(), cam_pos, err, shadow, st); break;
             case 4: s2 = shadow_launch<4>(job.scene, cap, cnt + CNT_SHADOWQ, bs.shadow.as<uint4>(),
-                                          bs.verts.as<float4>(), bs.entries.as<float4>(), err, shadow, st); break;
+                                          bs.verts.as<float4>(), bs.entries.as<float4>(), bs.lt.as<float4>(), cam_pos, err, shadow, st); break;
             default: s2 = shadow_launch<8>(job.scene, cap, cnt + CNT_SHADOWQ, bs.shadow.as<uint4>(),
-                                           bs.verts.as<float4>(), bs.entries.as<float4>(), err, shadow, st); break;
+                                           bs.verts.as<float4>(), bs.entries.as<float4>(), bs.lt.as<float4>(), cam_pos, err, shadow, st); break;
         }
         if (s2 != GR_OK) return s2;
         k_bdpt_gather<<<(p.n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(
             job.scene, p, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), bs.escape.as<float4>(),
-            bs.entry_base.as<uint32_t>(), bs.entries.as<float4>(), ps.light.as<float4>());
+            bs.entry_base.as<uint32_t>(), bs.entries.as<float4>(), ps.light.as<float4>(), bs.lt.as<float4>(),
+            bs.lt_pixel.as<uint32_t>(), job.splat);
         GR_CUDA_TRY(cudaGetLastError());
         launches += 3;
         if (job.film) {

@@ -22,18 +22,31 @@ __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_film_gather(const floa
     if (inside) film[static_cast<size_t>(y) * width + x] = acc;
 }
 
-__global__ void k_resolve(const float4* __restrict__ film, uint32_t n, float* rgb) {
+// accum / weight, plus splat * scale (light-tracing extension) when splat is not null.
+GR_D V3 resolved(const float4* __restrict__ film, const float4* __restrict__ splat, float scale, size_t i) {
+    float4 p = film[i];
+    V3 v = V3{p.x / p.w, p.y / p.w, p.z / p.w};
+    if (splat) {
+        float4 q = splat[i];
+        v = v + V3{q.x, q.y, q.z} * scale;
+    }
+    return v;
+}
+
+__global__ void k_resolve(const float4* __restrict__ film, const float4* __restrict__ splat, float scale, uint32_t n,
+                          float* rgb) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float4 p = film[i];
-    rgb[3 * i] = p.x / p.w;
-    rgb[3 * i + 1] = p.y / p.w;
-    rgb[3 * i + 2] = p.z / p.w;
+    V3 v = resolved(film, splat, scale, i);
+    rgb[3 * i] = v.x;
+    rgb[3 * i + 1] = v.y;
+    rgb[3 * i + 2] = v.z;
 }
 
 // ExrWriter::write_channels (render/exr.rs:138-166): per scanline y, the int32 line
 // number, the uint32 byte count and the B, G, R planes of film row height - y - 1.
-__global__ void k_exr_pack(const float4* __restrict__ film, uint32_t width, uint32_t height, unsigned char* out) {
+__global__ void k_exr_pack(const float4* __restrict__ film, const float4* __restrict__ splat, float scale,
+                           uint32_t width, uint32_t height, unsigned char* out) {
     uint32_t y = blockIdx.y;
     size_t line = 8 + static_cast<size_t>(width) * 12;
     unsigned char* l = out + y * line;
@@ -45,8 +58,8 @@ __global__ void k_exr_pack(const float4* __restrict__ film, uint32_t width, uint
     }
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= width) return;
-    float4 p = film[static_cast<size_t>(height - y - 1) * width + i];
-    float v[3] = {p.x / p.w, p.y / p.w, p.z / p.w};
+    V3 r = resolved(film, splat, scale, static_cast<size_t>(height - y - 1) * width + i);
+    float v[3] = {r.x, r.y, r.z};
     float* planes = reinterpret_cast<float*>(l + 8);  // 8 + 12 * width keeps 4-byte alignment
     planes[i] = v[2];
     planes[width + i] = v[1];
@@ -63,16 +76,17 @@ gr_status film_gather(const float2* st, const float4* color, uint32_t width, uin
     return GR_OK;
 }
 
-gr_status film_resolve(const float4* film, uint32_t n, float* rgb, cudaStream_t s) {
-    k_resolve<<<(n + 255) / 256, 256, 0, s>>>(film, n, rgb);
+gr_status film_resolve(const float4* film, const float4* splat, float splat_scale, uint32_t n, float* rgb,
+                       cudaStream_t s) {
+    k_resolve<<<(n + 255) / 256, 256, 0, s>>>(film, splat, splat_scale, n, rgb);
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }
 
-gr_status film_exr_pack(const float4* film, uint32_t width, uint32_t height, unsigned char* out, size_t,
-                        cudaStream_t s) {
+gr_status film_exr_pack(const float4* film, const float4* splat, float splat_scale, uint32_t width, uint32_t height,
+                        unsigned char* out, size_t, cudaStream_t s) {
     dim3 grid((width + 127) / 128, height);
-    k_exr_pack<<<grid, 128, 0, s>>>(film, width, height, out);
+    k_exr_pack<<<grid, 128, 0, s>>>(film, splat, splat_scale, width, height, out);
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }

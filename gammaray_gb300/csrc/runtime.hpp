@@ -64,7 +64,7 @@ struct PathState {
 // demand).  Walks are addressed by slot (2 per path: camera, light).
 struct BdptState {
     DevBuf q_slot[2], q_o[2], q_d[2], q_hit, tp, key, st, light;
-    DevBuf verts, vcount, flags, escape, entry_base, entries, shadow;
+    DevBuf verts, vcount, flags, escape, entry_base, entries, shadow, lt, lt_pixel;
     cudaError_t ensure(size_t paths, uint32_t max_len);
 };
 
@@ -109,6 +109,7 @@ struct gr_scene {
 struct gr_film {
     uint32_t width = 0, height = 0;
     gr::DevBuf pixels;  // float4 (accum.rgb, weight) per pixel
+    gr::DevBuf splat;   // float4 light-tracing splat sums (BDPT extension); allocated on first use
     uint32_t passes = 0;
     int device = 0;
 };
@@ -132,6 +133,7 @@ struct RenderJob {
     gr_render_params params;
     uint32_t width, height;
     float4* film;  // accumulate target, or null (samples only)
+    float4* splat = nullptr;  // light-tracing splat target (BDPT extension), or null
     float* samples_out;  // device (s, t, r, g, b) per pixel for gr_render_samples, or null
 };
 
@@ -139,9 +141,11 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st);
 gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st);
 gr_status film_gather(const float2* st_buf, const float4* color, uint32_t width, uint32_t height, uint32_t passes,
                       float4* film, cudaStream_t s);
-gr_status film_resolve(const float4* film, uint32_t n, float* rgb, cudaStream_t s);
-gr_status film_exr_pack(const float4* film, uint32_t width, uint32_t height, unsigned char* out, size_t data_offset,
-                        cudaStream_t s);
+// Resolve and EXR packing add splat * splat_scale when splat is not null.
+gr_status film_resolve(const float4* film, const float4* splat, float splat_scale, uint32_t n, float* rgb,
+                       cudaStream_t s);
+gr_status film_exr_pack(const float4* film, const float4* splat, float splat_scale, uint32_t width, uint32_t height,
+                        unsigned char* out, size_t data_offset, cudaStream_t s);
 
 int device_sm_count();
 

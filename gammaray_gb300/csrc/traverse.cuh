@@ -250,78 +250,89 @@ struct StackView {
     }
 };
 
-// One traversal step.  Returns true when the ray is finished (t.hit / t.closest hold
-// the closest hit).  With ANY_HIT it finishes at the first hit closer than t_max.
-template <int W, bool ANY_HIT, bool COUNT>
-GR_D bool trav_step(const DeviceScene& s, TravState& t, const StackView& stk, int* err, uint32_t* counts) {
+// Tests one wide node against the ray: pushes the far hit children (sorted by entry
+// distance, nearest last) and makes the nearest hit child the current reference.
+// Returns false when no child is hit.  A push beyond MAX_STACK sets *err = 1 and
+// `overflow`.
+template <int W, bool COUNT>
+GR_D bool visit_node(const DeviceScene& s, TravState& t, const StackView& stk, int* err, uint32_t* counts,
+                     bool& overflow) {
     const float inflate = 1.0f + 2.0f * gamma_n(3.0f);
-    if (t.ref >= 0) {
-        if (COUNT) counts[0] += 1;
-        const float4* nb = s.nodes + static_cast<size_t>(t.ref) * (2 * W);
-        float f[8 * W];
+    if (COUNT) counts[0] += 1;
+    const float4* nb = s.nodes + static_cast<size_t>(t.ref) * (2 * W);
+    float f[8 * W];
 #pragma unroll
-        for (int q = 0; q < 2 * W; ++q) {
-            float4 x = __ldg(nb + q);
-            f[4 * q] = x.x;
-            f[4 * q + 1] = x.y;
-            f[4 * q + 2] = x.z;
-            f[4 * q + 3] = x.w;
-        }
-        uint32_t key[W];
-        int h = 0;
+    for (int q = 0; q < 2 * W; ++q) {
+        float4 x = __ldg(nb + q);
+        f[4 * q] = x.x;
+        f[4 * q + 1] = x.y;
+        f[4 * q + 2] = x.z;
+        f[4 * q + 3] = x.w;
+    }
+    uint32_t key[W];
+    int h = 0;
 #pragma unroll
-        for (int j = 0; j < W; ++j) {
-            float lx = f[0 * W + j], ly = f[1 * W + j], lz = f[2 * W + j];
-            float hx = f[3 * W + j], hy = f[4 * W + j], hz = f[5 * W + j];
-            float t0x = ((t.nx ? hx : lx) - t.o.x) * t.inv.x;
-            float t1x = ((t.nx ? lx : hx) - t.o.x) * t.inv.x;
-            float t0y = ((t.ny ? hy : ly) - t.o.y) * t.inv.y;
-            float t1y = ((t.ny ? ly : hy) - t.o.y) * t.inv.y;
-            float t0z = ((t.nz ? hz : lz) - t.o.z) * t.inv.z;
-            float t1z = ((t.nz ? lz : hz) - t.o.z) * t.inv.z;
-            float tmin = fmaxf(fmaxf(t0x, t0y), t0z);
-            float tmax = fminf(fminf(t1x, t1y), t1z) * inflate;
-            bool hit = tmin <= tmax && tmin < t.closest && tmax > 0.0f;
-            float te = fmaxf(tmin, 0.0f);
-            key[j] = hit ? ((__float_as_uint(te) & ~7u) | static_cast<uint32_t>(j)) : 0xFFFFFFFFu;
-            h += hit ? 1 : 0;
-        }
-        if (h > 0) {
-            sort_keys<W>(key);
-            if (t.sp + h - 1 > MAX_STACK) {
-                *err = 1;
-                t.hit = -1;
-                return true;
-            }
+    for (int j = 0; j < W; ++j) {
+        float lx = f[0 * W + j], ly = f[1 * W + j], lz = f[2 * W + j];
+        float hx = f[3 * W + j], hy = f[4 * W + j], hz = f[5 * W + j];
+        float t0x = ((t.nx ? hx : lx) - t.o.x) * t.inv.x;
+        float t1x = ((t.nx ? lx : hx) - t.o.x) * t.inv.x;
+        float t0y = ((t.ny ? hy : ly) - t.o.y) * t.inv.y;
+        float t1y = ((t.ny ? ly : hy) - t.o.y) * t.inv.y;
+        float t0z = ((t.nz ? hz : lz) - t.o.z) * t.inv.z;
+        float t1z = ((t.nz ? lz : hz) - t.o.z) * t.inv.z;
+        float tmin = fmaxf(fmaxf(t0x, t0y), t0z);
+        float tmax = fminf(fminf(t1x, t1y), t1z) * inflate;
+        bool hit = tmin <= tmax && tmin < t.closest && tmax > 0.0f;
+        float te = fmaxf(tmin, 0.0f);
+        key[j] = hit ? ((__float_as_uint(te) & ~7u) | static_cast<uint32_t>(j)) : 0xFFFFFFFFu;
+        h += hit ? 1 : 0;
+    }
+    if (h == 0) return false;
+    sort_keys<W>(key);
+    if (t.sp + h - 1 > MAX_STACK) {
+        *err = 1;
+        overflow = true;
+        return false;
+    }
 #pragma unroll
-            for (int j = W - 1; j >= 1; --j) {
-                if (j < h) {
-                    stk.push(t.sp, select_child<W>(f, key[j] & 7u), __uint_as_float(key[j] & ~7u));
-                    ++t.sp;
-                }
-            }
-            t.ref = select_child<W>(f, key[0] & 7u);
-            return false;
-        }
-    } else {
-        uint32_t enc = ~static_cast<uint32_t>(t.ref);
-        uint32_t first = enc >> LEAF_COUNT_BITS;
-        uint32_t count = (enc & (MAX_LEAF_PRIMS - 1)) + 1;
-        if (COUNT) counts[1] += count;
-        for (uint32_t k = first; k < first + count; ++k) {
-            const float4* pr = s.prims + 3 * static_cast<size_t>(k);
-            float4 p0 = __ldg(pr), p1 = __ldg(pr + 1), p2 = __ldg(pr + 2);
-            float u, v;
-            float dist = intersect_prim(p0, p1, p2, t.o, t.d, u, v);
-            if (dist != 0.0f && dist < t.closest) {
-                t.closest = dist;
-                t.hit = static_cast<int32_t>(k);
-                t.hu = u;
-                t.hv = v;
-                if (ANY_HIT) return true;
-            }
+    for (int j = W - 1; j >= 1; --j) {
+        if (j < h) {
+            stk.push(t.sp, select_child<W>(f, key[j] & 7u), __uint_as_float(key[j] & ~7u));
+            ++t.sp;
         }
     }
+    t.ref = select_child<W>(f, key[0] & 7u);
+    return true;
+}
+
+// Intersects the primitives of leaf `ref`, keeping the closest hit in t.  With ANY_HIT
+// it returns true at the first hit closer than t.closest.
+template <bool ANY_HIT, bool COUNT>
+GR_D bool visit_leaf(const DeviceScene& s, TravState& t, int32_t ref, uint32_t* counts) {
+    uint32_t enc = ~static_cast<uint32_t>(ref);
+    uint32_t first = enc >> LEAF_COUNT_BITS;
+    uint32_t count = (enc & (MAX_LEAF_PRIMS - 1)) + 1;
+    if (COUNT) counts[1] += count;
+    for (uint32_t k = first; k < first + count; ++k) {
+        const float4* pr = s.prims + 3 * static_cast<size_t>(k);
+        float4 p0 = __ldg(pr), p1 = __ldg(pr + 1), p2 = __ldg(pr + 2);
+        float u, v;
+        float dist = intersect_prim(p0, p1, p2, t.o, t.d, u, v);
+        if (dist != 0.0f && dist < t.closest) {
+            t.closest = dist;
+            t.hit = static_cast<int32_t>(k);
+            t.hu = u;
+            t.hv = v;
+            if (ANY_HIT) return true;
+        }
+    }
+    return false;
+}
+
+// Pops the next stacked child that can still hold a closer hit into t.ref.  Returns
+// false when the stack is exhausted.
+GR_D bool pop_next(TravState& t, const StackView& stk) {
     while (t.sp > 0) {
         --t.sp;
         int32_t r;
@@ -329,10 +340,28 @@ GR_D bool trav_step(const DeviceScene& s, TravState& t, const StackView& stk, in
         stk.pop(t.sp, r, te);
         if (te < t.closest) {
             t.ref = r;
-            return false;
+            return true;
         }
     }
-    return true;
+    return false;
+}
+
+// One traversal step.  Returns true when the ray is finished (t.hit / t.closest hold
+// the closest hit).  With ANY_HIT it finishes at the first hit closer than t_max.
+template <int W, bool ANY_HIT, bool COUNT>
+GR_D bool trav_step(const DeviceScene& s, TravState& t, const StackView& stk, int* err, uint32_t* counts) {
+    if (t.ref >= 0) {
+        bool overflow = false;
+        bool descended = visit_node<W, COUNT>(s, t, stk, err, counts, overflow);
+        if (overflow) {
+            t.hit = -1;
+            return true;
+        }
+        if (descended) return false;
+    } else if (visit_leaf<ANY_HIT, COUNT>(s, t, t.ref, counts)) {
+        return true;
+    }
+    return !pop_next(t, stk);
 }
 
 inline size_t step_stack_smem_bytes(int threads) {

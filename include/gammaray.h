@@ -180,13 +180,19 @@ gr_status gr_film_clear(gr_film* film);
 /* Copies Film::pixels out: accum as 3 floats and weight as 1 float per pixel,
  * row-major, row 0 first (render/film.rs:26-36). */
 gr_status gr_film_read(const gr_film* film, float* accum, float* weight);
-/* accum / weight per pixel (render/exr.rs:154-156), 3 floats per pixel. */
+/* accum / weight per pixel (render/exr.rs:154-156), 3 floats per pixel, plus
+ * splat / passes when the film holds light-tracing splats. */
 gr_status gr_film_resolve(const gr_film* film, float* rgb);
 /* Uncompressed scanline EXR with B, G, R float channels, rows flipped, as
  * ExrWriter::update + write (render/exr.rs:168-199). */
 gr_status gr_film_write_exr(const gr_film* film, const char* path);
 /* Number of passes accumulated so far. */
 gr_status gr_film_passes(const gr_film* film, uint32_t* passes);
+/* The light-tracing splat sums (3 floats per pixel, zero unless a BDPT render with
+ * light_tracing = 1 wrote into the film).  No counterpart in the reference, whose film
+ * has no splat buffer (its BDPT has no light-tracing strategy); it follows PBRT 3e's
+ * Film::AddSplat.  gr_film_resolve and gr_film_write_exr add splat / passes. */
+gr_status gr_film_read_splat(const gr_film* film, float* splat);
 
 /* --------------------------------------------------------------------- render */
 
@@ -209,10 +215,16 @@ typedef struct gr_render_params {
     uint32_t rr_depth;
     /* Path tracer: aggressive roulette when depth > rr_aggressive_depth (20). */
     uint32_t rr_aggressive_depth;
-    /* BDPT strategy weights: 0 = uniform 1/(c+l) (reference, integrators.rs:345-354),
-     * 1 = power heuristic over the stored forward/reverse densities (extension). */
+    /* BDPT strategy weights (extension; the reference has 0):
+     *   0 = uniform 1/(c+l) (integrators.rs:345-354), 1/(c+l+1) with light_tracing;
+     *   1 = power heuristic over all strategies of a path (Veach 1997 eq. 10.9, in the
+     *       ratio form of PBRT 3e section 16.3.4), from area-measure forward / reverse
+     *       pdfs per vertex. */
     uint32_t mis;
-    /* BDPT: 1 adds light-tracing (t=1) connections splatted onto the film (extension). */
+    /* BDPT: 1 adds the light-tracing strategy (extension; PBRT's t = 1): every light-walk
+     * vertex that projects into the image is connected to the pinhole camera, tested for
+     * visibility and splatted with atomics into the film's splat buffer
+     * (gr_film_read_splat); resolve and EXR add splat / passes. */
     uint32_t light_tracing;
     uint32_t first_pass; /* pass index of the first pass (selects the random streams) */
     uint64_t seed;

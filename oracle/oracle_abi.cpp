@@ -123,7 +123,10 @@ struct gr_scene {
 struct gr_film {
     uint32_t width = 0, height = 0;
     std::vector<FilmPixel> pixels;
+    std::vector<Vec> splat;  // light-tracing splat sums (BDPT extension); empty until used
     uint32_t passes = 0;
+    bool has_splat() const { return !splat.empty(); }
+    float splat_scale() const { return passes ? 1.0f / static_cast<float>(passes) : 0.0f; }
 };
 
 extern "C" {
@@ -284,6 +287,7 @@ gr_status gr_film_destroy(gr_film* f) {
 gr_status gr_film_clear(gr_film* f) {
     if (!f) return fail(GR_ERR_INVALID_ARGUMENT, "null film");
     std::fill(f->pixels.begin(), f->pixels.end(), FilmPixel{Vec::zero(), 0.0f});
+    f->splat.clear();
     f->passes = 0;
     return GR_OK;
 }
@@ -295,14 +299,24 @@ gr_status gr_film_read(const gr_film* f, float* accum, float* weight) {
     }
     return GR_OK;
 }
+gr_status gr_film_read_splat(const gr_film* f, float* splat) {
+    if (!f || !splat) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
+    for (size_t i = 0; i < f->pixels.size(); ++i) put3(splat + 3 * i, f->has_splat() ? f->splat[i] : Vec::zero());
+    return GR_OK;
+}
 gr_status gr_film_resolve(const gr_film* f, float* rgb) {
     if (!f || !rgb) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
-    for (size_t i = 0; i < f->pixels.size(); ++i) put3(rgb + 3 * i, f->pixels[i].accum / f->pixels[i].weight);
+    for (size_t i = 0; i < f->pixels.size(); ++i) {
+        Vec v = f->pixels[i].accum / f->pixels[i].weight;
+        if (f->has_splat()) v = v + f->splat[i] * f->splat_scale();
+        put3(rgb + 3 * i, v);
+    }
     return GR_OK;
 }
 gr_status gr_film_write_exr(const gr_film* f, const char* path) {
     if (!f || !path) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
-    std::vector<unsigned char> b = exr_bytes(f->width, f->height, f->pixels);
+    std::vector<unsigned char> b =
+        exr_bytes(f->width, f->height, f->pixels, f->has_splat() ? &f->splat : nullptr, f->splat_scale());
     std::ofstream os(path, std::ios::binary);
     if (!os) return fail(GR_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
     os.write(reinterpret_cast<const char*>(b.data()), static_cast<std::streamsize>(b.size()));
@@ -317,8 +331,8 @@ gr_status gr_film_passes(const gr_film* f, uint32_t* p) {
 static gr_status check_params(const gr_render_params* p) {
     if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "null params");
     if (p->integrator < 0 || p->integrator > 2) return fail(GR_ERR_INVALID_ARGUMENT, "unknown integrator");
-    if (p->integrator == GR_INTEGRATOR_BDPT && (p->mis != 0 || p->light_tracing != 0))
-        return fail(GR_ERR_UNSUPPORTED, "the restatement implements the reference's uniform BDPT weights only");
+    if (p->integrator != GR_INTEGRATOR_BDPT && (p->mis != 0 || p->light_tracing != 0))
+        return fail(GR_ERR_INVALID_ARGUMENT, "mis and light_tracing apply to the BDPT integrator only");
     if (p->integrator == GR_INTEGRATOR_BDPT && p->max_depth > 16)
         return fail(GR_ERR_INVALID_ARGUMENT, "BDPT max_depth must be <= 16");
     return GR_OK;
@@ -329,16 +343,22 @@ static Camera make_camera(const gr_camera* c) {
                   Vec(c->rotate[1], c->rotate[2], c->rotate[3]), v3(c->translate));
 }
 
-// One Stage::trace pass (render/stage.rs:23-36) without the splat.
+// One Stage::trace pass (render/stage.rs:23-36) without the splat.  With the
+// light-tracing extension, `splats` receives each sample's light-tracing splats, in
+// sample order.
 static void trace_pass(const gr_scene* s, const Camera& cam, const gr_render_params* p, uint32_t w, uint32_t h,
-                       uint32_t pass, std::vector<FilmSample>& samples) {
+                       uint32_t pass, std::vector<FilmSample>& samples, std::vector<Splat>* splats = nullptr) {
     RenderSettings rs;
     rs.integrator = p->integrator;
     rs.max_depth = p->max_depth;
     rs.rr_depth = p->rr_depth;
     rs.rr_aggressive_depth = p->rr_aggressive_depth;
     rs.seed = p->seed;
+    rs.mis = p->mis != 0;
+    rs.light_tracing = p->light_tracing != 0;
+    const PinholeView view = PinholeView::of(cam);
     samples.assign(static_cast<size_t>(w) * h, FilmSample{Vec::zero(), 0.0f, 0.0f});
+    std::vector<std::vector<Splat>> per_sample(rs.light_tracing && splats ? samples.size() : 0);
     parallel_for(samples.size(), [&](size_t i) {
         thread_local std::vector<BdptVertex> cs, ls;
         uint32_t row = static_cast<uint32_t>(i / w), col = static_cast<uint32_t>(i % w);
@@ -347,9 +367,15 @@ static void trace_pass(const gr_scene* s, const Camera& cam, const gr_render_par
         sample_point(w, h, row, col, key, fs.s, fs.t);
         Ray ray = cam.compute_ray(fs.s, fs.t);
         if (p->integrator == GR_INTEGRATOR_PATH_TRACER) fs.color = integrate_pt(s->sc, ray, key, rs);
-        else if (p->integrator == GR_INTEGRATOR_BDPT) fs.color = integrate_bdpt(s->sc, ray, key, rs, cs, ls);
+        else if (p->integrator == GR_INTEGRATOR_BDPT)
+            fs.color = integrate_bdpt(s->sc, ray, key, rs, cs, ls, &view, w, h,
+                                      per_sample.empty() ? nullptr : &per_sample[i]);
         else fs.color = integrate_display(s->sc, ray);
     });
+    if (splats) {
+        splats->clear();
+        for (auto& v : per_sample) splats->insert(splats->end(), v.begin(), v.end());
+    }
 }
 
 gr_status gr_render(gr_scene* s, const gr_camera* c, const gr_render_params* p, gr_film* f) {
@@ -358,10 +384,16 @@ gr_status gr_render(gr_scene* s, const gr_camera* c, const gr_render_params* p, 
     if (st != GR_OK) return st;
     Camera cam = make_camera(c);
     std::vector<FilmSample> samples;
+    std::vector<Splat> splats;
+    const bool lt = p->integrator == GR_INTEGRATOR_BDPT && p->light_tracing != 0;
     try {
         for (uint32_t k = 0; k < p->spp; ++k) {
-            trace_pass(s, cam, p, f->width, f->height, p->first_pass + k, samples);
+            trace_pass(s, cam, p, f->width, f->height, p->first_pass + k, samples, lt ? &splats : nullptr);
             report_samples(f->width, f->height, samples, f->pixels);
+            if (lt) {
+                if (f->splat.empty()) f->splat.assign(f->pixels.size(), Vec::zero());
+                for (const Splat& sp : splats) f->splat[sp.pixel] = f->splat[sp.pixel] + sp.value;
+            }
             f->passes += 1;
         }
     } catch (const StackOverflow& e) {

@@ -274,3 +274,69 @@ def test_bdpt_counts_shadow_rays(gpu):
     st.render(w.camera, g.BdptIntegrator(), f, 2)
     s = st.last_stats()
     assert s.samples == 2 * 32 * 32 and s.extension_rays > s.samples and s.shadow_rays > 0
+
+
+@pytest.mark.parametrize("lt", [0, 1])
+@pytest.mark.parametrize("scene", ["cornell", "displaced_env_spheres"])
+def test_bdpt_mis_samples_per_path(gpu, oracle, scene, lt):
+    # Power-heuristic weights per path against the oracle (the mirror sphere exercises
+    # the delta-vertex rules); light-tracing splats are not part of per-path samples.
+    if scene == "cornell":
+        w = scenes.cornell_spheres(40, 40, 1)
+        prims, env = w.prims, w.environment
+    else:
+        w = scenes.displaced_sphere(40, 40, 1, bdpt=True, tris=20_000)
+        prims = w.prims + [g.Sphere(g.Material.diffuse_light((3, 3, 3)), g.Mat.translation((1.5, 1.0, 0)), 0.3),
+                           g.Sphere(g.Material.mirror(), g.Mat.translation((-1.5, -0.6, 0.5)), 0.5)]
+        env = w.environment
+    integ = g.BdptIntegrator(max_depth=10, mis=1, light_tracing=lt)
+    sg = g.Stage(prims, lib=gpu, environment=env, seed=23)
+    so = g.Stage(prims, lib=oracle, environment=env, seed=23)
+    a = sg.samples(w.camera, integ, 40, 40, 3)
+    b = so.samples(w.camera, integ, 40, 40, 3)
+    np.testing.assert_array_equal(a[..., :2], b[..., :2])
+    close = np.isclose(a[..., 2:], b[..., 2:], rtol=1e-4, atol=1e-5).all(axis=-1)
+    assert close.mean() >= 0.99, f"{scene}: {close.mean():.4f} of paths agree"
+    assert np.isfinite(a[..., 2:]).all()
+
+
+def test_bdpt_light_tracing_film_parity(gpu, oracle):
+    # The same light-tracing terms on both sides; the GPU adds them with atomics, so only
+    # the order of the additions (and BSDF ulps) differs.
+    w = scenes.cornell_spheres(40, 40, 1)
+    out = []
+    for L in (gpu, oracle):
+        st = g.Stage(w.prims, lib=L, seed=5)
+        f = g.Film(40, 40, lib=L)
+        st.render(w.camera, g.BdptIntegrator(max_depth=10, mis=1, light_tracing=1), f, 2)
+        out.append((f.read(), f.read_splat(), f.resolve(), f.passes()))
+    (ga, gw), gs, gr, gp = out[0]
+    (oa, ow), os_, orr, op = out[1]
+    assert gp == op == 2
+    assert gs.sum() > 0
+    rel = lambda x, y: float(np.sqrt(np.mean((x - y) ** 2) / np.mean(y ** 2)))
+    assert rel(gs, os_) < 1e-3, rel(gs, os_)
+    assert rel(ga, oa) < 1e-3 and rel(gw, ow) < 1e-6
+    assert rel(gr, orr) < 1e-3
+
+
+def test_bdpt_mis_unbiased_against_pt(gpu):
+    # MIS + light tracing on the GPU converges to the path tracer's image away from the
+    # directly visible light and the image edge (see test_oracle.far_from_bright).
+    from test_oracle import far_from_bright
+
+    w = scenes.cornell_spheres(64, 64, 1)
+    st = g.Stage(w.prims, lib=gpu, seed=4)
+    fp, fb = g.Film(64, 64, lib=gpu), g.Film(64, 64, lib=gpu)
+    st.render(w.camera, g.PathTracerIntegrator(), fp, 4096)
+    st.render(w.camera, g.BdptIntegrator(mis=1, light_tracing=1), fb, 256)
+    pt, b = fp.resolve(), fb.resolve()
+    keep = far_from_bright(pt)
+    ref, got = float(pt[keep].mean()), float(b[keep].mean())
+    assert abs(got - ref) / ref < 0.01, (ref, got)
+    # 8x8-pixel block means agree to within the noise of both images
+    k = keep.reshape(8, 8, 8, 8).transpose(0, 2, 1, 3).reshape(64, 64).all(axis=1)
+    bp = pt.reshape(8, 8, 8, 8, 3).mean(axis=(1, 3)).reshape(64, 3)[k]
+    bb = b.reshape(8, 8, 8, 8, 3).mean(axis=(1, 3)).reshape(64, 3)[k]
+    assert len(bp) >= 8
+    assert float(np.mean((bb - bp) ** 2) / np.mean(bp ** 2)) < 2e-3

@@ -241,3 +241,51 @@ def test_invalid_inputs(oracle):
     m = g.Mesh(g.Material.disney().build(), None, np.zeros((3, 3), np.float32), np.array([[0, 1, 5]]))
     with pytest.raises(_abi.GrError):
         g.Stage([m], lib=oracle)
+
+
+def far_from_bright(img, border=4, reach=4):
+    """Pixels at least `reach` px from any bright pixel (> 2) and `border` px inside the
+    image.  Camera samples reach neighbours through the 2-px Mitchell filter and 2-px
+    jitter, light-tracing splats do not, so near a directly visible light or the image
+    edge the two strategies estimate differently filtered pixels."""
+    bright = img.max(axis=-1) > 2.0
+    near = bright.copy()
+    for _ in range(reach):
+        near = near | np.roll(near, 1, 0) | np.roll(near, -1, 0) | np.roll(near, 1, 1) | np.roll(near, -1, 1)
+    keep = ~near
+    keep[:border, :] = keep[-border:, :] = keep[:, :border] = keep[:, -border:] = False
+    return keep
+
+
+@pytest.mark.parametrize("lt", [0, 1])
+def test_bdpt_mis_agrees_with_pt(oracle, lt):
+    # Power-heuristic weights sum to one over the strategies that can produce a path, so
+    # the MIS estimate is unbiased (unlike the reference's uniform weights): away from
+    # the light and the image edge its mean matches a 1024-spp path tracer's.
+    w = scenes.cornell_spheres(48, 48, 1)
+    st = g.Stage(w.prims, lib=oracle, seed=2)
+    fp, fb = g.Film(48, 48, lib=oracle), g.Film(48, 48, lib=oracle)
+    st.render(w.camera, g.PathTracerIntegrator(), fp, 1024)
+    st.render(w.camera, g.BdptIntegrator(mis=1, light_tracing=lt), fb, 64)
+    pt, b = fp.resolve(), fb.resolve()
+    keep = far_from_bright(pt)
+    assert keep.sum() > 1000
+    ref, got = float(pt[keep].mean()), float(b[keep].mean())
+    assert np.isfinite(b).all() and abs(got - ref) / ref < 0.02, (ref, got)
+    splat = fb.read_splat()
+    if lt:
+        assert splat.sum() > 0
+        acc, wt = fb.read()
+        np.testing.assert_allclose(b, acc / wt[..., None] + splat / 64, rtol=1e-5, atol=1e-6)
+    else:
+        assert not splat.any()
+
+
+def test_reference_bdpt_has_no_splats(oracle):
+    w = scenes.cornell_spheres(16, 16, 1)
+    st = g.Stage(w.prims, lib=oracle, seed=3)
+    f = g.Film(16, 16, lib=oracle)
+    st.render(w.camera, g.BdptIntegrator(), f, 2)
+    acc, wt = f.read()
+    assert not f.read_splat().any()
+    np.testing.assert_array_equal(f.resolve(), (acc / wt[..., None]).astype(np.float32))
