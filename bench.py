@@ -29,6 +29,9 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# DRAM bytes per extension ray of k_extend, measured with ncu on a 4-spp render of the
+# bench workload (profiles/extend_pt_displaced_sphere_1024.md).
+EXTEND_DRAM_BYTES_PER_RAY = 46.4
 sys.path.insert(0, ROOT)
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -49,6 +52,7 @@ def parse():
     ap.add_argument("--leaf-size", type=int, default=0, help="primitives per wide leaf; 0 = library default")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-bdpt", action="store_true", help="skip the BDPT measurement")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=3.0, help="Poisson arrival rate (requests/s)")
     ap.add_argument("--profile-case", action="store_true",
@@ -390,17 +394,17 @@ def run_ours(args, rank, world, local):
                 "extend_share_of_device_time": ext_ms / total_ms if total_ms else None,
                 "shade_share_of_device_time": shade_ms / total_ms if total_ms else None,
                 "extend_ms_per_launch": ext_ms / max(1, ext_launch)}
-    ncu_traffic = os.path.join(ROOT, "profiles", "extend_traffic.json")
-    if os.path.exists(ncu_traffic):
-        try:
-            with open(ncu_traffic) as f:
-                tr = json.load(f)
-            roofline["traffic"] = tr.get("dram_bytes_per_ray", 0) * rays / max(1, ext_launch)
-            roofline["traffic_source"] = tr.get("source")
-        except Exception:
-            pass
+    # DRAM traffic of k_extend per ray, from one ncu capture (dram__bytes_read.sum +
+    # dram__bytes_write.sum over every extend launch of a 4-spp render of this workload,
+    # whose 4 M-ray queues exceed L2; profiles/extend_pt_displaced_sphere_1024.md),
+    # scaled to the average launch of the timed renders.
+    roofline["traffic"] = EXTEND_DRAM_BYTES_PER_RAY * rays / max(1, ext_launch)
+    roofline["traffic_source"] = ("ncu dram bytes of all extend launches of a 4-spp render "
+                                  f"({EXTEND_DRAM_BYTES_PER_RAY} B/ray) x rays per timed launch")
 
-    batched = served = None
+    batched = served = bdpt = None
+    if rank == 0 and not args.no_bdpt:
+        bdpt = run_bdpt(lib, min(args.cpu_seconds, 8.0))
     if rank == 0 and not args.no_batch:
         batched = run_batched(lib)
     if rank == 0 and not args.no_serve:
@@ -412,12 +416,55 @@ def run_ours(args, rank, world, local):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": config_of(w), "mrays_per_s": mrays, "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
                 "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s": wall,
-                "batched": batched, "served": served,
+                "batched": batched, "served": served, "bdpt": bdpt,
                 "scene": {"components": int(info.num_components), "wide_nodes": int(info.num_wide_nodes),
                           "device_bytes": int(info.device_bytes), "build_s": info.build_seconds}}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_bdpt(lib, cpu_seconds):
+    """Config 3: BDPT on the 102,400-triangle scene at 512x512, 16 spp, path length 10,
+    with power-heuristic MIS and light-tracing splats (and, beside it, the reference's
+    uniform weights).  Device time per render; rays = extension + shadow rays."""
+    import gammaray_gb300 as g
+    from gammaray_gb300 import _abi, scenes
+
+    w = scenes.displaced_sphere(512, 512, 16, bdpt=True)
+    st = g.Stage(w.prims, lib=lib, environment=w.environment, seed=3)
+    samples = w.width * w.height * w.spp
+    out = {"workload": "bdpt_displaced_sphere_102k", "width": w.width, "height": w.height, "spp": w.spp,
+           "max_path_length": 10}
+    forms = (("mis_light_tracing", g.BdptIntegrator(max_depth=10, rr_depth=4, mis=1, light_tracing=1)),
+             ("reference_weights", g.BdptIntegrator(max_depth=10, rr_depth=4)))
+    for name, integ in forms:
+        f = g.Film(w.width, w.height, lib=lib)
+        st.render(w.camera, integ, f, 2)  # warm
+        ms, s = [], None
+        for _ in range(3):
+            f.clear()
+            st.render(w.camera, integ, f, w.spp)
+            s = st.last_stats()
+            ms.append(s.device_ms)
+        t = statistics.median(ms)
+        out[name] = {"msamples_per_s": samples / (t * 1e-3) / 1e6,
+                     "mrays_per_s": (s.extension_rays + s.shadow_rays) / (t * 1e-3) / 1e6,
+                     "extension_rays": int(s.extension_rays), "shadow_rays": int(s.shadow_rays),
+                     "device_ms": t}
+        f.close()
+    # The oracle on the host cores, whole 1-spp passes of the same workload (MIS + light tracing).
+    orc = _abi.Lib(os.path.join(ROOT, "oracle", "libgammaray_ref.so"))
+    so = g.Stage(w.prims, lib=orc, environment=w.environment, seed=3)
+    fo = g.Film(w.width, w.height, lib=orc)
+    passes, t0 = 0, time.perf_counter()
+    while passes == 0 or time.perf_counter() - t0 < cpu_seconds:
+        so.render(w.camera, forms[0][1], fo, 1)
+        passes += 1
+    dt = time.perf_counter() - t0
+    out["cpu_oracle_msamples_per_s"] = passes * w.width * w.height / dt / 1e6
+    out["cpu_oracle_sample"] = f"{passes} x 1-spp pass(es), {dt:.1f} s, {os.cpu_count()} threads"
+    return out
 
 
 def profile_case(args):

@@ -744,7 +744,7 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
             const size_t ssmem = sort_smem_bytes(BLOCK, BSHADE_PER_THREAD);
             GR_CUDA_TRY(allow_sort_smem(k_bdpt_shade, ssmem));
-            int grid = resident_grid(k_bdpt_shade, ssmem, (p.nslots + BSHADE_PER_THREAD - 1) / BSHADE_PER_THREAD);
+            int grid = resident_grid(k_bdpt_shade, ssmem, p.nslots);
             k_bdpt_shade<<<grid, BLOCK, ssmem, st>>>(job.scene, p, vs, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                                  ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
                                                  ps.q_hit.as<float4>(), bs.vcount.as<uint32_t>(), ps.tp.as<float4>(),

@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const Engin
                                                                     const DevUnit* __restrict__ units,
                                                                     const float4* __restrict__ s_hot,
                                                                     const uint4* __restrict__ s_cold, uint32_t mask) {
-    __shared__ StagedSample sm[FILM_SPAN * FILM_SPAN];
+    __shared__ StagedSample sm;
     const uint32_t total = c->gather_tiles, groups = c->gather_groups;
     for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
         uint32_t g = 0;
@@ -146,10 +146,9 @@ __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const Engin
         const bool inside = x < static_cast<int>(w) && y < static_cast<int>(h);
         float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (inside) acc = J.film[static_cast<size_t>(y) * w + x];
-        for (uint32_t k = 0; k < cnt; ++k) {  // the job's passes, in order
-            const DevUnit U = units[c->gather_units[first + k]];
-            gather_tile(sm, w, h, ox, oy, acc, RingSamples{s_hot, s_cold, U.prefix, w, mask});
-        }
+        gather_passes(sm, w, h, ox, oy, acc, cnt, [&](uint32_t k) {  // the job's passes, in order
+            return RingSamples{s_hot, s_cold, units[c->gather_units[first + k]].prefix, w, mask};
+        });
         if (inside && J.live) J.film[static_cast<size_t>(y) * w + x] = acc;
     }
 }
@@ -441,8 +440,7 @@ gr_status Engine::enqueue_iteration(int cur) {
     }
     GR_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(c) + offsetof(EngineCtl, q) + nxt * sizeof(uint32_t), 0, 4, st_));
     const size_t ssmem = sort_smem_bytes(EBLOCK, ESHADE_PER_THREAD);
-    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), EBLOCK, ssmem,
-                         (C + ESHADE_PER_THREAD - 1) / ESHADE_PER_THREAD);
+    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), EBLOCK, ssmem, C);
     k_eng_shade<<<sgrid, EBLOCK, ssmem, st_>>>(c, cur, jobs_.as<DevJob>(), unit_done_.as<uint32_t>(),
                                            q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>(),
                                            q_hit_.as<float4>(), s_hot_.as<float4>(), s_cold_.as<uint4>(),

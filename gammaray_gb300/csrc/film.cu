@@ -10,15 +10,15 @@ namespace {
 __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_film_gather(const float2* __restrict__ st,
                                                                      const float4* __restrict__ color, uint32_t width,
                                                                      uint32_t height, uint32_t passes, float4* film) {
-    __shared__ StagedSample sm[FILM_SPAN * FILM_SPAN];
+    __shared__ StagedSample sm;
     const int ox = blockIdx.x * FILM_TILE, oy = blockIdx.y * FILM_TILE;
     const int x = ox + threadIdx.x % FILM_TILE, y = oy + threadIdx.x / FILM_TILE;
     const bool inside = x < static_cast<int>(width) && y < static_cast<int>(height);
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (inside) acc = film[static_cast<size_t>(y) * width + x];
     const size_t npix = static_cast<size_t>(width) * height;
-    for (uint32_t pass = 0; pass < passes; ++pass)
-        gather_tile(sm, width, height, ox, oy, acc, LinearSamples{st, color, pass * npix, width});
+    gather_passes(sm, width, height, ox, oy, acc, passes,
+                  [&](uint32_t pass) { return LinearSamples{st, color, pass * npix, width}; });
     if (inside) film[static_cast<size_t>(y) * width + x] = acc;
 }
 

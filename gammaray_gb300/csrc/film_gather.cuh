@@ -33,40 +33,81 @@ GR_D float mitchell1(float x) {
            (1.0f / 6.0f);
 }
 
+// A tile's staged samples (structure of arrays, FILM_SPAN^2 of them) and, per tile pixel,
+// an 81-bit mask of the samples in its 9x9 neighbourhood whose footprint covers it (bit
+// dy * 9 + dx for the sample dy rows and dx columns below / right of the neighbourhood's
+// corner).  Visiting set bits in increasing order is visiting contributors in
+// increasing sample index, the reference's order.
+constexpr int FILM_WIN = 2 * FILM_HALO + 1;                      // 9
+constexpr int FILM_MASK_WORDS = (FILM_WIN * FILM_WIN + 31) / 32;  // 3
 struct StagedSample {
-    float cd, rd;  // col_discr, row_discr
-    short minc, maxc, minr, maxr;
-    float r, g, b;
+    float cd[FILM_SPAN * FILM_SPAN], rd[FILM_SPAN * FILM_SPAN];  // col_discr, row_discr
+    float r[FILM_SPAN * FILM_SPAN], g[FILM_SPAN * FILM_SPAN], b[FILM_SPAN * FILM_SPAN];
+    uint32_t mask[FILM_TILE * FILM_TILE][FILM_MASK_WORDS];
 };
 
-// Adds the samples of one pass to the tile (ox, oy) of `film`.  `src(row, col, st, rgb)`
-// loads that pixel's sample: its film position (s, t) and its radiance.  Every thread of
-// the block (256 = FILM_TILE^2) must call it; `sm` holds FILM_SPAN^2 entries.
-template <class Src>
-GR_D void gather_tile(StagedSample* sm, uint32_t width, uint32_t height, int ox, int oy, float4& acc, const Src& src) {
+// Adds the samples of `npass` passes, in pass order, to the tile (ox, oy) of `film`.
+// src_at(k) gives pass k's sample source: src(row, col, st, rgb) loads that pixel's
+// sample, its film position (s, t) and its radiance.  Every thread of the block (256 =
+// FILM_TILE^2) must call it; `sm` is the block's staging area.
+//
+// Per pass: each thread stages up to three samples (film.rs:82-97: continuous position,
+// footprint) and sets their bit in the mask of every tile pixel their footprint covers;
+// then each pixel adds its contributors, set bits in increasing order, with the Mitchell
+// weight of film.rs:100-106.  The footprint is the reference's, clamped to the image
+// the same way (film.rs:90-97).
+//
+// Software-pipelined: the global loads of pass k + 1 are issued into registers before
+// pass k is accumulated.  The additions per pixel are the reference's: pass by pass,
+// then in increasing sample index.
+constexpr int FILM_STAGE_PER_THREAD = (FILM_SPAN * FILM_SPAN + FILM_TILE * FILM_TILE - 1) / (FILM_TILE * FILM_TILE);
+
+template <class SrcAt>
+GR_D void gather_passes(StagedSample& sm, uint32_t width, uint32_t height, int ox, int oy, float4& acc,
+                        uint32_t npass, const SrcAt& src_at) {
     const int tx = threadIdx.x % FILM_TILE, ty = threadIdx.x / FILM_TILE;
     const int x = ox + tx, y = oy + ty;
     const bool inside = x < static_cast<int>(width) && y < static_cast<int>(height);
     const float wf = static_cast<float>(width), hf = static_cast<float>(height);
     const long long last_col = static_cast<long long>(width) - 1, last_row = static_cast<long long>(height) - 1;
-    __syncthreads();
-    for (int k = threadIdx.x; k < FILM_SPAN * FILM_SPAN; k += FILM_TILE * FILM_TILE) {
-        int sr = oy - FILM_HALO + k / FILM_SPAN, sc = ox - FILM_HALO + k % FILM_SPAN;
-        StagedSample e;
-        e.minc = 1;
-        e.maxc = 0;  // empty footprint
-        e.minr = 1;
-        e.maxr = 0;
-        e.cd = e.rd = 0.0f;
-        e.r = e.g = e.b = 0.0f;
-        if (sr >= 0 && sc >= 0 && sr < static_cast<int>(height) && sc < static_cast<int>(width)) {
-            float2 s;
-            V3 c;
-            src(static_cast<uint32_t>(sr), static_cast<uint32_t>(sc), s, c);
+    float2 rs[FILM_STAGE_PER_THREAD];
+    V3 rc[FILM_STAGE_PER_THREAD];
+    auto load = [&](uint32_t pass) {
+        const auto src = src_at(pass);
+#pragma unroll
+        for (int j = 0; j < FILM_STAGE_PER_THREAD; ++j) {
+            int k = threadIdx.x + j * FILM_TILE * FILM_TILE;
+            int sr = oy - FILM_HALO + k / FILM_SPAN, sc = ox - FILM_HALO + k % FILM_SPAN;
+            if (k < FILM_SPAN * FILM_SPAN && sr >= 0 && sc >= 0 && sr < static_cast<int>(height) &&
+                sc < static_cast<int>(width))
+                src(static_cast<uint32_t>(sr), static_cast<uint32_t>(sc), rs[j], rc[j]);
+        }
+    };
+    if (npass) load(0);
+    for (uint32_t pass = 0; pass < npass; ++pass) {
+        __syncthreads();  // the previous pass's accumulation is done with sm
+#pragma unroll
+        for (int w = 0; w < FILM_MASK_WORDS; ++w) sm.mask[threadIdx.x][w] = 0u;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < FILM_STAGE_PER_THREAD; ++j) {
+            int k = threadIdx.x + j * FILM_TILE * FILM_TILE;
+            if (k >= FILM_SPAN * FILM_SPAN) break;
+            int ky = k / FILM_SPAN, kx = k % FILM_SPAN;
+            int sr = oy - FILM_HALO + ky, sc = ox - FILM_HALO + kx;
+            if (sr < 0 || sc < 0 || sr >= static_cast<int>(height) || sc >= static_cast<int>(width)) continue;
+            float2 s = rs[j];
             // film.rs:82-97
             float col_cont = lerp(0.0f, wf, 0.5f * (s.x + 1.0f));
             float row_cont = lerp(0.0f, hf, 0.5f * (s.y + 1.0f));
             float cd = col_cont - 0.5f, rd = row_cont - 0.5f;
+            sm.cd[k] = cd;
+            sm.rd[k] = rd;
+            sm.r[k] = rc[j].x;
+            sm.g[k] = rc[j].y;
+            sm.b[k] = rc[j].z;
+            // Footprint (film.rs:90-97), then the tile pixels it covers; footprints never
+            // exceed +-4 px of the source pixel.
             long long mnc = static_cast<long long>(ceilf(cd - 2.0f));
             long long mxc = static_cast<long long>(floorf(cd + 2.0f));
             long long mnr = static_cast<long long>(ceilf(rd - 2.0f));
@@ -75,33 +116,31 @@ GR_D void gather_tile(StagedSample* sm, uint32_t width, uint32_t height, int ox,
             mxc = mxc < 0 ? 0 : (mxc > last_col ? last_col : mxc);
             mnr = mnr < 0 ? 0 : (mnr > last_row ? last_row : mnr);
             mxr = mxr < 0 ? 0 : (mxr > last_row ? last_row : mxr);
-            e.cd = cd;
-            e.rd = rd;
-            // Relative to the tile origin; footprints never exceed +-4 px of the source.
-            e.minc = static_cast<short>(mnc - ox);
-            e.maxc = static_cast<short>(mxc - ox);
-            e.minr = static_cast<short>(mnr - oy);
-            e.maxr = static_cast<short>(mxr - oy);
-            e.r = c.x;
-            e.g = c.y;
-            e.b = c.z;
+            int c0 = max(0, static_cast<int>(mnc) - ox), c1 = min(FILM_TILE - 1, static_cast<int>(mxc) - ox);
+            int r0 = max(0, static_cast<int>(mnr) - oy), r1 = min(FILM_TILE - 1, static_cast<int>(mxr) - oy);
+            for (int py = r0; py <= r1; ++py)
+                for (int px = c0; px <= c1; ++px) {
+                    int bit = (ky - py) * FILM_WIN + (kx - px);
+                    atomicOr(&sm.mask[py * FILM_TILE + px][bit >> 5], 1u << (bit & 31));
+                }
         }
-        sm[k] = e;
-    }
-    __syncthreads();
-    if (!inside) return;
-#pragma unroll 1
-    for (int dy = 0; dy <= 2 * FILM_HALO; ++dy) {
+        __syncthreads();
+        if (pass + 1 < npass) load(pass + 1);  // in flight while this pass accumulates
+        if (!inside) continue;
 #pragma unroll
-        for (int dx = 0; dx <= 2 * FILM_HALO; ++dx) {
-            const StagedSample& e = sm[(ty + dy) * FILM_SPAN + (tx + dx)];
-            if (tx >= e.minc && tx <= e.maxc && ty >= e.minr && ty <= e.maxr) {
-                float w = mitchell1((static_cast<float>(x) - e.cd) / 2.0f) *
-                          mitchell1((static_cast<float>(y) - e.rd) / 2.0f);
-                acc.x = acc.x + e.r * w;
-                acc.y = acc.y + e.g * w;
-                acc.z = acc.z + e.b * w;
-                acc.w += w;
+        for (int w = 0; w < FILM_MASK_WORDS; ++w) {
+            uint32_t m = sm.mask[threadIdx.x][w];
+            while (m) {
+                int bit = w * 32 + __ffs(m) - 1;
+                m &= m - 1;
+                int dy = bit / FILM_WIN, dx = bit - dy * FILM_WIN;
+                int k = (ty + dy) * FILM_SPAN + (tx + dx);
+                float wgt = mitchell1((static_cast<float>(x) - sm.cd[k]) / 2.0f) *
+                            mitchell1((static_cast<float>(y) - sm.rd[k]) / 2.0f);
+                acc.x = acc.x + sm.r[k] * wgt;
+                acc.y = acc.y + sm.g[k] * wgt;
+                acc.z = acc.z + sm.b[k] * wgt;
+                acc.w += wgt;
             }
         }
     }

@@ -293,7 +293,8 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
             if (timed) GR_TRY_S(mark(e0));
-            int grid = resident_grid(k_shade, shade_smem, (n + SHADE_PER_THREAD - 1) / SHADE_PER_THREAD);
+            // Every resident block; each picks its entries per thread from the queue length.
+            int grid = resident_grid(k_shade, shade_smem, n);
             k_shade<<<grid, BLOCK, shade_smem, st>>>(job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                             ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
                                             ps.q_hit.as<float4>(), ps.tp.as<float4>(), ps.light.as<float4>(),
@@ -496,7 +497,8 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
                 break;
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            int grid = resident_grid(k_shade, shade_smem, (n + SHADE_PER_THREAD - 1) / SHADE_PER_THREAD);
+            // Every resident block; each picks its entries per thread from the queue length.
+            int grid = resident_grid(k_shade, shade_smem, n);
             k_shade<<<grid, BLOCK, shade_smem, st>>>(sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit, tp,
                                             light, key, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt]);
             GR_CUDA_TRY(cudaGetLastError());
