@@ -382,6 +382,40 @@ def run_ours(args, rank, world, local):
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
            "includes": "host SAH build + wide collapse + upload, 64-spp render, film read-back"}
 
+    # The same render on a tree built on the GPU (GR_BUILD_DEVICE_LBVH), and end to end with
+    # that build: the reference's host SAH build is the default and the headline.
+    dev_build = None
+    if rank == 0:
+        g.Stage(w.prims[-1:], lib=lib, device_build=True).close()  # build kernels loaded
+        std = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1, device_build=True)
+        fd = g.Film(w.width, w.height, lib=lib)
+        std.render(w.camera, w.integrator, fd, 2)
+        dms = []
+        for _ in range(max(1, args.steps)):
+            fd.clear()
+            flush.zero_()
+            torch.cuda.synchronize()
+            std.render(w.camera, w.integrator, fd, w.spp)
+            dms.append(std.last_stats().device_ms)
+        dinfo = std.info()
+        de2e = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            st3 = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1, device_build=True)
+            f3 = g.Film(w.width, w.height, lib=lib)
+            st3.render(w.camera, w.integrator, f3, w.spp)
+            lib.call("gr_film_read", f3.handle, _abi.fptr(acc), _abi.fptr(wt))
+            de2e.append((time.perf_counter() - t1) * 1e3)
+            st3.close()
+            f3.close()
+        dev_build = {"build_ms_device": dinfo.build_seconds * 1e3, "build_ms_host_sah": info.build_seconds * 1e3,
+                     "wide_nodes": int(dinfo.num_wide_nodes),
+                     "msamples_per_s": samples_per_step / (statistics.median(dms) * 1e-3) / 1e6,
+                     "e2e_msamples_per_s": samples_per_step / (statistics.median(de2e) * 1e-3) / 1e6}
+        std.close()
+        fd.close()
+
     # Roofline of the dominant kernel (extension / closest hit): counted bytes per ray.
     node_bytes = 32 * info.bvh_width
     b_ray = nodes_per_ray * node_bytes + prims_per_ray * 48 + 48
@@ -416,7 +450,7 @@ def run_ours(args, rank, world, local):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": config_of(w), "mrays_per_s": mrays, "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
                 "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s": wall,
-                "batched": batched, "served": served, "bdpt": bdpt,
+                "batched": batched, "served": served, "bdpt": bdpt, "device_build": dev_build,
                 "scene": {"components": int(info.num_components), "wide_nodes": int(info.num_wide_nodes),
                           "device_bytes": int(info.device_bytes), "build_s": info.build_seconds}}
         print(json.dumps(line), flush=True)

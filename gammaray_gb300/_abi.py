@@ -91,7 +91,12 @@ class SceneDesc(C.Structure):
         ("environment", F3),
         ("bvh_width", C.c_uint32),
         ("leaf_size", C.c_uint32),
+        ("build", C.c_uint32),
     ]
+
+
+BUILD_HOST_SAH = 0
+BUILD_DEVICE_LBVH = 1
 
 
 class SceneInfo(C.Structure):

@@ -435,7 +435,7 @@ class Film:
         return sp
 
 
-def scene_desc(prims, environment=(0.0, 0.0, 0.0), bvh_width: int = 0, leaf_size: int = 0):
+def scene_desc(prims, environment=(0.0, 0.0, 0.0), bvh_width: int = 0, leaf_size: int = 0, build: int = 0):
     """gr_scene_desc for `prims` (materials deduplicated by identity, in first-use order).
     Returns (desc, keepalive); the keepalive owns the arrays the desc points into."""
     materials: list[Material] = []
@@ -456,6 +456,7 @@ def scene_desc(prims, environment=(0.0, 0.0, 0.0), bvh_width: int = 0, leaf_size
     d.environment[:] = [float(x) for x in environment]
     d.bvh_width = bvh_width
     d.leaf_size = leaf_size
+    d.build = build
     return d, (materials, mat_descs, prim_descs, list(prims))
 
 
@@ -473,16 +474,19 @@ class Stage:
     """render/stage.rs:10-36 — owns the prims and their BVH; trace() renders one pass.
 
     Extensions (defaults reproduce the reference): `environment` radiance for escaped
-    rays, device `bvh_width` / `leaf_size`, and the random `seed`.
+    rays, device `bvh_width` / `leaf_size`, the random `seed`, and `device_build=True`
+    for a BVH built on the GPU (GR_BUILD_DEVICE_LBVH) instead of the reference's host
+    SAH build.
     """
 
     def __init__(self, prims, lib: _abi.Lib | None = None, environment=(0.0, 0.0, 0.0), bvh_width: int = 0,
-                 leaf_size: int = 0, seed: int = 0):
+                 leaf_size: int = 0, seed: int = 0, device_build: bool = False):
         self.lib = _default_lib(lib)
         self.prims = list(prims)
         self.seed = int(seed)
         self._pass = 0
-        d, keep = scene_desc(self.prims, environment, bvh_width, leaf_size)
+        d, keep = scene_desc(self.prims, environment, bvh_width, leaf_size,
+                             _abi.BUILD_DEVICE_LBVH if device_build else _abi.BUILD_HOST_SAH)
         h = C.c_void_p()
         self.lib.call("gr_scene_create", C.byref(d), C.byref(h))
         self.handle = h

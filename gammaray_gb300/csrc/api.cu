@@ -179,10 +179,17 @@ gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out) {
     SceneBuffers& b = s->buf;
     cudaStream_t st = s->stream;
     uint64_t total = 0;
-    GR_TRY(upload(b.nodes, h.nodes, st, total));
-    GR_TRY(upload(b.prims, h.prims, st, total));
-    GR_TRY(upload(b.tri_nidx, h.tri_normal_idx, st, total));
-    GR_TRY(upload(b.tri_uvidx, h.tri_uv_idx, st, total));
+    if (h.device_build) {
+        uint32_t num_wide = 0, stack_depth = 0;
+        GR_TRY(build_bvh_device(h, b, st, num_wide, stack_depth, total));
+        h.num_wide_nodes = num_wide;
+        h.stack_depth = stack_depth;
+    } else {
+        GR_TRY(upload(b.nodes, h.nodes, st, total));
+        GR_TRY(upload(b.prims, h.prims, st, total));
+        GR_TRY(upload(b.tri_nidx, h.tri_normal_idx, st, total));
+        GR_TRY(upload(b.tri_uvidx, h.tri_uv_idx, st, total));
+    }
     GR_TRY(upload(b.normals, h.normals, st, total));
     GR_TRY(upload(b.uvs, h.uvs, st, total));
     GR_TRY(upload(b.prim_material, h.prim_material, st, total));
@@ -225,7 +232,10 @@ gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out) {
 }
 
 static uint64_t planned_bytes(const HostBuild& h) {
-    return h.nodes.size() * 4 + h.prims.size() * 4 + (h.tri_normal_idx.size() + h.tri_uv_idx.size()) * 4 +
+    // A device build's node count is known only after it runs: at most one wide node
+    // per component.
+    const uint64_t nodes = h.device_build ? h.num_components * 8 * h.width * 4 : h.nodes.size() * 4;
+    return nodes + h.prims.size() * 4 + (h.tri_normal_idx.size() + h.tri_uv_idx.size()) * 4 +
            (h.normals.size() + h.uvs.size()) * 4 + h.prim_material.size() * 4 + h.materials.size() * sizeof(DevMaterial) +
            h.lights.size() * sizeof(LightRec) + h.light_tris.size() * 4 +
            (h.light_tri_normal_idx.size() + h.light_tri_uv_idx.size()) * 4 + h.light_cdf.size() * 4;

@@ -116,6 +116,11 @@ struct gr_film {
 
 namespace gr {
 
+// Device BVH build (bvh_build.cu) for a HostBuild made with GR_BUILD_DEVICE_LBVH:
+// fills b.nodes, b.prims, b.tri_nidx, b.tri_uvidx (leaf order).
+gr_status build_bvh_device(const HostBuild& h, SceneBuffers& b, cudaStream_t st, uint32_t& num_wide,
+                           uint32_t& stack_depth, uint64_t& bytes);
+
 // Kernel-side entry points (implemented in the .cu files).
 gr_status launch_trace(const DeviceScene& s, const float* rays, uint64_t n, gr_hit* hits, bool any_hit,
                        const float* tmax, int* err, cudaStream_t st);

@@ -71,6 +71,11 @@ struct HostBuild {
     uint32_t width = 4;
     uint32_t stack_depth = 0;
     bool any_normals = false, any_uvs = false;
+    // Device build (GR_BUILD_DEVICE_LBVH): records above are in component order, the
+    // tree is made on the GPU from these boxes (lo.xyz, hi.xyz per component).
+    bool device_build = false;
+    uint32_t leaf_size = 0;
+    std::vector<float> item_boxes;
 };
 
 // Evaluates DisneyMaterialBuilder::build and the lobe constructors

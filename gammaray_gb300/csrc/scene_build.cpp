@@ -483,22 +483,18 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
         return false;
     }
 
-    RefBuilder rb(items);
-    rb.nodes.reserve(2 * items.size());
-    rb.order.reserve(items.size());
-    std::vector<uint32_t> idx(items.size());
-    std::iota(idx.begin(), idx.end(), 0u);
-    int32_t root = rb.build(idx.data(), idx.size());
-    out.num_binary_nodes = rb.nodes.size();
+    if (desc.build != GR_BUILD_HOST_SAH && desc.build != GR_BUILD_DEVICE_LBVH) {
+        err = "build must be GR_BUILD_HOST_SAH or GR_BUILD_DEVICE_LBVH";
+        return false;
+    }
+    out.device_build = desc.build == GR_BUILD_DEVICE_LBVH;
 
-    // Leaf-order primitive records.
+    // Primitive records: in leaf order for the host build, in component order for the
+    // device build (which sorts them itself, bvh_build.cu).
     out.prims.resize(items.size() * 12, 0.0f);
-    std::vector<Box> comp_box(items.size());
     if (out.any_normals) out.tri_normal_idx.assign(items.size() * 3, NO_INDEX);
     if (out.any_uvs) out.tri_uv_idx.assign(items.size() * 3, NO_INDEX);
-    for (size_t k = 0; k < rb.order.size(); ++k) {
-        const Item& it = items[rb.order[k]];
-        comp_box[k] = it.box;
+    auto put_record = [&](size_t k, const Item& it) {
         const gr_prim_desc& d = desc.prims[it.prim];
         float* r = &out.prims[k * 12];
         if (d.kind == GR_PRIM_SPHERE) {
@@ -526,14 +522,38 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
             if (out.any_uvs && d.tri_uvs)
                 for (int q = 0; q < 3; ++q) out.tri_uv_idx[3 * k + q] = ubase[it.prim] + d.tri_uvs[3 * it.comp + q];
         }
-    }
+    };
 
-    Collapser col(rb.nodes, comp_box, W, L, out.nodes);
-    uint32_t su = 0;
-    Cand rc = col.of_bin(root);
-    col.emit(rc, su);
-    out.stack_depth = su + 1;
-    out.num_wide_nodes = out.nodes.size() / (8 * W);
+    if (out.device_build) {
+        out.leaf_size = L;
+        out.item_boxes.resize(items.size() * 6);
+        for (size_t k = 0; k < items.size(); ++k) {
+            put_record(k, items[k]);
+            for (int a = 0; a < 3; ++a) {
+                out.item_boxes[6 * k + a] = items[k].box.lo[a];
+                out.item_boxes[6 * k + 3 + a] = items[k].box.hi[a];
+            }
+        }
+    } else {
+        RefBuilder rb(items);
+        rb.nodes.reserve(2 * items.size());
+        rb.order.reserve(items.size());
+        std::vector<uint32_t> idx(items.size());
+        std::iota(idx.begin(), idx.end(), 0u);
+        int32_t root = rb.build(idx.data(), idx.size());
+        out.num_binary_nodes = rb.nodes.size();
+        std::vector<Box> comp_box(items.size());
+        for (size_t k = 0; k < rb.order.size(); ++k) {
+            comp_box[k] = items[rb.order[k]].box;
+            put_record(k, items[rb.order[k]]);
+        }
+        Collapser col(rb.nodes, comp_box, W, L, out.nodes);
+        uint32_t su = 0;
+        Cand rc = col.of_bin(root);
+        col.emit(rc, su);
+        out.stack_depth = su + 1;
+        out.num_wide_nodes = out.nodes.size() / (8 * W);
+    }
 
     // Light tables (Bvh::build caches light prims, bvh.rs:364-370; Mesh area CDF, mesh.rs:161-170).
     for (uint32_t p = 0; p < desc.num_prims; ++p) {

@@ -131,7 +131,19 @@ typedef struct gr_scene_desc {
      * The CPU restatement ignores both (it keeps the reference's binary BVH). */
     uint32_t bvh_width;
     uint32_t leaf_size;
+    /* Which builder makes the tree (the CPU restatement always uses the reference's):
+     *   GR_BUILD_HOST_SAH (0): the reference's SAH build on the host (geom/bvh.rs:182-382)
+     *                          collapsed to the wide layout;
+     *   GR_BUILD_DEVICE_LBVH (1): a linear BVH built on the GPU (Morton-sorted primitives,
+     *                          Karras 2012 radix tree, same wide collapse) — an extension
+     *                          for large scenes, where the host build dominates scene
+     *                          creation.  Closest hits are the same; ties at exactly
+     *                          equal distance may pick the other primitive. */
+    uint32_t build;
 } gr_scene_desc;
+
+#define GR_BUILD_HOST_SAH 0u
+#define GR_BUILD_DEVICE_LBVH 1u
 
 typedef struct gr_scene gr_scene;
 
