@@ -22,6 +22,14 @@ constexpr uint32_t SORT_BUCKETS = 32;
 #endif
 constexpr uint32_t SHADE_PER_THREAD = GR_SHADE_PER_THREAD;
 
+// Rays per thread per chunk when the extension kernels trace their queue grouped by
+// direction (octant and dominant axis; 0: no sort).  Measured on the path-tracer
+// workload: 8 -> +2.2%; 2, 32 and 64 slower (the barrier per chunk waits for the chunk's
+// slowest ray, which outweighs the coherence gained).
+#ifndef GR_EXTEND_SORT
+#define GR_EXTEND_SORT 8
+#endif
+
 // The sort's shared memory (dynamic, sort_smem_bytes(NT, PER) bytes at the start of the
 // block's dynamic shared memory): bucket sizes, then per-entry bucket and sorted order.
 struct SortView {

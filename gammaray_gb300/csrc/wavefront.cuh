@@ -6,7 +6,9 @@
 #include <cstdlib>
 
 #include "runtime.hpp"
+#include "shade_sort.cuh"
 #include "traverse.cuh"
+
 
 namespace gr {
 namespace {
@@ -49,7 +51,7 @@ __global__ void GR_EXTEND_BOUNDS k_extend(DeviceScene s, const uint32_t* __restr
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
     uint32_t counts[2] = {0, 0};
     const uint32_t budget = 8u * s.num_components + 4096u;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    auto trace = [&](uint32_t q) {
         float4 o4 = q_o[q], d4 = q_d[q];
         TravState t;
         trav_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX);
@@ -63,7 +65,31 @@ __global__ void GR_EXTEND_BOUNDS k_extend(DeviceScene s, const uint32_t* __restr
             }
         }
         q_hit[q] = make_float4(t.closest, __int_as_float(t.hit), t.hu, t.hv);
+    };
+#if GR_EXTEND_SORT
+    // Each block traces its chunk of the queue grouped by direction (octant, dominant axis).
+    const SortView sv =
+        sort_view<BLOCK, GR_EXTEND_SORT>(smem + static_cast<size_t>(SMEM_STACK) * BLOCK * (sizeof(int32_t) + sizeof(float)));
+    const uint32_t per = chunk_per_thread<BLOCK, GR_EXTEND_SORT>(n, gridDim.x);
+    const uint32_t chunk = BLOCK * per;
+    for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
+        const uint32_t cn = min(chunk, n - c0);
+        sort_chunk<BLOCK, GR_EXTEND_SORT>(sv, cn, per, [&](uint32_t i) {
+            float4 d = q_d[c0 + i];
+            float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+            uint32_t dom = ax >= ay && ax >= az ? 0u : (ay >= az ? 1u : 2u);
+            uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+            return oct * 3u + dom;
+        });
+        for (uint32_t e = 0; e < per; ++e) {
+            uint32_t i = e * BLOCK + threadIdx.x;
+            if (i < cn) trace(c0 + sv.order[i]);
+        }
+        __syncthreads();  // sv is reused by the next chunk
     }
+#else
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) trace(q);
+#endif
     if (COUNT && (counts[0] | counts[1])) {
         atomicAdd(rays + (CNT_NODES - CNT_RAYS) / 2, static_cast<unsigned long long>(counts[0]));
         atomicAdd(rays + (CNT_PRIMS - CNT_RAYS) / 2, static_cast<unsigned long long>(counts[1]));
@@ -103,7 +129,7 @@ int resident_grid(K kernel, size_t smem, uint32_t n) {
 template <int W, bool COUNT>
 gr_status extend_launch(const DeviceScene& s, uint32_t cap_n, const uint32_t* count, const float4* qo,
                         const float4* qd, float4* qh, int* err, unsigned long long* rays, cudaStream_t st) {
-    size_t smem = step_stack_smem_bytes(BLOCK);
+    size_t smem = step_stack_smem_bytes(BLOCK) + (GR_EXTEND_SORT ? sort_smem_bytes(BLOCK, GR_EXTEND_SORT) : 0);
     int grid = resident_grid(k_extend<W, COUNT>, smem, cap_n);
     k_extend<W, COUNT><<<grid, BLOCK, smem, st>>>(s, count, qo, qd, qh, err, rays);
     return GR_OK;
