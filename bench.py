@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-bdpt", action="store_true", help="skip the BDPT measurement")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=3.0, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--serve-target", type=float, default=1e-3,
+                    help="relMSE target of the progressive serving leg (0: skip it)")
     ap.add_argument("--profile-case", action="store_true",
                     help="render the workload once (untimed, --spp passes) and exit: the small case for ncu")
     return ap.parse_args()
@@ -234,7 +236,7 @@ def run_batched(lib):
             "films_equal_plain": same}
 
 
-def run_served(lib, n_req, rate, seed=11):
+def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3):
     """Config 5: 16 resident scenes (10k-2M triangles); Poisson arrivals; random pose,
     resolution 256^2..1920x1080, spp 1-256, depth 4-16.  Served by the continuous-
     batching loop vs a FIFO timeline of one gr_render per request on the same GPU."""
@@ -291,11 +293,68 @@ def run_served(lib, n_req, rate, seed=11):
         lat.append(st.finish_ms - st.submit_ms)
         srv.take(rid)
     srv.close()
-    return {"workload": "serve_16_scenes", "requests": n_req, "rate_per_s": rate, "samples": samples,
+    out = {"workload": "serve_16_scenes", "requests": n_req, "rate_per_s": rate, "samples": samples,
+           "msamples_per_s": samples / span / 1e6, "latency_ms": percentiles(lat),
+           "plain_fifo_msamples_per_s": samples / plain_span / 1e6, "plain_fifo_latency_ms": percentiles(lat_plain),
+           "plain_busy_msamples_per_s": samples / sum(dur) / 1e6,
+           "speedup_vs_plain_fifo": plain_span / span}
+    if target_rel_mse > 0:
+        out["progressive"] = run_progressive(lib, g, serve, stages, reqs, target_rel_mse)
+    return out
+
+
+PROGRESSIVE_MAX_PASSES = 1024
+
+
+def run_progressive(lib, g, serve, stages, reqs, target):
+    """The same requests refined progressively: each stops at the first checkpoint (8, 16,
+    32, ... passes) whose half-film relMSE estimate is <= target, or at 1024 passes (the
+    drawn spp is not used here: relMSE, not a pass count, ends a request).  The plain comparator renders each request's final pass count with one
+    gr_render, FIFO, as if it had known the count in advance."""
+    srv = serve.Server(lib, max_active=16)
+    ids = {}
+    t0 = time.perf_counter()
+    nxt = 0
+    while nxt < len(reqs) or any(srv.poll(i).state < 2 for i in ids.values()):
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt]["arrival"] <= now:
+            r = reqs[nxt]
+            ids[nxt] = srv.submit(stages[r["scene"]], r["cam"], g.PathTracerIntegrator(max_depth=r["depth"]),
+                                  r["res"][0], r["res"][1], PROGRESSIVE_MAX_PASSES, target_rel_mse=target)
+            nxt += 1
+        if nxt < len(reqs) and not any(srv.poll(i).state < 2 for i in ids.values()):
+            time.sleep(max(0.0, reqs[nxt]["arrival"] - now))
+            continue
+        srv.step(2.0)
+    span = time.perf_counter() - t0 - reqs[0]["arrival"]
+    lat, passes, met, est = [], [], 0, []
+    for k, rid in ids.items():
+        st = srv.poll(rid)
+        lat.append(st.finish_ms - st.submit_ms)
+        passes.append(int(st.passes_done))
+        est.append(float(st.rel_mse))
+        met += st.rel_mse <= target
+        srv.take(rid)
+    srv.close()
+    samples = sum(r["res"][0] * r["res"][1] * n for r, n in zip(reqs, passes))
+    finish, lat_plain, busy = 0.0, [], 0.0
+    for r, n in zip(reqs, passes):
+        f = g.Film(*r["res"], lib=lib)
+        t1 = time.perf_counter()
+        stages[r["scene"]].render(r["cam"], g.PathTracerIntegrator(max_depth=r["depth"]), f, n)
+        d = time.perf_counter() - t1
+        f.close()
+        busy += d
+        start = max(finish, r["arrival"])
+        finish = start + d
+        lat_plain.append((finish - r["arrival"]) * 1e3)
+    plain_span = finish - reqs[0]["arrival"]
+    hist = {str(n): passes.count(n) for n in sorted(set(passes))}
+    return {"target_rel_mse": target, "reached_target": int(met), "passes_histogram": hist,
+            "rel_mse_estimate": percentiles(est), "samples": samples,
             "msamples_per_s": samples / span / 1e6, "latency_ms": percentiles(lat),
             "plain_fifo_msamples_per_s": samples / plain_span / 1e6, "plain_fifo_latency_ms": percentiles(lat_plain),
-            "plain_busy_msamples_per_s": samples / sum(dur) / 1e6,
-            "speedup_vs_plain_fifo": plain_span / span}
+            "plain_busy_msamples_per_s": samples / busy / 1e6, "speedup_vs_plain_fifo": plain_span / span}
 
 
 def run_ours(args, rank, world, local):
@@ -442,7 +501,7 @@ def run_ours(args, rank, world, local):
     if rank == 0 and not args.no_batch:
         batched = run_batched(lib)
     if rank == 0 and not args.no_serve:
-        served = run_served(lib, args.serve_requests, args.serve_rate)
+        served = run_served(lib, args.serve_requests, args.serve_rate, target_rel_mse=args.serve_target)
     if rank == 0:
         cb = cpu_baseline(w, args.cpu_seconds) if world == 1 else None
         line = {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,

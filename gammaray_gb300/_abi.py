@@ -250,6 +250,8 @@ class Request(C.Structure):
         ("params", RenderParams),
         ("width", C.c_uint32),
         ("height", C.c_uint32),
+        ("target_rel_mse", C.c_float),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -260,6 +262,8 @@ class RequestStatus(C.Structure):
         ("submit_ms", C.c_double),
         ("start_ms", C.c_double),
         ("finish_ms", C.c_double),
+        ("rel_mse", C.c_float),
+        ("reserved", C.c_uint32),
     ]
 
 

@@ -247,7 +247,49 @@ struct ServerRequest {
     uint32_t passes_done = 0;
     double submit_ms = 0, start_ms = 0, finish_ms = 0;
     uint64_t bytes = 0;
+    // Progressive refinement: even passes go to `film` (job), odd passes to `film2`
+    // (job2); passes are appended up to `limit`, the next checkpoint (8, 16, 32, ...).
+    bool progressive = false;
+    DevBuf film2;
+    uint32_t job2 = 0;
+    uint32_t limit = 0;
+    float rel_mse = 0.0f;
+    uint32_t cap() const { return progressive ? limit : req.params.spp; }
 };
+
+constexpr uint32_t FIRST_CHECKPOINT = 8;
+constexpr int EST_BLOCKS = 256;
+
+// Per-block sums of |a - b|^2 and |(accum_a + accum_b) / (weight_a + weight_b)|^2 over the
+// pixels of two half-films (a, b = accum / weight); pixels without weight are skipped.
+// Fixed blocks and an in-order host sum keep the estimate the same from run to run.
+__global__ void __launch_bounds__(256) k_half_film_error(const float4* __restrict__ a, const float4* __restrict__ b,
+                                                         uint32_t n, double2* __restrict__ partial) {
+    double d = 0.0, m = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 pa = a[i], pb = b[i];
+        if (!(pa.w > 0.0f) || !(pb.w > 0.0f)) continue;
+        double ax = pa.x / pa.w, ay = pa.y / pa.w, az = pa.z / pa.w;
+        double bx = pb.x / pb.w, by = pb.y / pb.w, bz = pb.z / pb.w;
+        double w = static_cast<double>(pa.w) + pb.w;
+        double fx = (static_cast<double>(pa.x) + pb.x) / w, fy = (static_cast<double>(pa.y) + pb.y) / w,
+               fz = (static_cast<double>(pa.z) + pb.z) / w;
+        d += (ax - bx) * (ax - bx) + (ay - by) * (ay - by) + (az - bz) * (az - bz);
+        m += fx * fx + fy * fy + fz * fz;
+    }
+    __shared__ double sd[256], sm[256];
+    sd[threadIdx.x] = d;
+    sm[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (static_cast<int>(threadIdx.x) < o) {
+            sd[threadIdx.x] += sd[threadIdx.x + o];
+            sm[threadIdx.x] += sm[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = make_double2(sd[0], sm[0]);
+}
 
 struct gr_server {
     std::mutex mu;
@@ -280,12 +322,22 @@ gr_status schedule(gr_server* s) {
         if (s->opts.max_active && active >= s->opts.max_active) break;
         if (s->used + r->bytes > s->budget) break;  // admission by free device memory, in arrival order
         gr_status st;
-        GR_CUDA_TRY(r->film.ensure(r->bytes));
-        GR_CUDA_TRY(cudaMemset(r->film.ptr, 0, r->bytes));
+        const size_t film_bytes = r->progressive ? r->bytes / 2 : r->bytes;
+        GR_CUDA_TRY(r->film.ensure(film_bytes));
+        GR_CUDA_TRY(cudaMemset(r->film.ptr, 0, film_bytes));
         DevJob dj = make_job(r->req.scene, r->req.camera, r->req.params, r->req.width, r->req.height,
                              r->film.as<float4>());
         st = s->engine.add_job(dj, 0, 0, r->job);
         if (st != GR_OK) return st;
+        if (r->progressive) {
+            const size_t half = r->bytes / 2;
+            GR_CUDA_TRY(r->film2.ensure(half));
+            GR_CUDA_TRY(cudaMemset(r->film2.ptr, 0, half));
+            DevJob d2 = make_job(r->req.scene, r->req.camera, r->req.params, r->req.width, r->req.height,
+                                 r->film2.as<float4>());
+            st = s->engine.add_job(d2, 0, 0, r->job2);
+            if (st != GR_OK) return st;
+        }
         s->used += r->bytes;
         r->state = GR_REQUEST_RUNNING;
         r->start_ms = s->now_ms();
@@ -302,17 +354,18 @@ gr_status schedule(gr_server* s) {
     // one backlog (about two pools) of work.
     std::vector<ServerRequest*> order;
     for (auto& r : s->reqs)
-        if (r->state == GR_REQUEST_RUNNING && r->appended < r->req.params.spp) order.push_back(r.get());
+        if (r->state == GR_REQUEST_RUNNING && r->appended < r->cap()) order.push_back(r.get());
     std::stable_sort(order.begin(), order.end(), [](ServerRequest* a, ServerRequest* b) {
-        uint64_t ra = static_cast<uint64_t>(a->req.params.spp - a->appended) * a->req.width * a->req.height;
-        uint64_t rb = static_cast<uint64_t>(b->req.params.spp - b->appended) * b->req.width * b->req.height;
+        uint64_t ra = static_cast<uint64_t>(a->cap() - a->appended) * a->req.width * a->req.height;
+        uint64_t rb = static_cast<uint64_t>(b->cap() - b->appended) * b->req.width * b->req.height;
         return ra < rb;
     });
     std::vector<std::pair<uint32_t, uint32_t>> batch;
     std::vector<ServerRequest*> owners;
     for (ServerRequest* r : order) {
-        while (backlog < want && r->appended < r->req.params.spp) {
-            batch.emplace_back(r->job, r->req.params.first_pass + r->appended);
+        while (backlog < want && r->appended < r->cap()) {
+            const bool odd = r->progressive && (r->appended & 1u);
+            batch.emplace_back(odd ? r->job2 : r->job, r->req.params.first_pass + r->appended);
             owners.push_back(r);
             r->appended += 1;
             backlog += static_cast<uint64_t>(r->req.width) * r->req.height;
@@ -328,6 +381,29 @@ gr_status schedule(gr_server* s) {
     return GR_OK;
 }
 
+// relMSE estimate of a progressive request's image from its two half-films: the
+// half-images a and b are independent estimates with variance v each, so E|a - b|^2 = 2v
+// and the full image (variance v / 2) has MSE ~ sum |a - b|^2 / 4.
+gr_status half_film_rel_mse(gr_server* s, const ServerRequest& r, float& out) {
+    DevBuf partial;
+    GR_CUDA_TRY(partial.ensure(EST_BLOCKS * sizeof(double2)));
+    const uint32_t n = r.req.width * r.req.height;
+    cudaStream_t st = s->engine.stream();
+    k_half_film_error<<<EST_BLOCKS, 256, 0, st>>>(r.film.as<float4>(), r.film2.as<float4>(), n,
+                                                 partial.as<double2>());
+    GR_CUDA_TRY(cudaGetLastError());
+    std::vector<double2> h(EST_BLOCKS);
+    GR_CUDA_TRY(cudaMemcpyAsync(h.data(), partial.ptr, EST_BLOCKS * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    GR_CUDA_TRY(cudaStreamSynchronize(st));
+    double d = 0.0, m = 0.0;
+    for (const double2& v : h) {
+        d += v.x;
+        m += v.y;
+    }
+    out = m > 0.0 ? static_cast<float>(d / 4.0 / m) : 0.0f;
+    return GR_OK;
+}
+
 // Marks passes gathered (every unit below the engine's g_lo is in its film).
 gr_status progress(gr_server* s) {
     EngineCtl c;
@@ -338,10 +414,17 @@ gr_status progress(gr_server* s) {
         uint32_t d = 0;
         for (uint32_t u : r->units) d += u < c.g_lo ? 1 : 0;
         r->passes_done = d;
-        if (d == r->req.params.spp) {
-            r->state = GR_REQUEST_DONE;
-            r->finish_ms = s->now_ms();
+        if (d != r->cap()) continue;
+        if (r->progressive) {  // a checkpoint: estimate the error from the two half-films
+            st = half_film_rel_mse(s, *r, r->rel_mse);
+            if (st != GR_OK) return st;
+            if (!(r->rel_mse <= r->req.target_rel_mse) && r->limit < r->req.params.spp) {
+                r->limit = std::min(2 * r->limit, r->req.params.spp);
+                continue;
+            }
         }
+        r->state = GR_REQUEST_DONE;
+        r->finish_ms = s->now_ms();
     }
     return GR_OK;
 }
@@ -397,6 +480,15 @@ gr_status gr_server_submit(gr_server* s, const gr_request* r, uint64_t* id) {
     q->req = *r;
     q->state = r->params.spp ? GR_REQUEST_QUEUED : GR_REQUEST_DONE;
     q->bytes = static_cast<uint64_t>(r->width) * r->height * sizeof(float4);
+    if (!(r->target_rel_mse >= 0.0f)) {
+        set_error("target_rel_mse must be >= 0");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    if (r->target_rel_mse > 0.0f) {  // two half-films
+        q->progressive = true;
+        q->bytes *= 2;
+        q->limit = std::min(FIRST_CHECKPOINT, r->params.spp);
+    }
     q->submit_ms = s->now_ms();
     if (q->bytes > s->budget) {
         set_error("request film exceeds the server's memory budget");
@@ -445,6 +537,8 @@ gr_status gr_server_poll(gr_server* s, uint64_t id, gr_request_status* out) {
     out->submit_ms = r->submit_ms;
     out->start_ms = r->start_ms;
     out->finish_ms = r->finish_ms;
+    out->rel_mse = r->rel_mse;
+    out->reserved = 0;
     return GR_OK;
 }
 
@@ -462,6 +556,11 @@ gr_status gr_server_cancel(gr_server* s, uint64_t id) {
     if (r->state == GR_REQUEST_RUNNING) {
         gr_status st = s->engine.cancel_job(r->job);
         if (st != GR_OK) return st;
+        if (r->progressive) {
+            st = s->engine.cancel_job(r->job2);
+            if (st != GR_OK) return st;
+            r->limit = r->appended;
+        }
         // Its appended units still drain (paths die on their next shade; the gather
         // skips the film); no further passes are appended.
         r->req.params.spp = r->appended;
@@ -490,6 +589,12 @@ gr_status gr_server_take(gr_server* s, uint64_t id, float* accum, float* weight)
         if (r->film.ptr && (accum || weight)) {
             std::vector<float4> px(n);
             GR_CUDA_TRY(cudaMemcpy(px.data(), r->film.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
+            if (r->progressive && r->film2.ptr) {  // even + odd passes
+                std::vector<float4> p2(n);
+                GR_CUDA_TRY(cudaMemcpy(p2.data(), r->film2.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
+                for (size_t i = 0; i < n; ++i)
+                    px[i] = make_float4(px[i].x + p2[i].x, px[i].y + p2[i].y, px[i].z + p2[i].z, px[i].w + p2[i].w);
+            }
             for (size_t i = 0; i < n; ++i) {
                 if (accum) {
                     accum[3 * i] = px[i].x;

@@ -33,12 +33,16 @@ class Server:
         except Exception:
             pass
 
-    def submit(self, stage, camera, integrator, width: int, height: int, spp: int, first_pass: int = 0) -> int:
+    def submit(self, stage, camera, integrator, width: int, height: int, spp: int, first_pass: int = 0,
+               target_rel_mse: float = 0.0) -> int:
+        """Queues a render of `spp` passes; with target_rel_mse > 0, passes stop once the
+        estimated relative MSE reaches it (spp is then the most passes)."""
         r = _abi.Request()
         r.scene = stage.handle.value
         r.camera = camera.desc()
         r.params = stage.params(integrator, spp, first_pass)
         r.width, r.height = width, height
+        r.target_rel_mse = float(target_rel_mse)
         rid = C.c_uint64()
         self.lib.call("gr_server_submit", self.handle, C.byref(r), C.byref(rid))
         self.sizes[rid.value] = (width, height)

@@ -414,6 +414,13 @@ typedef struct gr_request {
     gr_render_params params;
     uint32_t width;
     uint32_t height;
+    /* Progressive refinement (serving extension).  0: render exactly params.spp passes.
+     * > 0: render passes until the estimated relative MSE of the image falls to this
+     * target, at most params.spp passes.  The estimate compares two half-images (even and
+     * odd passes): relMSE ~ sum |a - b|^2 / 4 / sum |(a + b) / 2|^2.  It is taken after 8,
+     * 16, 32, ... passes, so the pass count, and the image, depend on the request alone. */
+    float target_rel_mse;
+    uint32_t reserved;
 } gr_request;
 
 typedef enum gr_request_state {
@@ -430,6 +437,8 @@ typedef struct gr_request_status {
     double submit_ms;  /* host clock, milliseconds since server creation */
     double start_ms;
     double finish_ms;
+    float rel_mse;     /* latest relative-MSE estimate of a progressive request, else 0 */
+    uint32_t reserved;
 } gr_request_status;
 
 gr_status gr_server_create(const gr_server_options* options, gr_server** out);
@@ -439,7 +448,8 @@ gr_status gr_server_submit(gr_server* server, const gr_request* request, uint64_
 gr_status gr_server_step(gr_server* server, double budget_ms);
 gr_status gr_server_poll(gr_server* server, uint64_t id, gr_request_status* out);
 gr_status gr_server_cancel(gr_server* server, uint64_t id);
-/* Copies the finished film (accum, weight) of a request and releases it. */
+/* Copies the finished film (accum, weight) of a request and releases it (a progressive
+ * request's two half-films are summed). */
 gr_status gr_server_take(gr_server* server, uint64_t id, float* accum, float* weight);
 
 #ifdef __cplusplus

@@ -102,3 +102,93 @@ def test_server_admission_and_cancel(gpu):
     s.take(c)
     with pytest.raises(Exception):
         s.submit(st, w.camera, w.integrator, w.width * 4, w.height * 4, 1)  # film larger than the budget
+
+
+def half_films(st, w, passes, gpu):
+    """Even and odd passes rendered pass by pass into two films, as a progressive request
+    splits them."""
+    import ctypes as C
+    films = [g.Film(w.width, w.height, lib=gpu), g.Film(w.width, w.height, lib=gpu)]
+    cam = w.camera.desc()
+    for p in range(passes):
+        prm = st.params(w.integrator, 1, p)
+        gpu.call("gr_render", st.handle, C.byref(cam), C.byref(prm), films[p % 2].handle)
+    return [f.read() for f in films]
+
+
+def rel_mse_estimate(fa, fb):
+    (aa, wa), (ab, wb) = fa, fb
+    ok = (wa > 0) & (wb > 0)
+    a = aa[ok].astype(np.float64) / wa[ok, None]
+    b = ab[ok].astype(np.float64) / wb[ok, None]
+    f = (aa[ok].astype(np.float64) + ab[ok]) / (wa[ok, None].astype(np.float64) + wb[ok, None])
+    return float(np.sum((a - b) ** 2) / 4 / np.sum(f ** 2))
+
+
+def test_server_progressive_stops_at_a_checkpoint(gpu):
+    w = small_workloads(1, seed=11)[0]
+    st = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=2)
+    s = serve.Server(gpu, path_capacity=1 << 16)
+    loose = s.submit(st, w.camera, w.integrator, w.width, w.height, 256, target_rel_mse=10.0)
+    tight = s.submit(st, w.camera, w.integrator, w.width, w.height, 48, target_rel_mse=1e-12)
+    s.run_until_done([loose, tight])
+    sl, stt = s.poll(loose), s.poll(tight)
+    assert sl.state == 2 and sl.passes_done == 8 and 0 < sl.rel_mse <= 10.0
+    assert stt.state == 2 and stt.passes_done == 48 and stt.rel_mse > 1e-12  # capped by spp
+    # The estimate is the two half-films' (even and odd passes) and falls with more passes.
+    est8 = rel_mse_estimate(*half_films(st, w, 8, gpu))
+    np.testing.assert_allclose(sl.rel_mse, est8, rtol=1e-4)
+    fa, fb = half_films(st, w, 48, gpu)
+    np.testing.assert_allclose(stt.rel_mse, rel_mse_estimate(fa, fb), rtol=1e-4)
+    assert stt.rel_mse < sl.rel_mse
+    # take() returns the sum of the half-films.
+    acc, wt = s.take(tight)
+    np.testing.assert_allclose(acc, fa[0] + fb[0], rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(wt, fa[1] + fb[1], rtol=1e-6, atol=1e-7)
+
+
+def test_server_progressive_target_and_mix(gpu):
+    ws = small_workloads(3, seed=12)
+    stages = [g.Stage(w.prims, lib=gpu, environment=w.environment, seed=k) for k, w in enumerate(ws)]
+    w0 = ws[0]
+    est = {n: rel_mse_estimate(*half_films(stages[0], w0, n, gpu)) for n in (8, 16, 32, 64)}
+    target = est[32] * 1.01  # met at 32 passes at the latest
+    want = min(n for n in est if est[n] <= target)
+    alone = serve.Server(gpu, path_capacity=1 << 16)
+    rid = alone.submit(stages[0], w0.camera, w0.integrator, w0.width, w0.height, 64, target_rel_mse=target)
+    alone.run_until_done([rid])
+    sa = alone.poll(rid)
+    assert sa.passes_done == want and sa.rel_mse <= target
+    a_acc, a_w = alone.take(rid)
+    mixed = serve.Server(gpu, path_capacity=1 << 16)
+    ids = [mixed.submit(stages[k], ws[k].camera, ws[k].integrator, ws[k].width, ws[k].height, 6) for k in (1, 2)]
+    mixed.step(1.0)
+    rid0 = mixed.submit(stages[0], w0.camera, w0.integrator, w0.width, w0.height, 64, target_rel_mse=target)
+    ids.append(mixed.submit(stages[1], ws[1].camera, ws[1].integrator, ws[1].width, ws[1].height, 64,
+                            target_rel_mse=1e-12))
+    mixed.run_until_done(ids + [rid0])
+    sm = mixed.poll(rid0)
+    assert sm.passes_done == sa.passes_done and sm.rel_mse == sa.rel_mse
+    m_acc, m_w = mixed.take(rid0)
+    np.testing.assert_array_equal(m_w, a_w)
+    np.testing.assert_allclose(m_acc, a_acc, rtol=1e-6, atol=1e-7)
+    assert mixed.poll(ids[-1]).passes_done == 64
+
+
+def test_server_progressive_cancel_and_budget(gpu):
+    w = small_workloads(1, seed=13)[0]
+    st = g.Stage(w.prims, lib=gpu, environment=w.environment)
+    film_bytes = w.width * w.height * 16
+    s = serve.Server(gpu, memory_budget_bytes=2 * film_bytes, path_capacity=1 << 16)
+    a = s.submit(st, w.camera, w.integrator, w.width, w.height, 64, target_rel_mse=1e-12)
+    b = s.submit(st, w.camera, w.integrator, w.width, w.height, 4)  # waits: a holds two films
+    s.step(0.5)
+    assert s.poll(b).state == 0
+    s.cancel(a)
+    assert s.poll(a).state == 3
+    s.take(a)  # releases both half-films
+    s.run_until_done([b])
+    assert s.poll(b).state == 2
+    s.take(b)
+    with pytest.raises(Exception):
+        s.submit(st, w.camera, w.integrator, w.width, w.height, 4, target_rel_mse=-1.0)
