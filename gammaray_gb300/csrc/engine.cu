@@ -58,7 +58,7 @@ GR_D uint32_t find_unit(const DevUnit* __restrict__ units, uint32_t lo, uint32_t
 
 // Single thread: what to gather and how many paths to issue this iteration.
 __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const DevUnit* __restrict__ units,
-                           const uint32_t* __restrict__ unit_done, uint32_t cap, uint32_t ring) {
+                           const uint32_t* __restrict__ unit_done, uint32_t cap, uint32_t ring, int cur) {
     // Finished units, consecutive from the oldest, grouped by job (pass order kept).
     uint32_t u = c->g_lo, n = 0, groups = 0;
     uint32_t gjob[GATHER_MAX];
@@ -80,6 +80,18 @@ __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const 
         ++n;
         ++u;
     }
+    // Gather in larger batches: a call adds several passes per film tile, so the
+    // film's read-modify-write and the staging prologue are paid once for them.  Wait
+    // until half a capacity of finished paths is waiting, unless the unit list is full,
+    // every appended unit has finished, or the ring would soon limit the fill.
+    const unsigned long long fin = (u < c->units_count ? units[u].prefix : c->paths_total) - c->gather_lo_prefix;
+    const bool flush = n == GATHER_MAX || u == c->units_count || fin >= cap / 2 ||
+                       c->gcur + cap > c->gather_lo_prefix + ring;
+    if (!flush) {
+        n = 0;
+        groups = 0;
+        u = c->g_lo;
+    }
     uint32_t first = 0, tiles = 0;
     for (uint32_t g = 0; g < groups; ++g) {
         c->gather_group_first[g] = first;
@@ -96,13 +108,17 @@ __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const 
     c->gather_tiles = tiles;
     c->g_lo = u;
     c->gather_lo_prefix = u < c->units_count ? units[u].prefix : c->paths_total;
-    unsigned long long live = c->gcur - c->samples_done;
+    // Every live path has its next ray in the current queue (the last shade's survivors).
+    unsigned long long live = c->q[cur];
     unsigned long long room = cap > live ? cap - live : 0;
     unsigned long long rem = c->paths_total - c->gcur;
     unsigned long long lim = c->gather_lo_prefix + ring - c->gcur;  // ring slots free of ungathered samples
     unsigned long long nf = min(room, min(rem, lim));
     c->fill_n = static_cast<uint32_t>(nf);
     c->fill_base = c->gcur;
+    // The fill's camera rays go after the last shade's survivors, at fixed positions.
+    c->fill_qbase = c->q[cur];
+    c->q[cur] += static_cast<uint32_t>(nf);
     if (nf) {  // every unit before g_lo is issued, so the fill starts at or after it
         c->fill_ulo = find_unit(units, c->g_lo, c->units_count, c->gcur);
         c->fill_uhi = find_unit(units, c->fill_ulo, c->units_count, c->gcur + nf - 1);
@@ -154,42 +170,36 @@ __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const Engin
 }
 
 // Starts the next fill_n paths in their ring slots (coalesced: consecutive paths,
-// consecutive slots) and queues their camera rays.
+// consecutive slots) and queues their camera rays at the positions the plan reserved
+// (no atomics).
 __global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob* __restrict__ jobs,
-                                                     const DevUnit* __restrict__ units, uint32_t mask, int cur,
+                                                     const DevUnit* __restrict__ units, uint32_t mask,
                                                      float4* __restrict__ s_hot, uint4* __restrict__ s_cold,
                                                      uint32_t* __restrict__ q_slot, float4* __restrict__ q_o,
                                                      float4* __restrict__ q_d) {
-    const uint32_t n = c->fill_n;
+    const uint32_t n = c->fill_n, qbase = c->fill_qbase;
     const unsigned long long base = c->fill_base;
     const uint32_t ulo = c->fill_ulo, uhi = c->fill_uhi + 1;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += stride) {
-        uint32_t i = b + (threadIdx.x & 31u);
-        bool alive = false;
-        uint32_t slot = 0, job = 0;
-        V3 o = v3zero(), d = v3zero();
-        if (i < n) {
-            unsigned long long p = base + i;
-            slot = static_cast<uint32_t>(p & mask);
-            uint32_t u = find_unit(units, ulo, uhi, p);
-            DevUnit U = units[u];
-            uint32_t pixel = static_cast<uint32_t>(p - U.prefix);
-            job = U.job;
-            const DevJob& J = jobs[job];
-            uint32_t row = pixel / J.width, col = pixel - (pixel / J.width) * J.width;
-            uint64_t key = path_key(J.seed, U.pass, pixel);
-            float s, t;
-            film_sample_point(J.width, J.height, row, col, key, s, t);
-            camera_ray(J.cam, s, t, o, d);
-            s_hot[2 * static_cast<size_t>(slot)] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-            s_hot[2 * static_cast<size_t>(slot) + 1] =
-                make_float4(0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(key)),
-                            __uint_as_float(static_cast<uint32_t>(key >> 32)));
-            s_cold[slot] = make_uint4(u, 0, __float_as_uint(s), __float_as_uint(t));
-            alive = true;
-        }
-        push_ray(alive, &c->q[cur], slot, o, d, job, 0, q_slot, q_o, q_d);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long p = base + i;
+        const uint32_t slot = static_cast<uint32_t>(p & mask);
+        const uint32_t u = find_unit(units, ulo, uhi, p);
+        const DevUnit U = units[u];
+        const uint32_t pixel = static_cast<uint32_t>(p - U.prefix);
+        const DevJob& J = jobs[U.job];
+        const uint32_t row = pixel / J.width, col = pixel - row * J.width;
+        const uint64_t key = path_key(J.seed, U.pass, pixel);
+        float s, t;
+        film_sample_point(J.width, J.height, row, col, key, s, t);
+        V3 o, d;
+        camera_ray(J.cam, s, t, o, d);
+        s_hot[2 * static_cast<size_t>(slot)] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        s_hot[2 * static_cast<size_t>(slot) + 1] = make_float4(
+            0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(key)), __uint_as_float(static_cast<uint32_t>(key >> 32)));
+        s_cold[slot] = make_uint4(u, 0, __float_as_uint(s), __float_as_uint(t));
+        q_slot[qbase + i] = slot;
+        q_o[qbase + i] = make_float4(o.x, o.y, o.z, __uint_as_float(U.job));
+        q_d[qbase + i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
     }
 }
 
@@ -236,8 +246,9 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
     const int nxt = cur ^ 1;
     const uint32_t n = c->q[cur];
     const unsigned lane = threadIdx.x & 31u;
-    // Material-sorted shading (shade_sort.cuh), by (job, material, chosen lobe); misses,
-    // cancelled and display-colour jobs share bucket 0.  Block-uniform chunk loop.
+    // Material-sorted shading (shade_sort.cuh), by code path (chosen lobe type and the
+    // material's lobe types, whatever the job); misses, cancelled and display-colour
+    // jobs share bucket 0.  Block-uniform chunk loop.
     const uint32_t per = chunk_per_thread<EBLOCK, ESHADE_PER_THREAD>(n, gridDim.x);
     const uint32_t chunk = EBLOCK * per;
     for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
@@ -250,7 +261,7 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
             if (!J.live || J.display || k < 0) return 0u;
             float4 kb = s_hot[2 * static_cast<size_t>(q_slot[q]) + 1];
             uint64_t key = (static_cast<uint64_t>(__float_as_uint(kb.w)) << 32) | __float_as_uint(kb.z);
-            return shade_bucket(J.scene, k, uniform01(key, DIM_CAMERA_WALK + 4 * __float_as_uint(q_d[q].w)), jb);
+            return shade_bucket(J.scene, k, uniform01(key, DIM_CAMERA_WALK + 4 * __float_as_uint(q_d[q].w)), 0);
         });
         for (uint32_t e = 0; e < per; ++e) {
             uint32_t i = e * EBLOCK + threadIdx.x;
@@ -310,16 +321,13 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
                     unit = s_cold[slot].x;
                 }
             }
-            // Finished paths count their unit done: one atomic per unit per warp, and one
-            // per warp for the engine total.  The plan and gather kernels that read the
-            // counts and the samples are later launches on the same stream.
-            unsigned fm = __ballot_sync(0xffffffffu, finished);
-            if (fm) {
+            // Finished paths count their unit done: one atomic per unit per warp.  The
+            // plan and gather kernels that read the counts and the samples are later
+            // launches on the same stream.
+            if (__any_sync(0xffffffffu, finished)) {
                 unsigned same = __match_any_sync(0xffffffffu, unit);
                 if (finished && lane == static_cast<unsigned>(__ffs(same) - 1))
                     atomicAdd(unit_done + unit, static_cast<uint32_t>(__popc(same)));
-                if (lane == static_cast<unsigned>(__ffs(fm) - 1))
-                    atomicAdd(&c->samples_done, static_cast<unsigned long long>(__popc(fm)));
             }
             push_ray(alive, &c->q[nxt], slot, new_o, new_d, job, depth + 1, nslot, no, nd);
         }
@@ -418,13 +426,13 @@ gr_status Engine::enqueue_iteration(int cur) {
     EngineCtl* c = ctl_.as<EngineCtl>();
     const uint32_t C = cfg_.capacity;
     const int nxt = cur ^ 1;
-    k_eng_plan<<<1, 1, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), C, ring_);
+    k_eng_plan<<<1, 1, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), C, ring_, cur);
     GR_CUDA_TRY(cudaGetLastError());
     k_eng_gather<<<GATHER_BLOCKS, FILM_TILE * FILM_TILE, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(),
                                                                    s_hot_.as<float4>(), s_cold_.as<uint4>(), ring_ - 1);
     GR_CUDA_TRY(cudaGetLastError());
     int fgrid = grid_for(reinterpret_cast<const void*>(k_eng_fill), EBLOCK, 0, C);
-    k_eng_fill<<<fgrid, EBLOCK, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), ring_ - 1, cur,
+    k_eng_fill<<<fgrid, EBLOCK, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), ring_ - 1,
                                           s_hot_.as<float4>(), s_cold_.as<uint4>(), q_slot_[cur].as<uint32_t>(),
                                           q_o_[cur].as<float4>(), q_d_[cur].as<float4>());
     GR_CUDA_TRY(cudaGetLastError());
@@ -565,8 +573,9 @@ gr_status Engine::run(uint32_t max_pairs, bool& done) {
         }
     } fr{ev};
     const char* done_ptr = reinterpret_cast<const char*>(ctl_.ptr) + offsetof(EngineCtl, done);
-    // Progress guard: every 256 replays the issued / gathered counters must have moved.
-    unsigned long long last_samples = ~0ull;
+    // Progress guard: every 256 replays the traced-ray / gathered counters must have
+    // moved.
+    unsigned long long last_rays = ~0ull;
     uint32_t last_glo = ~0u;
     for (uint32_t k = 0; k < max_pairs; ++k) {
         if (k && (k & 255) == 0) {
@@ -574,11 +583,11 @@ gr_status Engine::run(uint32_t max_pairs, bool& done) {
             GR_CUDA_TRY(cudaStreamSynchronize(st_));
             GR_CUDA_TRY(cudaMemcpy(&c, ctl_.ptr, sizeof(EngineCtl), cudaMemcpyDeviceToHost));
             if (c.done) break;
-            if (c.samples_done == last_samples && c.g_lo == last_glo) {
+            if (c.rays == last_rays && c.g_lo == last_glo) {
                 set_error("engine: no progress over 256 iterations");
                 return GR_ERR_INTERNAL;
             }
-            last_samples = c.samples_done;
+            last_rays = c.rays;
             last_glo = c.g_lo;
         }
         GR_CUDA_TRY(cudaGraphLaunch(graph_, st_));

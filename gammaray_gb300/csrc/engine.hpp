@@ -52,11 +52,11 @@ struct EngineCtl {
     unsigned long long gather_lo_prefix;
     unsigned long long fill_base;
     unsigned long long rays;
-    unsigned long long samples_done;
     uint32_t units_count;
     uint32_t g_lo;  // oldest unit not yet gathered
     uint32_t q[2];
     uint32_t fill_n;
+    uint32_t fill_qbase;  // queue position of the fill's first camera ray
     uint32_t fill_ulo, fill_uhi;  // units holding the paths of this fill: [fill_ulo, fill_uhi]
     uint32_t gather_n;       // units to gather this iteration, grouped by job
     uint32_t gather_groups;  // distinct jobs among them

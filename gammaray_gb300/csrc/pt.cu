@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
 
 
 // Material-sorted shading (shade_sort.cuh): each block sorts its chunk of the queue by
-// (material, chosen lobe), then shades it in that order.
+// code path (chosen lobe type, the material's lobe types), then shades it in that order.
 
 __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t depth,
                                                  const uint32_t* __restrict__ count_in,

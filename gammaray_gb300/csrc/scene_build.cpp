@@ -14,10 +14,12 @@
 // component range; otherwise the interior child of largest surface area is opened
 // until the node is full.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <functional>
 #include <numeric>
+#include <thread>
 
 #include "scene.hpp"
 
@@ -72,13 +74,49 @@ struct BinNode {
     uint32_t first, count;  // component range of the whole subtree
 };
 
+// One component during the binary build: its box, centroid and item index.  The build
+// permutes these records in place (not an index array into the items), so each pass
+// over a node's range reads memory in order.  The high bits of `id` carry the SAH
+// bucket between the bucket count and the partition of the same node.
+struct Rec {
+    Box box;
+    float cen[3];
+    uint32_t id;
+};
+constexpr int ID_BITS = 31 - LEAF_COUNT_BITS;  // components < 2^ID_BITS (checked before the build)
+constexpr uint32_t ID_MASK = (1u << ID_BITS) - 1u;
+
+// The reference's recursive build (geom/bvh.rs:182-382).  Every choice depends only on
+// the records of the node's range and their order, so subtrees are built on separate
+// threads with the same result: nodes come from a shared atomic counter (their
+// numbering is free; the collapse follows child links), and a leaf's first component is
+// its offset in the record array, which is the reference's leaf order.
 class RefBuilder {
   public:
-    std::vector<Item>& items;
+    Rec* base;
     std::vector<BinNode> nodes;
-    std::vector<uint32_t> order;  // item index per ordered component
+    std::atomic<uint32_t> next{0};
+    unsigned threads = 1;
+    int spawn_depth = 0;
+    static constexpr size_t SPAWN_MIN = 8192;     // smaller subtrees stay on their thread
+    static constexpr size_t SPLIT_PASS = 131072;  // larger nodes split their passes
 
-    explicit RefBuilder(std::vector<Item>& it) : items(it) {}
+    RefBuilder(Rec* recs, size_t n) : base(recs), nodes(2 * n) {
+        threads = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+        // SAH splits are uneven: spawn about four subtrees per thread.
+        while (spawn_depth < 8 && (1u << spawn_depth) < 4 * threads) ++spawn_depth;
+        if (threads == 1) spawn_depth = 0;
+    }
+
+    // Runs fn(k, begin, end) over `parts` contiguous pieces of [0, n), on threads.
+    template <class F>
+    static void in_parts(size_t n, unsigned parts, const F& fn) {
+        std::vector<std::thread> th;
+        th.reserve(parts);
+        for (unsigned k = 1; k < parts; ++k) th.emplace_back([&, k] { fn(k, n * k / parts, n * (k + 1) / parts); });
+        fn(0u, size_t(0), n / parts);
+        for (auto& t : th) t.join();
+    }
 
     static int bucket(const Box& cb, const float* c, int dim) {
         const int NB = 12;
@@ -89,20 +127,21 @@ class RefBuilder {
         return static_cast<int>(b);
     }
 
+    // The reference's unstable partition (geom/util.rs): swaps matches to the front.
     template <class P>
-    static size_t partition(uint32_t* s, size_t len, const P& pred) {
+    static size_t partition(Rec* s, size_t len, const P& pred) {
         size_t cursor = 0;
         for (size_t i = 0; i < len; ++i)
             if (pred(s[i])) std::swap(s[i], s[cursor++]);
         return cursor;
     }
 
-    void nth_element(uint32_t* s, size_t len, size_t nth, int dim) {
+    static void nth_element(Rec* s, size_t len, size_t nth, int dim) {
         while (len >= 2) {
             size_t pivot = len / 2;
             std::swap(s[pivot], s[len - 1]);
-            float pv = items[s[len - 1]].cen[dim];
-            size_t fpi = partition(s, len - 1, [&](uint32_t x) { return items[x].cen[dim] < pv; });
+            float pv = s[len - 1].cen[dim];
+            size_t fpi = partition(s, len - 1, [&](const Rec& x) { return x.cen[dim] < pv; });
             std::swap(s[len - 1], s[fpi]);
             if (nth < fpi) {
                 len = fpi - 1;  // one short of the pivot, as geom/util.rs:40
@@ -116,12 +155,65 @@ class RefBuilder {
         }
     }
 
-    int32_t build(uint32_t* s, size_t n) {
-        Box box = Box::empty();
-        for (size_t i = 0; i < n; ++i) box.grow(items[s[i]].box);
+    // Node box and centroid box.  min / max are exact, so a split pass gives the
+    // serial result.
+    void bounds(const Rec* s, size_t n, Box& box, Box& cb) const {
+        box = Box::empty();
+        cb = Box::empty();
+        if (n < SPLIT_PASS || threads == 1) {
+            for (size_t i = 0; i < n; ++i) {
+                box.grow(s[i].box);
+                cb.grow(s[i].cen);
+            }
+            return;
+        }
+        std::vector<Box> pb(threads, Box::empty()), pc(threads, Box::empty());
+        in_parts(n, threads, [&](unsigned k, size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i) {
+                pb[k].grow(s[i].box);
+                pc[k].grow(s[i].cen);
+            }
+        });
+        for (unsigned k = 0; k < threads; ++k) {
+            box.grow(pb[k]);
+            cb.grow(pc[k]);
+        }
+    }
+
+    // SAH bucket of each record (kept in its id's high bits), with per-bucket counts and
+    // boxes.
+    template <int NB>
+    void buckets(Rec* s, size_t n, const Box& cb, int dim, size_t* count, Box* bb) const {
+        auto pass = [&](size_t b, size_t e, size_t* c, Box* x) {
+            for (size_t i = b; i < e; ++i) {
+                int k = bucket(cb, s[i].cen, dim);
+                s[i].id = (s[i].id & ID_MASK) | (static_cast<uint32_t>(k) << ID_BITS);
+                c[k] += 1;
+                x[k].grow(s[i].box);
+            }
+        };
+        for (int b = 0; b < NB; ++b) {
+            count[b] = 0;
+            bb[b] = Box::empty();
+        }
+        if (n < SPLIT_PASS || threads == 1) {
+            pass(0, n, count, bb);
+            return;
+        }
+        std::vector<size_t> pc(threads * NB, 0);
+        std::vector<Box> px(threads * NB, Box::empty());
+        in_parts(n, threads, [&](unsigned k, size_t b, size_t e) { pass(b, e, &pc[k * NB], &px[k * NB]); });
+        for (unsigned k = 0; k < threads; ++k)
+            for (int b = 0; b < NB; ++b) {
+                count[b] += pc[k * NB + b];
+                bb[b].grow(px[k * NB + b]);
+            }
+    }
+
+    int32_t build(Rec* s, size_t n, int depth = 0) {
+        Box box, cb;
+        bounds(s, n, box, cb);
         if (n == 1) return leaf(s, n, box);
-        Box cb = Box::empty();
-        for (size_t i = 0; i < n; ++i) cb.grow(items[s[i]].cen);
         int dim = cb.max_extent();
         if (cb.lo[dim] == cb.hi[dim]) return leaf(s, n, box);
         size_t mid;
@@ -129,15 +221,10 @@ class RefBuilder {
             mid = n / 2;
             nth_element(s, n, mid, dim);
         } else {
-            const int NB = 12;
-            size_t count[NB] = {0};
+            constexpr int NB = 12;
+            size_t count[NB];
             Box bb[NB];
-            for (int b = 0; b < NB; ++b) bb[b] = Box::empty();
-            for (size_t i = 0; i < n; ++i) {
-                int b = bucket(cb, items[s[i]].cen, dim);
-                count[b] += 1;
-                bb[b].grow(items[s[i]].box);
-            }
+            buckets<NB>(s, n, cb, dim, count, bb);
             float cost[NB - 1];
             for (int i = 0; i < NB - 1; ++i) {
                 Box b0 = Box::empty(), b1 = Box::empty();
@@ -161,14 +248,22 @@ class RefBuilder {
                     min_b = i;
                 }
             if (n > 255 || min_cost < static_cast<float>(n)) {
-                mid = partition(s, n, [&](uint32_t x) { return bucket(cb, items[x].cen, dim) <= min_b; });
+                const uint32_t mb = static_cast<uint32_t>(min_b);
+                mid = partition(s, n, [&](const Rec& x) { return (x.id >> ID_BITS) <= mb; });
             } else {
                 mid = n / 2;
                 nth_element(s, n, mid, dim);
             }
         }
-        int32_t c0 = build(s, mid);
-        int32_t c1 = build(s + mid, n - mid);
+        int32_t c0, c1;
+        if (depth < spawn_depth && mid >= SPAWN_MIN && n - mid >= SPAWN_MIN) {
+            std::thread left([&] { c0 = build(s, mid, depth + 1); });
+            c1 = build(s + mid, n - mid, depth + 1);
+            left.join();
+        } else {
+            c0 = build(s, mid, depth + 1);
+            c1 = build(s + mid, n - mid, depth + 1);
+        }
         BinNode nd;
         nd.box = nodes[c0].box;
         nd.box.grow(nodes[c1].box);
@@ -176,19 +271,22 @@ class RefBuilder {
         nd.child[1] = c1;
         nd.first = nodes[c0].first;
         nd.count = nodes[c0].count + nodes[c1].count;
-        nodes.push_back(nd);
-        return static_cast<int32_t>(nodes.size() - 1);
+        return put(nd);
     }
 
-    int32_t leaf(uint32_t* s, size_t n, const Box& box) {
+    int32_t leaf(Rec* s, size_t n, const Box& box) {
         BinNode nd;
         nd.box = box;
         nd.child[0] = nd.child[1] = -1;
-        nd.first = static_cast<uint32_t>(order.size());
+        nd.first = static_cast<uint32_t>(s - base);
         nd.count = static_cast<uint32_t>(n);
-        for (size_t i = 0; i < n; ++i) order.push_back(s[i]);
-        nodes.push_back(nd);
-        return static_cast<int32_t>(nodes.size() - 1);
+        return put(nd);
+    }
+
+    int32_t put(const BinNode& nd) {
+        uint32_t k = next.fetch_add(1, std::memory_order_relaxed);
+        nodes[k] = nd;
+        return static_cast<int32_t>(k);
     }
 };
 
@@ -233,19 +331,18 @@ class Collapser {
     // Emits the node for `c` (which must be expandable, or the root) and returns its
     // index and the worst-case stack use of its subtree.
     uint32_t emit(const Cand& c, uint32_t& stack_use) {
-        std::vector<Cand> cands;
+        Cand cands[8];
+        uint32_t nc = 0;
         if (expandable(c)) {
-            Cand a, b;
-            expand(c, a, b);
-            cands.push_back(a);
-            cands.push_back(b);
+            expand(c, cands[0], cands[1]);
+            nc = 2;
         } else {
-            cands.push_back(c);
+            cands[nc++] = c;
         }
-        while (cands.size() < W) {
+        while (nc < W) {
             int best = -1;
             float best_area = -1.0f;
-            for (size_t i = 0; i < cands.size(); ++i) {
+            for (uint32_t i = 0; i < nc; ++i) {
                 if (!expandable(cands[i])) continue;
                 float a = cands[i].box.area();
                 if (!(a <= best_area)) {
@@ -256,8 +353,10 @@ class Collapser {
             if (best < 0) break;
             Cand a, b;
             expand(cands[best], a, b);
+            for (uint32_t i = nc; i > static_cast<uint32_t>(best) + 1; --i) cands[i] = cands[i - 1];
             cands[best] = a;
-            cands.insert(cands.begin() + best + 1, b);
+            cands[best + 1] = b;
+            ++nc;
         }
         uint32_t idx = static_cast<uint32_t>(out.size() / (8 * W));
         out.resize(out.size() + 8 * W, 0.0f);
@@ -266,7 +365,7 @@ class Collapser {
             float* node = &out[static_cast<size_t>(idx) * 8 * W];
             int32_t ref;
             Box bx = Box::empty();  // empty slots never hit
-            if (j < cands.size()) {
+            if (j < nc) {
                 const Cand& k = cands[j];
                 bx = k.box;
                 if (!expandable(k)) {
@@ -286,14 +385,14 @@ class Collapser {
             }
             std::memcpy(&node[6 * W + j], &ref, 4);
         }
-        stack_use = static_cast<uint32_t>(cands.size()) - 1 + sub_max;
+        stack_use = nc - 1 + sub_max;
         return idx;
     }
 };
 
 }  // namespace
 
-bool build_material(const gr_material_desc& d, DevMaterial& m, std::string& err) {
+static bool build_lobes(const gr_material_desc& d, DevMaterial& m, std::string& err) {
     std::memset(&m, 0, sizeof(m));
     auto set3 = [](float* dst, V3 v) {
         dst[0] = v.x;
@@ -375,6 +474,14 @@ bool build_material(const gr_material_desc& d, DevMaterial& m, std::string& err)
     return true;
 }
 
+bool build_material(const gr_material_desc& d, DevMaterial& m, std::string& err) {
+    if (!build_lobes(d, m, err)) return false;
+    // The shading sort's key for the material's mixture: its lobe count and types.
+    m.lobe_set = static_cast<uint32_t>(m.n_lobes);
+    for (int j = 0; j < m.n_lobes; ++j) m.lobe_set = m.lobe_set * 8u + static_cast<uint32_t>(m.lobe[j].type);
+    return true;
+}
+
 static void put_bits(float* dst, uint32_t v) { std::memcpy(dst, &v, 4); }
 
 bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
@@ -401,6 +508,12 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
     }
     // Component list in prim order (Bvh::build, bvh.rs:340-350), with mesh data offsets.
     std::vector<Item> items;
+    {
+        size_t total = 0;
+        for (uint32_t p = 0; p < desc.num_prims && desc.prims; ++p)
+            total += desc.prims[p].kind == GR_PRIM_MESH ? desc.prims[p].num_tris : 1;
+        items.reserve(total);
+    }
     std::vector<uint32_t> vbase(desc.num_prims, 0), nbase(desc.num_prims, 0), ubase(desc.num_prims, 0);
     uint32_t nrm_total = 0, uv_total = 0;
     for (uint32_t p = 0; p < desc.num_prims; ++p) {
@@ -535,18 +648,28 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
             }
         }
     } else {
-        RefBuilder rb(items);
-        rb.nodes.reserve(2 * items.size());
-        rb.order.reserve(items.size());
-        std::vector<uint32_t> idx(items.size());
-        std::iota(idx.begin(), idx.end(), 0u);
-        int32_t root = rb.build(idx.data(), idx.size());
+        std::vector<Rec> recs(items.size());
+        for (size_t k = 0; k < items.size(); ++k) {
+            recs[k].box = items[k].box;
+            std::memcpy(recs[k].cen, items[k].cen, sizeof(recs[k].cen));
+            recs[k].id = static_cast<uint32_t>(k);
+        }
+        RefBuilder rb(recs.data(), recs.size());
+        int32_t root = rb.build(recs.data(), recs.size());
+        rb.nodes.resize(rb.next.load());
         out.num_binary_nodes = rb.nodes.size();
         std::vector<Box> comp_box(items.size());
-        for (size_t k = 0; k < rb.order.size(); ++k) {
-            comp_box[k] = items[rb.order[k]].box;
-            put_record(k, items[rb.order[k]]);
-        }
+        auto records = [&](unsigned, size_t b, size_t e) {
+            for (size_t k = b; k < e; ++k) {
+                const Item& it = items[recs[k].id & ID_MASK];
+                comp_box[k] = it.box;
+                put_record(k, it);
+            }
+        };
+        if (recs.size() >= RefBuilder::SPLIT_PASS && rb.threads > 1)
+            RefBuilder::in_parts(recs.size(), rb.threads, records);
+        else
+            records(0, 0, recs.size());
         Collapser col(rb.nodes, comp_box, W, L, out.nodes);
         uint32_t su = 0;
         Cand rc = col.of_bin(root);

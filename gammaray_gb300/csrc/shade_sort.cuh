@@ -1,8 +1,9 @@
 // Block-local counting sort of a chunk of queue positions by a small bucket id.  The
 // shading kernels use it to run coherent warps: a block sorts its chunk of the queue by
-// (material, chosen lobe) in shared memory, then shades the chunk in that order, so a
-// warp runs one material's one lobe sampler instead of a mix of all of them.  The order
-// only decides which thread handles which queue entry; no result depends on it.
+// code path (the chosen lobe's type and the material's lobe types) in shared memory,
+// then shades the chunk in that order, so a warp runs one lobe sampler and one mixture
+// instead of a mix of all of them.  The order only decides which thread handles which
+// queue entry; no result depends on it.
 #pragma once
 
 #include "common.cuh"
@@ -102,16 +103,21 @@ GR_D void sort_chunk(const SortView& sm, uint32_t cn, uint32_t per, F bucket_of)
     __syncthreads();
 }
 
-// Bucket of a shading entry: 0 when the ray escaped, else a hash of the hit's material,
-// of `salt` (a job, a walk kind) and of the lobe Material::sample_world will pick from
-// the uniform u0 (material.rs:151-153).
+// Bucket of a shading entry: 0 when the ray escaped.  Otherwise the code path
+// Material::sample_world will take: the type of the lobe it picks from the uniform u0
+// (material.rs:151-153) and the material's lobe types, which the mixture's f / pdf loop
+// runs through.  Six lobe types use buckets 1-30 (5 each), the lobe set and `salt` (a
+// walk kind) choosing among the 5.  Materials of any scene or job with the same lobe
+// types share a bucket.
 GR_D uint32_t shade_bucket(const DeviceScene& s, int32_t k, float u0, uint32_t salt) {
     if (k < 0) return 0;
     uint32_t prim = __float_as_uint(__ldg(s.prims + 3 * static_cast<size_t>(k)).w);
-    uint32_t mat = __ldg(s.prim_material + prim);
-    uint32_t nl = static_cast<uint32_t>(s.materials[mat].n_lobes);
-    uint32_t r = nl ? range_index(u0, nl) : 0;
-    return 1 + ((salt * 0x9E3779B1u) ^ (mat * MAX_LOBES + r)) % (SORT_BUCKETS - 1);
+    const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
+    const uint32_t nl = static_cast<uint32_t>(m.n_lobes);
+    if (nl == 0) return 1;
+    const uint32_t r = range_index(u0, nl);
+    const uint32_t chosen = static_cast<uint32_t>(m.lobe[r].type);
+    return 1 + 5 * (chosen % 6) + ((m.lobe_set + salt) * 0x9E3779B1u >> 16) % 5;
 }
 
 }  // namespace gr

@@ -383,8 +383,9 @@ typedef struct gr_job {
 } gr_job;
 
 typedef struct gr_batch_options {
-    uint32_t path_capacity;  /* paths in flight; 0 = autotuned */
-    uint32_t block_size;     /* threads per block; 0 = autotuned */
+    uint32_t path_capacity;  /* paths in flight; 0 = the smallest power of two holding the
+                                batch's samples, between 1 M and 64 M */
+    uint32_t block_size;     /* extension kernel threads per block; 0 = 128 */
     uint32_t use_graph;      /* capture the bounce loop in a CUDA graph */
     uint32_t reserved;
 } gr_batch_options;
@@ -403,7 +404,7 @@ typedef struct gr_server gr_server;
 typedef struct gr_server_options {
     uint64_t memory_budget_bytes; /* admission limit for films; 0 = 90% of free device memory */
     uint32_t max_active;          /* concurrent renders; 0 = unlimited */
-    uint32_t path_capacity;       /* paths in flight; 0 = default */
+    uint32_t path_capacity;       /* paths in flight; 0 = 64 M (about 18 GB of queues and path state) */
     uint32_t bvh_width;           /* BVH width of the scenes served (2, 4, 8); 0 = 4 */
     uint32_t block_size;          /* extension kernel block size; 0 = 128 */
 } gr_server_options;

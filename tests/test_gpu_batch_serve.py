@@ -46,7 +46,7 @@ def test_batch_autotune_and_display(gpu):
         integ = g.DisplayColorIntegrator() if k == 0 else w.integrator
         jobs.append(batch.Job(st, w.camera, integ, g.Film(w.width, w.height, lib=gpu), w.spp))
     opt = batch.autotune(jobs, gpu)
-    assert opt.path_capacity in (1 << 21, 1 << 23, 1 << 24) and opt.block_size in (128, 256)
+    assert opt.path_capacity in (1 << 23, 1 << 25, 1 << 26) and opt.block_size in (128, 256)
     for j in jobs:
         assert j.film.passes() == 0  # trials render into scratch films
     batch.render_batch(jobs, gpu, opt.path_capacity, opt.block_size)
