@@ -19,6 +19,7 @@
 #include <cstring>
 #include <functional>
 #include <numeric>
+#include <pthread.h>
 #include <thread>
 
 #include "scene.hpp"
@@ -83,30 +84,73 @@ struct Rec {
     float cen[3];
     uint32_t id;
 };
+// A thread with a large stack: the reference's build recurses once per tree level, and
+// a skewed split (one component against the rest) adds a level per component.  64 MB
+// holds about 70,000 levels; the memory is committed only as it is touched.
+class BuildThread {
+  public:
+    static constexpr size_t STACK = size_t(64) << 20;
+    explicit BuildThread(std::function<void()> fn) : fn_(std::move(fn)) {
+        pthread_attr_t at;
+        pthread_attr_init(&at);
+        pthread_attr_setstacksize(&at, STACK);
+        ok_ = pthread_create(&t_, &at, &BuildThread::entry, this) == 0;
+        pthread_attr_destroy(&at);
+        if (!ok_) fn_();  // no thread: run here
+    }
+    void join() {
+        if (ok_) pthread_join(t_, nullptr);
+        ok_ = false;
+    }
+    ~BuildThread() { join(); }
+
+  private:
+    static void* entry(void* self) {
+        static_cast<BuildThread*>(self)->fn_();
+        return nullptr;
+    }
+    std::function<void()> fn_;
+    pthread_t t_{};
+    bool ok_ = false;
+};
+
 constexpr int ID_BITS = 31 - LEAF_COUNT_BITS;  // components < 2^ID_BITS (checked before the build)
 constexpr uint32_t ID_MASK = (1u << ID_BITS) - 1u;
 
 // The reference's recursive build (geom/bvh.rs:182-382).  Every choice depends only on
 // the records of the node's range and their order, so subtrees are built on separate
-// threads with the same result: nodes come from a shared atomic counter (their
-// numbering is free; the collapse follows child links), and a leaf's first component is
-// its offset in the record array, which is the reference's leaf order.
+// threads with the same result.  Node numbering is free (the collapse follows child
+// links): each thread takes nodes from its own chunks of CHUNK slots, so a subtree's
+// nodes sit together.  A leaf's first component is its offset in the record array, which
+// is the reference's leaf order.
 class RefBuilder {
   public:
+    static constexpr size_t SPAWN_MIN = 2048;    // smaller subtrees stay on their thread
+    static constexpr size_t SPLIT_PASS = 32768;  // larger nodes split their passes
+    static constexpr uint32_t CHUNK = 1024;      // node slots taken at a time by a thread
+
+    // A thread's current chunk of node slots.
+    struct Alloc {
+        uint32_t next = 0, end = 0, used = 0;
+    };
+
     Rec* base;
     std::vector<BinNode> nodes;
     std::atomic<uint32_t> next{0};
+    std::atomic<uint64_t> used{0};
     unsigned threads = 1;
     int spawn_depth = 0;
-    static constexpr size_t SPAWN_MIN = 8192;     // smaller subtrees stay on their thread
-    static constexpr size_t SPLIT_PASS = 131072;  // larger nodes split their passes
 
-    RefBuilder(Rec* recs, size_t n) : base(recs), nodes(2 * n) {
+    RefBuilder(Rec* recs, size_t n) : base(recs) {
         threads = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
         // SAH splits are uneven: spawn about four subtrees per thread.
         while (spawn_depth < 8 && (1u << spawn_depth) < 4 * threads) ++spawn_depth;
-        if (threads == 1) spawn_depth = 0;
+        if (threads == 1 || n < 2 * SPAWN_MIN) spawn_depth = 0;
+        // At most 2n - 1 nodes, plus the unused tail of each thread's last chunk.
+        nodes.resize(2 * n + (static_cast<size_t>(2) << spawn_depth) * CHUNK);
     }
+
+    uint64_t node_count() const { return used.load(); }
 
     // Runs fn(k, begin, end) over `parts` contiguous pieces of [0, n), on threads.
     template <class F>
@@ -180,51 +224,74 @@ class RefBuilder {
         }
     }
 
-    // SAH bucket of each record (kept in its id's high bits), with per-bucket counts and
-    // boxes.
+    // SAH bucket of each record (kept in its id's high bits), with per-bucket counts,
+    // boxes and centroid bounds (from which the children's bounds follow exactly).
     template <int NB>
-    void buckets(Rec* s, size_t n, const Box& cb, int dim, size_t* count, Box* bb) const {
-        auto pass = [&](size_t b, size_t e, size_t* c, Box* x) {
+    void buckets(Rec* s, size_t n, const Box& cb, int dim, size_t* count, Box* bb, Box* cbb) const {
+        auto pass = [&](size_t b, size_t e, size_t* c, Box* x, Box* y) {
             for (size_t i = b; i < e; ++i) {
                 int k = bucket(cb, s[i].cen, dim);
                 s[i].id = (s[i].id & ID_MASK) | (static_cast<uint32_t>(k) << ID_BITS);
                 c[k] += 1;
                 x[k].grow(s[i].box);
+                y[k].grow(s[i].cen);
             }
         };
         for (int b = 0; b < NB; ++b) {
             count[b] = 0;
             bb[b] = Box::empty();
+            cbb[b] = Box::empty();
         }
         if (n < SPLIT_PASS || threads == 1) {
-            pass(0, n, count, bb);
+            pass(0, n, count, bb, cbb);
             return;
         }
         std::vector<size_t> pc(threads * NB, 0);
-        std::vector<Box> px(threads * NB, Box::empty());
-        in_parts(n, threads, [&](unsigned k, size_t b, size_t e) { pass(b, e, &pc[k * NB], &px[k * NB]); });
+        std::vector<Box> px(threads * NB, Box::empty()), py(threads * NB, Box::empty());
+        in_parts(n, threads,
+                 [&](unsigned k, size_t b, size_t e) { pass(b, e, &pc[k * NB], &px[k * NB], &py[k * NB]); });
         for (unsigned k = 0; k < threads; ++k)
             for (int b = 0; b < NB; ++b) {
                 count[b] += pc[k * NB + b];
                 bb[b].grow(px[k * NB + b]);
+                cbb[b].grow(py[k * NB + b]);
             }
     }
 
-    int32_t build(Rec* s, size_t n, int depth = 0) {
+    int32_t build(Rec* s, size_t n) {
+        int32_t root = -1;
+        BuildThread t([&] {
+            Alloc a;
+            root = build(s, n, 0, a, nullptr);
+            used += a.used;
+        });
+        t.join();
+        return root;
+    }
+
+    // `known`, when given, holds the range's box and centroid box.
+    int32_t build(Rec* s, size_t n, int depth, Alloc& a, const Box* known) {
         Box box, cb;
-        bounds(s, n, box, cb);
-        if (n == 1) return leaf(s, n, box);
+        if (known) {
+            box = known[0];
+            cb = known[1];
+        } else {
+            bounds(s, n, box, cb);
+        }
+        if (n == 1) return leaf(s, n, box, a);
         int dim = cb.max_extent();
-        if (cb.lo[dim] == cb.hi[dim]) return leaf(s, n, box);
+        if (cb.lo[dim] == cb.hi[dim]) return leaf(s, n, box, a);
         size_t mid;
+        Box kids[4] = {Box::empty(), Box::empty(), Box::empty(), Box::empty()};  // box, centroid box per side
+        bool kids_known = false;
         if (n <= 4) {
             mid = n / 2;
             nth_element(s, n, mid, dim);
         } else {
             constexpr int NB = 12;
             size_t count[NB];
-            Box bb[NB];
-            buckets<NB>(s, n, cb, dim, count, bb);
+            Box bb[NB], cbb[NB];
+            buckets<NB>(s, n, cb, dim, count, bb, cbb);
             float cost[NB - 1];
             for (int i = 0; i < NB - 1; ++i) {
                 Box b0 = Box::empty(), b1 = Box::empty();
@@ -250,19 +317,31 @@ class RefBuilder {
             if (n > 255 || min_cost < static_cast<float>(n)) {
                 const uint32_t mb = static_cast<uint32_t>(min_b);
                 mid = partition(s, n, [&](const Rec& x) { return (x.id >> ID_BITS) <= mb; });
+                for (int b = 0; b < NB; ++b) {
+                    Box* side = b <= min_b ? kids : kids + 2;
+                    side[0].grow(bb[b]);
+                    side[1].grow(cbb[b]);
+                }
+                kids_known = true;
             } else {
                 mid = n / 2;
                 nth_element(s, n, mid, dim);
             }
         }
+        const Box* k0 = kids_known ? kids : nullptr;
+        const Box* k1 = kids_known ? kids + 2 : nullptr;
         int32_t c0, c1;
         if (depth < spawn_depth && mid >= SPAWN_MIN && n - mid >= SPAWN_MIN) {
-            std::thread left([&] { c0 = build(s, mid, depth + 1); });
-            c1 = build(s + mid, n - mid, depth + 1);
+            BuildThread left([&] {
+                Alloc la;
+                c0 = build(s, mid, depth + 1, la, k0);
+                used += la.used;
+            });
+            c1 = build(s + mid, n - mid, depth + 1, a, k1);
             left.join();
         } else {
-            c0 = build(s, mid, depth + 1);
-            c1 = build(s + mid, n - mid, depth + 1);
+            c0 = build(s, mid, depth + 1, a, k0);
+            c1 = build(s + mid, n - mid, depth + 1, a, k1);
         }
         BinNode nd;
         nd.box = nodes[c0].box;
@@ -271,22 +350,26 @@ class RefBuilder {
         nd.child[1] = c1;
         nd.first = nodes[c0].first;
         nd.count = nodes[c0].count + nodes[c1].count;
-        return put(nd);
+        return put(nd, a);
     }
 
-    int32_t leaf(Rec* s, size_t n, const Box& box) {
+    int32_t leaf(Rec* s, size_t n, const Box& box, Alloc& a) {
         BinNode nd;
         nd.box = box;
         nd.child[0] = nd.child[1] = -1;
         nd.first = static_cast<uint32_t>(s - base);
         nd.count = static_cast<uint32_t>(n);
-        return put(nd);
+        return put(nd, a);
     }
 
-    int32_t put(const BinNode& nd) {
-        uint32_t k = next.fetch_add(1, std::memory_order_relaxed);
-        nodes[k] = nd;
-        return static_cast<int32_t>(k);
+    int32_t put(const BinNode& nd, Alloc& a) {
+        if (a.next == a.end) {
+            a.next = next.fetch_add(CHUNK, std::memory_order_relaxed);
+            a.end = a.next + CHUNK;
+        }
+        nodes[a.next] = nd;
+        ++a.used;
+        return static_cast<int32_t>(a.next++);
     }
 };
 
@@ -656,8 +739,7 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
         }
         RefBuilder rb(recs.data(), recs.size());
         int32_t root = rb.build(recs.data(), recs.size());
-        rb.nodes.resize(rb.next.load());
-        out.num_binary_nodes = rb.nodes.size();
+        out.num_binary_nodes = rb.node_count();
         std::vector<Box> comp_box(items.size());
         auto records = [&](unsigned, size_t b, size_t e) {
             for (size_t k = b; k < e; ++k) {
