@@ -363,32 +363,47 @@ GR_D float light_dir_pdf(const Frame& f, V3 w) {
 
 GR_D float remap0(float x) { return x != 0.0f ? x : 1.0f; }
 
-constexpr int MAX_WALK = 16;
+// One walk's part of the MIS sum for a connection at its vertex n - 1.  With the
+// connection's reverse pdfs rev1 (vertex n - 1) and rev2 (vertex n - 2),
+//   a = remap0(rev1) / remap0(afwd[n-1]),  b = remap0(rev2) / remap0(afwd[n-2]),
+//   part = [cond(n-1)] a^2 + (a b)^2 ([cond(n-2)] + P(n-3)),
+// where P(m) = q(m)^2 ([cond(m)] + P(m-1)), q(m) = remap0(arev[m]) / remap0(afwd[m]), sums
+// the vertices whose reverse pdfs the connection leaves alone.  This is the chained-ratio
+// loop (each ratio squared and summed unless the vertex or the one before it is a delta
+// vertex) regrouped, so a weight costs O(1) and P advances by one step per vertex.
+// skip0: the camera walk's k = 0 term (the light-tracing strategy) is left out.
+struct WalkMis {
+    VPdf v1{0.0f, 0.0f, false}, v2{0.0f, 0.0f, false}, v3{0.0f, 0.0f, false};  // vertices n-1, n-2, n-3
+    float P = 0.0f;  // P(n - 3)
+    uint32_t n = 0;
+    bool skip0 = false;
 
-// Weight of strategy (c, l) from both walks' vertex pdfs, with the reverse pdfs the
-// connection implies for the last vertex of each walk and the one before it.
-// lt_possible: the light-tracing strategy can produce this path.
-GR_D float mis_weight(const VPdf* cp, const VPdf* lp, uint32_t c, uint32_t l, float z_rev, float zm_rev, float y_rev,
-                      float ym_rev, bool lt_possible) {
-    float sum = 0.0f, r = 1.0f;
-    for (uint32_t k = c; k-- > 0;) {
-        float rev = k + 1 == c ? z_rev : (k + 2 == c ? zm_rev : cp[k].arev);
-        r *= remap0(rev) / remap0(cp[k].afwd);
-        bool here = k + 1 == c ? false : cp[k].delta;
-        bool before = k == 0 ? false : cp[k - 1].delta;
-        if (k == 0 && !lt_possible) continue;
-        if (!here && !before) sum += r * r;
+    GR_D bool cond_interior(uint32_t k, const VPdf& v, const VPdf& before) const {
+        return !v.delta && !(k >= 1 && before.delta) && !(k == 0 && skip0);
     }
-    r = 1.0f;
-    for (uint32_t k = l; k-- > 0;) {
-        float rev = k + 1 == l ? y_rev : (k + 2 == l ? ym_rev : lp[k].arev);
-        r *= remap0(rev) / remap0(lp[k].afwd);
-        bool here = k + 1 == l ? false : lp[k].delta;
-        bool before = k == 0 ? false : lp[k - 1].delta;
-        if (!here && !before) sum += r * r;
+    // Moves the connection one vertex out: v is the record of vertex n.
+    GR_D void push(const VPdf& v) {
+        if (n >= 2) {  // vertex n - 2 becomes interior
+            float q = remap0(v2.arev) / remap0(v2.afwd);
+            P = q * q * ((cond_interior(n - 2, v2, v3) ? 1.0f : 0.0f) + P);
+        }
+        v3 = v2;
+        v2 = v1;
+        v1 = v;
+        ++n;
     }
-    return 1.0f / (1.0f + sum);
-}
+    GR_D float part(float rev1, float rev2) const {
+        if (n == 0) return 0.0f;
+        float a = remap0(rev1) / remap0(v1.afwd);
+        bool c1 = n == 1 ? !skip0 : !v2.delta;
+        float sum = c1 ? a * a : 0.0f;
+        if (n >= 2) {
+            float ab = a * (remap0(rev2) / remap0(v2.afwd));
+            sum += ab * ab * ((cond_interior(n - 2, v2, v3) ? 1.0f : 0.0f) + P);
+        }
+        return sum;
+    }
+};
 
 struct VPos {
     V3 point, ng;
@@ -398,10 +413,49 @@ GR_D VPos load_pos(const Verts& vs, uint32_t k, uint32_t slot) {
     return VPos{V3{f0.x, f0.y, f0.z}, V3{f5.x, f5.y, f5.z}};
 }
 
-// MIS weight of camera strategy (c >= 1, l >= 0) with a non-zero connection.
-GR_D float strategy_weight(const DeviceScene& s, const Verts& vs, uint32_t i, const VPdf* cp, const VPdf* lp,
-                           uint32_t c, uint32_t l, const Vtx& z, const Vtx* y, bool lt_possible) {
-    const DevMaterial& zm = s.materials[z.material];
+// A walk vertex's BSDF toward a connection: the value f(wi, wo) (material.rs:66-93) and,
+// for the MIS weights, pdf(wi, wo) and pdf(wo, wi) (material.rs:95-119), each summed in
+// the same order as f_world / pdf_world.  One out-of-line copy serves every call site of
+// the connection kernel, whose divergent warps otherwise miss in the instruction cache
+// on many inlined copies of the Disney mixture.
+struct VEval {
+    V3 f;
+    float pdf_fwd, pdf_rev;
+};
+static __device__ __noinline__ VEval eval_vertex(const DevMaterial& m, V3 wi, V3 wo, const Frame& fr, bool c2l,
+                                                 bool pdfs) {
+    VEval e{v3zero(), 0.0f, 0.0f};
+    V3 il = world_to_local(wi, fr.tangent, fr.binormal, fr.normal);
+    V3 ol = world_to_local(wo, fr.tangent, fr.binormal, fr.normal);
+    bool refl = (dot(wi, fr.geom_normal) * dot(wo, fr.geom_normal)) > 0.0f;
+    float pf = 0.0f, pr = 0.0f;
+#pragma unroll 1
+    for (int k = 0; k < m.n_lobes; ++k) {
+        const DevLobe& L = m.lobe[k];
+        if ((refl && (L.kind & LOBE_REFLECTION)) || (!refl && (L.kind & LOBE_TRANSMISSION)))
+            e.f = e.f + lobe_f(L, il, ol, c2l);
+        // Both directions through one call site (one inlined copy of the lobe pdfs).
+#pragma unroll 1
+        for (int d = 0; pdfs && d < 2; ++d) {
+            float q = lobe_pdf(L, d ? ol : il, d ? il : ol);
+            if (d) pr += q;
+            else pf += q;
+        }
+    }
+    if (pdfs && m.n_lobes) {
+        const float n = static_cast<float>(m.n_lobes);
+        e.pdf_fwd = il.z == 0.0f ? 0.0f : pf / n;
+        e.pdf_rev = ol.z == 0.0f ? 0.0f : pr / n;
+    }
+    return e;
+}
+
+// MIS weight of camera strategy (c >= 1, l >= 0) with a non-zero connection; cw and lw
+// stand at c and l vertices.  For l >= 1, ez and ey are the connection's evaluations at
+// z (camera side, toward y) and y (light side, toward z; for l = 1 the light's
+// direction pdf in pdf_fwd).
+GR_D float strategy_weight(const DeviceScene& s, const Verts& vs, uint32_t i, const WalkMis& cw, const WalkMis& lw,
+                           uint32_t c, uint32_t l, const Vtx& z, const Vtx* y, const VEval& ez, const VEval& ey) {
     float z_rev = 0.0f, zm_rev = 0.0f, y_rev = 0.0f, ym_rev = 0.0f;
     if (l == 0) {  // the camera walk hit a light
         z_rev = light_point_pdf(s, z.prim);
@@ -410,21 +464,70 @@ GR_D float strategy_weight(const DeviceScene& s, const Verts& vs, uint32_t i, co
             zm_rev = to_area(light_dir_pdf(z.frame, z.incoming), z.point, zp.point, zp.ng);
         }
     } else {
-        const DevMaterial& ym = s.materials[y->material];
-        V3 w_yz = normalized(z.point - y->point);
-        float pz = l == 1 ? light_dir_pdf(y->frame, w_yz) : pdf_world(ym, y->incoming, w_yz, y->frame);
-        z_rev = to_area(pz, y->point, z.point, z.frame.geom_normal);
+        z_rev = to_area(ey.pdf_fwd, y->point, z.point, z.frame.geom_normal);
         if (c >= 2) {
             VPos zp = load_pos(vs, c - 2, 2 * i);
-            zm_rev = to_area(pdf_world(zm, -w_yz, z.incoming, z.frame), z.point, zp.point, zp.ng);
+            zm_rev = to_area(ez.pdf_rev, z.point, zp.point, zp.ng);
         }
-        y_rev = to_area(pdf_world(zm, z.incoming, -w_yz, z.frame), z.point, y->point, y->frame.geom_normal);
+        y_rev = to_area(ez.pdf_fwd, z.point, y->point, y->frame.geom_normal);
         if (l >= 2) {
             VPos yp = load_pos(vs, l - 2, 2 * i + 1);
-            ym_rev = to_area(pdf_world(ym, w_yz, y->incoming, y->frame), y->point, yp.point, yp.ng);
+            ym_rev = to_area(ey.pdf_rev, y->point, yp.point, yp.ng);
         }
     }
-    return mis_weight(cp, lp, c, l, z_rev, zm_rev, y_rev, ym_rev, lt_possible);
+    return 1.0f / (1.0f + cw.part(z_rev, zm_rev) + lw.part(y_rev, ym_rev));
+}
+
+// ------------------------------------------ connection order: paths by walk lengths
+// The connection kernel runs a thread per path through loops over both walks' vertices;
+// paths of equal (camera, light) vertex counts make warps of equal trip counts.  A
+// counting sort of the path indices by that pair (17 x 17 buckets, walks <= 16) gives
+// the order; which thread handles which path changes no result.
+constexpr uint32_t LEN_BUCKETS = 17 * 17;
+
+GR_D uint32_t len_bucket(const uint32_t* vcount, const uint32_t* flags, uint32_t i) {
+    if (flags[i] & F_SKIP) return 0;
+    return min(vcount[2 * i], 16u) * 17u + min(vcount[2 * i + 1], 16u);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_bdpt_len_count(uint32_t n, const uint32_t* __restrict__ vcount,
+                                                          const uint32_t* __restrict__ flags, uint32_t* hist) {
+    __shared__ uint32_t h[LEN_BUCKETS];
+    for (uint32_t b = threadIdx.x; b < LEN_BUCKETS; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[len_bucket(vcount, flags, i)], 1u);
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < LEN_BUCKETS; b += blockDim.x)
+        if (h[b]) atomicAdd(&hist[b], h[b]);
+}
+
+// One thread: bucket counts -> first positions (exclusive prefix sum), in place.
+__global__ void k_bdpt_len_scan(uint32_t* hist) {
+    uint32_t run = 0;
+    for (uint32_t b = 0; b < LEN_BUCKETS; ++b) {
+        uint32_t c = hist[b];
+        hist[b] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_bdpt_len_scatter(uint32_t n, const uint32_t* __restrict__ vcount,
+                                                            const uint32_t* __restrict__ flags, uint32_t* pos,
+                                                            uint32_t* __restrict__ order) {
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        const bool in = i < n;
+        const uint32_t key = in ? len_bucket(vcount, flags, i) : 0xFFFFFFFFu;
+        // One atomic per distinct bucket in the warp.
+        const unsigned same = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(same) - 1;
+        uint32_t base = 0;
+        if (in && static_cast<int>(lane) == leader) base = atomicAdd(&pos[key], static_cast<uint32_t>(__popc(same)));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (in) order[base + __popc(same & ((1u << lane) - 1u))] = i;
+    }
 }
 
 // connect() for every strategy of one path, in the reference's loop order, each term
@@ -436,21 +539,18 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParam
                                                         const uint32_t* __restrict__ flags, uint32_t* counters,
                                                         uint32_t* __restrict__ entry_base, float4* __restrict__ entries,
                                                         uint4* __restrict__ shadow_q, float4* __restrict__ lt,
-                                                        uint32_t* __restrict__ lt_pixel) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+                                                        uint32_t* __restrict__ lt_pixel,
+                                                        const uint32_t* __restrict__ order) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    const uint32_t i = order[t];
     uint32_t fl = flags[i];
     if (fl & F_SKIP) return;
     uint32_t cs = vcount[2 * i], ls = vcount[2 * i + 1];
     uint32_t ne = num_entries(cs, ls, p.max_len);
     uint32_t base = ne ? atomicAdd(counters + CNT_ENTRIES, ne) : 0;
     entry_base[i] = base;
-    VPdf cp[MAX_WALK], lp[MAX_WALK];
     bool lt_possible = false;
-    if (p.mis) {
-        for (uint32_t k = 0; k < cs; ++k) cp[k] = load_pdf(vs, k, 2 * i);
-        for (uint32_t k = 0; k < ls; ++k) lp[k] = load_pdf(vs, k, 2 * i + 1);
-    }
     if (p.lt && cs > 0) {
         VPos z1 = load_pos(vs, 0, 2 * i);
         float4 f0 = vs.at(0, 0, 2 * i);
@@ -459,24 +559,37 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParam
     }
     const uint32_t extra = p.lt ? 1u : 0u;
     uint32_t j = base;
+    WalkMis cw;
+    cw.skip0 = !lt_possible;
     for (uint32_t c = 1; c <= cs; ++c) {
         Vtx cv = load_vertex(vs, c - 1, 2 * i);
-        for (uint32_t l = 0; l <= ls; ++l) {
-            if (c + l > p.max_len) continue;
+        if (p.mis) cw.push(load_pdf(vs, c - 1, 2 * i));
+        WalkMis lw;
+        for (uint32_t l = 0; l <= ls && c + l <= p.max_len; ++l) {
             V3 term = v3zero();
             float flag = E_NO_TEST;
             Vtx lv;
+            VEval ez{v3zero(), 0.0f, 0.0f}, ey{v3zero(), 0.0f, 0.0f};
             if (l == 0) {
                 if (cv.prim != NO_INDEX) term = mul(cv.tp, cv.emission);
             } else {
                 lv = load_vertex(vs, l - 1, 2 * i + 1);
+                if (p.mis) lw.push(load_pdf(vs, l - 1, 2 * i + 1));
                 if (cv.prim != NO_INDEX && lv.prim != NO_INDEX && cv.connectible && lv.connectible) {
                     V3 c2l = normalized(lv.point - cv.point);
-                    V3 l2c = -c2l;
+                    V3 l2c = -c2l;  // equals normalized(cv.point - lv.point) bit for bit
                     const DevMaterial& cm = s.materials[cv.material];
                     const DevMaterial& lm = s.materials[lv.material];
-                    V3 cr = f_world(cm, cv.incoming, c2l, cv.frame, true);
-                    V3 ce = l == 1 ? light_world(lm, l2c, lv.frame) : f_world(lm, lv.incoming, l2c, lv.frame, false);
+                    ez = eval_vertex(cm, cv.incoming, c2l, cv.frame, true, p.mis);
+                    V3 cr = ez.f;
+                    V3 ce;
+                    if (l == 1) {
+                        ce = light_world(lm, l2c, lv.frame);
+                        ey.pdf_fwd = light_dir_pdf(lv.frame, l2c);
+                    } else {
+                        ey = eval_vertex(lm, lv.incoming, l2c, lv.frame, false, p.mis);
+                        ce = ey.f;
+                    }
                     float g = fabsf(dot(cv.frame.normal, c2l));
                     float cdn = convert_density(cv.point, lv.point, lv.frame);
                     term = mul(mul(mul(cv.tp, cr), ce), lv.tp) * (g * cdn);
@@ -491,7 +604,7 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParam
             }
             float w;
             if (!p.mis) w = 1.0f / static_cast<float>(c + l + extra);  // integrators.rs:345-354
-            else w = is_zero(term) ? 0.0f : strategy_weight(s, vs, i, cp, lp, c, l, cv, l ? &lv : nullptr, lt_possible);
+            else w = is_zero(term) ? 0.0f : strategy_weight(s, vs, i, cw, lw, c, l, cv, l ? &lv : nullptr, ez, ey);
             term = term * w;
             entries[j] = make_float4(term.x, term.y, term.z, flag);
             ++j;
@@ -501,17 +614,21 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParam
     // Light tracing: light-walk vertex y -> camera.  We / pdf of a pinhole camera is
     // 1 / (area cos^3 dist^2) (PBRT 3e section 16.1.1).
     const uint32_t lmax = min(ls, p.max_len);
+    WalkMis lw;
     for (uint32_t l = 1; l <= p.max_len; ++l) {
         size_t e = static_cast<size_t>(i) * p.max_len + (l - 1);
         float4 out = make_float4(0.0f, 0.0f, 0.0f, E_NO_TEST);
         uint32_t pix = 0;
         if (l <= lmax) {
             Vtx y = load_vertex(vs, l - 1, 2 * i + 1);
+            if (p.mis) lw.push(load_pdf(vs, l - 1, 2 * i + 1));
             float ss, tt, dist, cvw;
             if (y.prim != NO_INDEX && y.connectible && p.view.project(y.point, ss, tt, dist, cvw)) {
                 V3 w_yc = (p.view.pos - y.point) / dist;
                 const DevMaterial& ym = s.materials[y.material];
-                V3 F = l == 1 ? light_world(ym, w_yc, y.frame) : f_world(ym, y.incoming, w_yc, y.frame, false);
+                VEval ev{v3zero(), 0.0f, 0.0f};
+                if (l >= 2) ev = eval_vertex(ym, y.incoming, w_yc, y.frame, false, p.mis);
+                V3 F = l == 1 ? light_world(ym, w_yc, y.frame) : ev.f;
                 float g = fabsf(dot(y.frame.normal, w_yc)) / (p.view.area * cvw * cvw * cvw * dist * dist);
                 V3 L = mul(y.tp, F) * g;
                 if (!nearly_zero(L)) {
@@ -523,9 +640,9 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParam
                         float ym_rev = 0.0f;
                         if (l >= 2) {
                             VPos yp = load_pos(vs, l - 2, 2 * i + 1);
-                            ym_rev = to_area(pdf_world(ym, w_yc, y.incoming, y.frame), y.point, yp.point, yp.ng);
+                            ym_rev = to_area(ev.pdf_rev, y.point, yp.point, yp.ng);
                         }
-                        w = mis_weight(cp, lp, 0, l, 0.0f, 0.0f, y_rev, ym_rev, true);
+                        w = 1.0f / (1.0f + lw.part(y_rev, ym_rev));
                     }
                     L = L * w;
                     uint32_t col = min(p.width - 1, static_cast<uint32_t>(floorf(0.5f * (ss + 1.0f) * p.width)));
@@ -679,6 +796,8 @@ cudaError_t BdptState::ensure(size_t paths, uint32_t max_len) {
     if ((e = shadow.ensure((pairs + lt_n) * sizeof(uint4))) != cudaSuccess) return e;
     if ((e = lt.ensure(lt_n * sizeof(float4))) != cudaSuccess) return e;
     if ((e = lt_pixel.ensure(lt_n * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = order.ensure(paths * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = len_hist.ensure(2 * LEN_BUCKETS * sizeof(uint32_t))) != cudaSuccess) return e;
     return cudaSuccess;
 }
 
@@ -754,9 +873,21 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             GR_CUDA_TRY(cudaGetLastError());
             launches += 2;
         }
+        {
+            const int sgrid = static_cast<int>(std::min<uint32_t>((p.n + BLOCK - 1) / BLOCK, 1024u));
+            uint32_t* hist = bs.len_hist.as<uint32_t>();
+            GR_CUDA_TRY(cudaMemsetAsync(hist, 0, LEN_BUCKETS * sizeof(uint32_t), st));
+            k_bdpt_len_count<<<sgrid, BLOCK, 0, st>>>(p.n, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), hist);
+            k_bdpt_len_scan<<<1, 1, 0, st>>>(hist);
+            k_bdpt_len_scatter<<<sgrid, BLOCK, 0, st>>>(p.n, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), hist,
+                                                       bs.order.as<uint32_t>());
+            GR_CUDA_TRY(cudaGetLastError());
+            launches += 3;
+        }
         k_bdpt_connect<<<(p.n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(
             job.scene, p, vs, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), cnt, bs.entry_base.as<uint32_t>(),
-            bs.entries.as<float4>(), bs.shadow.as<uint4>(), bs.lt.as<float4>(), bs.lt_pixel.as<uint32_t>());
+            bs.entries.as<float4>(), bs.shadow.as<uint4>(), bs.lt.as<float4>(), bs.lt_pixel.as<uint32_t>(),
+            bs.order.as<uint32_t>());
         GR_CUDA_TRY(cudaGetLastError());
         uint32_t cap = p.n * (max_pairs(max_len) + (p.lt ? max_len : 0u));
         gr_status s2;

@@ -65,6 +65,7 @@ struct PathState {
 struct BdptState {
     DevBuf q_slot[2], q_o[2], q_d[2], q_hit, tp, key, st, light;
     DevBuf verts, vcount, flags, escape, entry_base, entries, shadow, lt, lt_pixel;
+    DevBuf order, len_hist;  // paths ordered by walk lengths for the connection kernel
     cudaError_t ensure(size_t paths, uint32_t max_len);
 };
 
