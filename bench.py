@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=3.0, help="Poisson arrival rate (requests/s)")
     ap.add_argument("--serve-target", type=float, default=1e-3,
                     help="relMSE target of the progressive serving leg (0: skip it)")
+    ap.add_argument("--profile-bdpt", action="store_true",
+                    help="with --profile-case: the BDPT workload (512x512, MIS + light tracing)")
     ap.add_argument("--profile-case", action="store_true",
                     help="render the workload once (untimed, --spp passes) and exit: the small case for ncu")
     return ap.parse_args()
@@ -562,14 +564,21 @@ def run_bdpt(lib, cpu_seconds):
 
 def profile_case(args):
     import gammaray_gb300 as g
+    from gammaray_gb300 import scenes
 
     lib = g.load()
-    w = workload(args)
+    if args.profile_bdpt:  # the BDPT line's scene and integrator (MIS + light tracing)
+        w = scenes.displaced_sphere(512, 512, args.spp or 1, bdpt=True)
+        w.integrator = g.BdptIntegrator(max_depth=10, rr_depth=4, mis=1, light_tracing=1)
+    else:
+        w = workload(args)
     st = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1)
     film = g.Film(w.width, w.height, lib=lib)
     st.render(w.camera, w.integrator, film, w.spp)
     s = st.last_stats()
-    print(json.dumps({"profile_case": config_of(w), "device_ms": s.device_ms, "rays": s.extension_rays,
+    case = {"workload": "bdpt_displaced_sphere_102k", "width": w.width, "height": w.height, "spp": w.spp} \
+        if args.profile_bdpt else config_of(w)
+    print(json.dumps({"profile_case": case, "device_ms": s.device_ms, "rays": s.extension_rays,
                       "launches": s.kernel_launches}))
 
 

@@ -534,7 +534,10 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_len_scatter(uint32_t n, const ui
 // times its weight (uniform or MIS).  With light tracing, each light-walk vertex inside
 // the image gets a camera term in lt[i * max_len + l - 1] (value, flag) and its film
 // pixel in lt_pixel.
-__global__ void __launch_bounds__(BLOCK) k_bdpt_connect(DeviceScene s, BdptParams p, Verts vs,
+#ifndef GR_CONNECT_MIN_BLOCKS
+#define GR_CONNECT_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(BLOCK, GR_CONNECT_MIN_BLOCKS) k_bdpt_connect(DeviceScene s, BdptParams p, Verts vs,
                                                         const uint32_t* __restrict__ vcount,
                                                         const uint32_t* __restrict__ flags, uint32_t* counters,
                                                         uint32_t* __restrict__ entry_base, float4* __restrict__ entries,
