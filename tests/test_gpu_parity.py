@@ -212,6 +212,23 @@ def test_image_statistics(gpu, oracle):
     assert rel_mse < 1e-3, rel_mse
 
 
+def test_converged_render_within_rel_mse(gpu, oracle):
+    # A converged GPU render against the oracle's 4096-spp render of the same scene, with
+    # independent random streams (different seeds): relMSE <= 1e-3.  On this scene one
+    # render's relMSE is about 1.05 / spp, so two independent 4096-spp renders differ
+    # by about 5e-4.
+    w = scenes.cornell_spheres(48, 48, 4096)
+    imgs = []
+    for L, seed in ((gpu, 21), (oracle, 22)):
+        st = g.Stage(w.prims, lib=L, seed=seed)
+        f = g.Film(48, 48, lib=L)
+        st.render(w.camera, w.integrator, f, 4096)
+        imgs.append(f.resolve())
+    a, b = imgs
+    rel_mse = float(np.mean((a - b) ** 2) / np.mean(b ** 2))
+    assert rel_mse <= 1e-3, rel_mse
+
+
 def test_exr_matches_oracle(gpu, oracle, tmp_path):
     w = scenes.cornell_spheres(20, 12, 1)
     out = []
