@@ -108,6 +108,7 @@ class SceneInfo(C.Structure):
         ("num_lights", C.c_uint32),
         ("bvh_width", C.c_uint32),
         ("build_seconds", C.c_double),
+        ("tree_hash", C.c_uint64),
     ]
 
 

@@ -246,7 +246,7 @@ gr_status gr_scene_plan(const gr_scene_desc* desc, gr_scene_info* o) {
     auto t0 = std::chrono::steady_clock::now();
     HostBuild h;
     std::string err;
-    if (!build_scene(*desc, h, err)) return fail(GR_ERR_INVALID_ARGUMENT, err);
+    if (!build_scene(*desc, h, err, true)) return fail(GR_ERR_INVALID_ARGUMENT, err);
     std::memset(o, 0, sizeof(*o));
     o->num_components = h.num_components;
     o->num_binary_nodes = h.num_binary_nodes;
@@ -255,6 +255,7 @@ gr_status gr_scene_plan(const gr_scene_desc* desc, gr_scene_info* o) {
     o->num_lights = static_cast<uint32_t>(h.lights.size());
     o->bvh_width = h.width;
     o->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    o->tree_hash = h.tree_hash;
     return GR_OK;
 }
 

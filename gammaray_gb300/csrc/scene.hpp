@@ -67,6 +67,7 @@ struct HostBuild {
     std::vector<float> light_cdf;
     uint64_t num_components = 0;
     uint64_t num_binary_nodes = 0;
+    uint64_t tree_hash = 0;  // when asked for: see gr_scene_info.tree_hash
     uint64_t num_wide_nodes = 0;
     uint32_t width = 4;
     uint32_t stack_depth = 0;
@@ -84,6 +85,6 @@ bool build_material(const gr_material_desc& d, DevMaterial& out, std::string& er
 
 // Validates the descriptor, runs the reference SAH build (geom/bvh.rs:182-382) and
 // collapses the binary tree into a width-W BVH.
-bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err);
+bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bool tree_hash = false);
 
 }  // namespace gr

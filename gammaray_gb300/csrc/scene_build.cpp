@@ -567,7 +567,44 @@ bool build_material(const gr_material_desc& d, DevMaterial& m, std::string& err)
 
 static void put_bits(float* dst, uint32_t v) { std::memcpy(dst, &v, 4); }
 
-bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
+// FNV-1a over the binary tree in depth-first order, left child first: each node's box,
+// then a leaf's component count and (prim, component) ids, or an inner node's tag.
+static uint64_t tree_hash(const std::vector<BinNode>& nodes, int32_t root, const std::vector<Rec>& recs,
+                          const std::vector<Item>& items) {
+    uint64_t h = 1469598103934665603ull;
+    auto add = [&](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; ++i) {
+            h ^= b[i];
+            h *= 1099511628211ull;
+        }
+    };
+    std::vector<int32_t> stack{root};
+    while (!stack.empty()) {
+        const BinNode& nd = nodes[stack.back()];
+        stack.pop_back();
+        add(nd.box.lo, sizeof(nd.box.lo));
+        add(nd.box.hi, sizeof(nd.box.hi));
+        if (nd.child[0] < 0) {
+            const uint32_t tag = 1, count = nd.count;
+            add(&tag, 4);
+            add(&count, 4);
+            for (uint32_t j = 0; j < nd.count; ++j) {
+                const Item& it = items[recs[nd.first + j].id & ID_MASK];
+                const uint32_t pc[2] = {it.prim, it.comp};
+                add(pc, sizeof(pc));
+            }
+        } else {
+            const uint32_t tag = 0;
+            add(&tag, 4);
+            stack.push_back(nd.child[1]);
+            stack.push_back(nd.child[0]);
+        }
+    }
+    return h;
+}
+
+bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bool want_tree_hash) {
     out = HostBuild();
     uint32_t W = desc.bvh_width ? desc.bvh_width : 4;
     if (W != 2 && W != 4 && W != 8) {
@@ -740,6 +777,7 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err) {
         RefBuilder rb(recs.data(), recs.size());
         int32_t root = rb.build(recs.data(), recs.size());
         out.num_binary_nodes = rb.node_count();
+        if (want_tree_hash) out.tree_hash = tree_hash(rb.nodes, root, recs, items);
         std::vector<Box> comp_box(items.size());
         auto records = [&](unsigned, size_t b, size_t e) {
             for (size_t k = b; k < e; ++k) {

@@ -155,6 +155,9 @@ typedef struct gr_scene_info {
     uint32_t num_lights;
     uint32_t bvh_width;
     double build_seconds;
+    uint64_t tree_hash;        /* gr_scene_plan only: FNV-1a over the binary tree in depth-first
+                                  order (each node's box; each leaf's prim and component ids);
+                                  equal for equal trees.  0 elsewhere and for device builds. */
 } gr_scene_info;
 
 /* Replaces Stage::new / Bvh::build (render/stage.rs:15-20, geom/bvh.rs:339-382):

@@ -240,11 +240,43 @@ gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out) {
     return GR_OK;
 }
 
+// FNV-1a over the flattened tree (depth-first, left child first, as bvh.rs:310-337
+// lays it out): each node's box, then a leaf's count and (prim, component) ids, or an
+// inner node's tag.  The GPU library hashes its build the same way.
+static uint64_t tree_hash(const Bvh& b) {
+    uint64_t h = 1469598103934665603ull;
+    auto add = [&](const void* p, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; ++i) {
+            h ^= c[i];
+            h *= 1099511628211ull;
+        }
+    };
+    for (const LinearNode& nd : b.nodes) {
+        const float box[6] = {nd.bbox.min.x, nd.bbox.min.y, nd.bbox.min.z, nd.bbox.max.x, nd.bbox.max.y, nd.bbox.max.z};
+        add(box, sizeof(box));
+        if (nd.num_components > 0) {
+            const uint32_t tag = 1, count = static_cast<uint32_t>(nd.num_components);
+            add(&tag, 4);
+            add(&count, 4);
+            for (size_t j = 0; j < nd.num_components; ++j) {
+                const uint32_t pc[2] = {b.components[nd.offset + j].first, b.components[nd.offset + j].second};
+                add(pc, sizeof(pc));
+            }
+        } else {
+            const uint32_t tag = 0;
+            add(&tag, 4);
+        }
+    }
+    return h;
+}
+
 gr_status gr_scene_plan(const gr_scene_desc* desc, gr_scene_info* o) {
     gr_scene* s = nullptr;
     gr_status st = gr_scene_create(desc, &s);
     if (st != GR_OK) return st;
     st = gr_scene_get_info(s, o);
+    if (st == GR_OK) o->tree_hash = tree_hash(s->sc.bvh);
     delete s;
     return st;
 }

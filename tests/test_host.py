@@ -71,6 +71,24 @@ def test_product_host_build_matches_oracle_tree(oracle):
         assert a.num_lights == b.num_lights
 
 
+def test_threaded_host_build_is_the_reference_tree(oracle):
+    # The product's build runs subtrees and large passes on threads; its binary tree
+    # must be the serial restatement's exactly (boxes, leaf order, ids), at sizes that
+    # use the threads (>= 32,768 components split their passes) and on skewed inputs.
+    lib = gpu_lib()
+    mat = g.Material.disney().build()
+    rng = np.random.default_rng(9)
+    verts = (rng.standard_cauchy(size=(60_000, 3)) * 0.1).astype(np.float32)  # heavy tails: skewed splits
+    cases = [scenes.displaced_sphere(8, 8, 1, tris=120_000).prims,
+             [g.Mesh(mat, None, verts, rng.integers(0, 60_000, (80_000, 3)).astype(np.uint32))],
+             scenes.cornell_spheres().prims]
+    for prims in cases:
+        a = g.api.plan_scene(prims, lib=lib)
+        b = g.api.plan_scene(prims, lib=oracle)
+        assert a.num_binary_nodes == b.num_binary_nodes
+        assert a.tree_hash == b.tree_hash != 0
+
+
 def test_wide_collapse_shrinks_with_width():
     lib = gpu_lib()
     w = scenes.displaced_sphere(8, 8, 1, tris=20_000)
