@@ -775,6 +775,13 @@ gr_status shadow_launch(const DeviceScene& s, uint32_t cap, const uint32_t* coun
 
 }  // namespace
 
+size_t BdptState::bytes_per_path(uint32_t max_len) {
+    const size_t pairs = max_pairs(max_len);
+    return 2 * (2 * (4 + 16 + 16) + 16 + 16) + 8 + 8 + 16  // queues, hits, throughput; key, st, light
+           + 2 * max_len * VREC * 16 + 2 * 4 + 4 + 16 + 4     // vertices, counts, flags, escape, entry base
+           + pairs * 16 + (pairs + max_len) * 16 + max_len * (16 + 4) + 4;  // entries, shadow queue, lt, order
+}
+
 cudaError_t BdptState::ensure(size_t paths, uint32_t max_len) {
     size_t slots = 2 * paths;
     size_t pairs = static_cast<size_t>(max_pairs(max_len)) * paths;
@@ -810,8 +817,20 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     const uint32_t total = job.samples_out ? 1u : rp.spp;
     if (total == 0) return GR_OK;
     const uint32_t max_len = rp.max_depth ? rp.max_depth : 16;
+    // Paths in flight: up to 4 M (the bench's 512x512 x 16 spp in one group; 0.5 M -> 1 M
+    // -> 2 M -> 4 M measured 96 -> 117 -> 135 -> 146 Msamples/s with MIS), within the
+    // smaller of 24 GB and a quarter of free device memory.
     const char* env = std::getenv("GR_BDPT_PATHS_IN_FLIGHT");
-    uint32_t target = env && std::atoi(env) > 0 ? static_cast<uint32_t>(std::atoi(env)) : (1u << 19);
+    uint32_t target;
+    if (env && std::atoi(env) > 0) {
+        target = static_cast<uint32_t>(std::atoi(env));
+    } else {
+        size_t free_b = 0, total_b = 0;
+        GR_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+        const size_t budget = std::min<size_t>(size_t(24) << 30, free_b / 4);
+        const size_t fit = budget / BdptState::bytes_per_path(max_len);
+        target = static_cast<uint32_t>(std::max<size_t>(1u << 19, std::min<size_t>(1u << 22, fit)));
+    }
     uint32_t group = std::max(1u, std::min(total, target / std::max(1u, npix)));
     const size_t npaths = static_cast<size_t>(group) * npix;
     BdptState& bs = device_work().bdpt;

@@ -67,6 +67,7 @@ struct BdptState {
     DevBuf verts, vcount, flags, escape, entry_base, entries, shadow, lt, lt_pixel;
     DevBuf order, len_hist;  // paths ordered by walk lengths for the connection kernel
     cudaError_t ensure(size_t paths, uint32_t max_len);
+    static size_t bytes_per_path(uint32_t max_len);  // device bytes ensure() needs per path
 };
 
 // The large wavefront buffers are shared by every scene on a device (renders on one
