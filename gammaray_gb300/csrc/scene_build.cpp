@@ -654,6 +654,7 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
             for (int k = 0; k < 3; ++k) {  // Sphere::bbox_world (sphere.rs:47-58)
                 it.box.lo[k] = d.center[k] - d.radius;
                 it.box.hi[k] = d.center[k] + d.radius;
+                it.cen[k] = 0.5f * it.box.lo[k] + 0.5f * it.box.hi[k];  // bvh.rs:26
             }
             items.push_back(it);
         } else if (d.kind == GR_PRIM_MESH) {
@@ -661,31 +662,48 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
                 err = "mesh " + std::to_string(p) + " has no triangles";
                 return false;
             }
-            for (uint32_t t = 0; t < d.num_tris; ++t) {
-                for (int k = 0; k < 3; ++k) {
-                    if (d.tri_vertices[3 * t + k] >= d.num_vertices) {
-                        err = "vertex index out of range";
-                        return false;
-                    }
-                }
+            // Triangle t: its index checks (0: fine, else the first that fails) and its
+            // item.  Large meshes run on threads; the error reported is the first
+            // failing triangle's, as in a serial pass.
+            const size_t ibase = items.size();
+            items.resize(ibase + d.num_tris);
+            auto triangle = [&](uint32_t t) -> int {
+                for (int k = 0; k < 3; ++k)
+                    if (d.tri_vertices[3 * t + k] >= d.num_vertices) return 1;
                 if (d.tri_normals && d.tri_normals[3 * t] != GR_NO_INDEX)
                     for (int k = 0; k < 3; ++k)
-                        if (d.tri_normals[3 * t + k] >= d.num_normals) {
-                            err = "normal index out of range";
-                            return false;
-                        }
+                        if (d.tri_normals[3 * t + k] >= d.num_normals) return 2;
                 if (d.tri_uvs)
                     for (int k = 0; k < 3; ++k)
-                        if (d.tri_uvs[3 * t + k] >= d.num_uvs) {
-                            err = "uv index out of range";
-                            return false;
-                        }
-                Item it;
+                        if (d.tri_uvs[3 * t + k] >= d.num_uvs) return 3;
+                Item& it = items[ibase + t];
                 it.prim = p;
                 it.comp = t;
                 it.box = Box::empty();  // Mesh::bbox_world (mesh.rs:262-268)
                 for (int k = 0; k < 3; ++k) it.box.grow(d.vertices + 3 * d.tri_vertices[3 * t + k]);
-                items.push_back(it);
+                for (int k = 0; k < 3; ++k) it.cen[k] = 0.5f * it.box.lo[k] + 0.5f * it.box.hi[k];  // bvh.rs:26
+                return 0;
+            };
+            uint64_t bad = UINT64_MAX;  // (triangle << 2) | check of the first failure
+            const unsigned hw = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+            if (d.num_tris >= RefBuilder::SPLIT_PASS && hw > 1) {
+                std::vector<uint64_t> part_bad(hw, UINT64_MAX);
+                RefBuilder::in_parts(d.num_tris, hw, [&](unsigned k, size_t b, size_t e) {
+                    for (size_t t = b; t < e; ++t)
+                        if (int c = triangle(static_cast<uint32_t>(t))) {
+                            part_bad[k] = (static_cast<uint64_t>(t) << 2) | static_cast<uint64_t>(c);
+                            break;
+                        }
+                });
+                for (uint64_t v : part_bad) bad = std::min(bad, v);
+            } else {
+                for (uint32_t t = 0; t < d.num_tris && bad == UINT64_MAX; ++t)
+                    if (int c = triangle(t)) bad = (static_cast<uint64_t>(t) << 2) | static_cast<uint64_t>(c);
+            }
+            if (bad != UINT64_MAX) {
+                const int c = static_cast<int>(bad & 3u);
+                err = c == 1 ? "vertex index out of range" : (c == 2 ? "normal index out of range" : "uv index out of range");
+                return false;
             }
             if (d.tri_normals && d.num_normals) {
                 out.any_normals = true;
@@ -704,8 +722,6 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
             return false;
         }
     }
-    for (Item& it : items)  // centroid = 0.5 min + 0.5 max (bvh.rs:26)
-        for (int k = 0; k < 3; ++k) it.cen[k] = 0.5f * it.box.lo[k] + 0.5f * it.box.hi[k];
     out.num_components = items.size();
     if (items.empty()) {
         err = "scene has no components";
@@ -769,12 +785,18 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
         }
     } else {
         std::vector<Rec> recs(items.size());
-        for (size_t k = 0; k < items.size(); ++k) {
-            recs[k].box = items[k].box;
-            std::memcpy(recs[k].cen, items[k].cen, sizeof(recs[k].cen));
-            recs[k].id = static_cast<uint32_t>(k);
-        }
+        auto fill = [&](unsigned, size_t b, size_t e) {
+            for (size_t k = b; k < e; ++k) {
+                recs[k].box = items[k].box;
+                std::memcpy(recs[k].cen, items[k].cen, sizeof(recs[k].cen));
+                recs[k].id = static_cast<uint32_t>(k);
+            }
+        };
         RefBuilder rb(recs.data(), recs.size());
+        if (recs.size() >= RefBuilder::SPLIT_PASS && rb.threads > 1)
+            RefBuilder::in_parts(recs.size(), rb.threads, fill);
+        else
+            fill(0, 0, recs.size());
         int32_t root = rb.build(recs.data(), recs.size());
         out.num_binary_nodes = rb.node_count();
         if (want_tree_hash) out.tree_hash = tree_hash(rb.nodes, root, recs, items);

@@ -107,6 +107,28 @@ def test_plan_rejects_bad_input():
         g.api.plan_scene([m], lib=lib)
 
 
+def test_large_mesh_reports_the_first_bad_triangle(oracle):
+    # A mesh this large is validated on threads; the error is still the first failing
+    # triangle's (here a uv index at triangle 5,000 before a vertex index at 30,000).
+    lib = gpu_lib()
+    rng = np.random.default_rng(3)
+    n = 40_000
+    v = rng.random((1000, 3)).astype(np.float32)
+    t = rng.integers(0, 1000, (n, 3)).astype(np.uint32)
+    uv = rng.random((1000, 2)).astype(np.float32)
+    tuv = rng.integers(0, 1000, (n, 3)).astype(np.uint32)
+    t[30_000, 1] = 5000
+    tuv[5_000, 2] = 5000
+    m = g.Mesh(g.Material.disney().build(), None, v, t, uvs=uv, tri_uvs=tuv)
+    for L in (lib, oracle):
+        with pytest.raises(_abi.GrError, match="uv index"):
+            g.api.plan_scene([m], lib=L)
+    tuv[5_000, 2] = 0
+    m = g.Mesh(g.Material.disney().build(), None, v, t, uvs=uv, tri_uvs=tuv)
+    with pytest.raises(_abi.GrError, match="vertex index"):
+        g.api.plan_scene([m], lib=lib)
+
+
 def _free_port():
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
