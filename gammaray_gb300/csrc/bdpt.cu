@@ -531,9 +531,7 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_len_scatter(uint32_t n, const ui
 }
 
 // connect() for every strategy of one path, in the reference's loop order, each term
-// times its weight (uniform or MIS).  With light tracing, each light-walk vertex inside
-// the image gets a camera term in lt[i * max_len + l - 1] (value, flag) and its film
-// pixel in lt_pixel.
+// times its weight (uniform or MIS).
 #ifndef GR_CONNECT_MIN_BLOCKS
 #define GR_CONNECT_MIN_BLOCKS 1
 #endif
@@ -541,8 +539,7 @@ __global__ void __launch_bounds__(BLOCK, GR_CONNECT_MIN_BLOCKS) k_bdpt_connect(D
                                                         const uint32_t* __restrict__ vcount,
                                                         const uint32_t* __restrict__ flags, uint32_t* counters,
                                                         uint32_t* __restrict__ entry_base, float4* __restrict__ entries,
-                                                        uint4* __restrict__ shadow_q, float4* __restrict__ lt,
-                                                        uint32_t* __restrict__ lt_pixel,
+                                                        uint4* __restrict__ shadow_q,
                                                         const uint32_t* __restrict__ order) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.n) return;
@@ -613,7 +610,24 @@ __global__ void __launch_bounds__(BLOCK, GR_CONNECT_MIN_BLOCKS) k_bdpt_connect(D
             ++j;
         }
     }
-    if (!p.lt) return;
+
+}
+
+// The light-tracing strategy (t = 1, an MIS extension): each light-walk vertex inside
+// the image gets a camera term in lt[i * max_len + l - 1] (value, flag) and its film
+// pixel in lt_pixel.  A kernel of its own, after the connections, so that neither
+// kernel carries the other's code and registers.
+__global__ void __launch_bounds__(BLOCK) k_bdpt_light_trace(DeviceScene s, BdptParams p, Verts vs,
+                                                            const uint32_t* __restrict__ vcount,
+                                                            const uint32_t* __restrict__ flags, uint32_t* counters,
+                                                            uint4* __restrict__ shadow_q, float4* __restrict__ lt,
+                                                            uint32_t* __restrict__ lt_pixel,
+                                                            const uint32_t* __restrict__ order) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    const uint32_t i = order[t];
+    if (flags[i] & F_SKIP) return;
+    const uint32_t ls = vcount[2 * i + 1];
     // Light tracing: light-walk vertex y -> camera.  We / pdf of a pinhole camera is
     // 1 / (area cos^3 dist^2) (PBRT 3e section 16.1.1).
     const uint32_t lmax = min(ls, p.max_len);
@@ -908,9 +922,15 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         }
         k_bdpt_connect<<<(p.n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(
             job.scene, p, vs, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), cnt, bs.entry_base.as<uint32_t>(),
-            bs.entries.as<float4>(), bs.shadow.as<uint4>(), bs.lt.as<float4>(), bs.lt_pixel.as<uint32_t>(),
-            bs.order.as<uint32_t>());
+            bs.entries.as<float4>(), bs.shadow.as<uint4>(), bs.order.as<uint32_t>());
         GR_CUDA_TRY(cudaGetLastError());
+        if (p.lt) {
+            k_bdpt_light_trace<<<(p.n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(
+                job.scene, p, vs, bs.vcount.as<uint32_t>(), bs.flags.as<uint32_t>(), cnt, bs.shadow.as<uint4>(),
+                bs.lt.as<float4>(), bs.lt_pixel.as<uint32_t>(), bs.order.as<uint32_t>());
+            GR_CUDA_TRY(cudaGetLastError());
+            ++launches;
+        }
         uint32_t cap = p.n * (max_pairs(max_len) + (p.lt ? max_len : 0u));
         gr_status s2;
         switch (job.scene.width) {
