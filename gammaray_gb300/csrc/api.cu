@@ -60,9 +60,9 @@ gr_status sync_check(cudaStream_t st, const char* what, uint32_t bounce, uint32_
 }
 
 template <class T>
-static gr_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st, uint64_t& total) {
+static gr_status upload(DevBuf& b, const T& v, cudaStream_t st, uint64_t& total) {
     if (v.empty()) return GR_OK;
-    size_t bytes = v.size() * sizeof(T);
+    size_t bytes = v.size() * sizeof(v[0]);
     GR_CUDA_TRY(b.ensure(bytes));
     GR_CUDA_TRY(cudaMemcpyAsync(b.ptr, v.data(), bytes, cudaMemcpyHostToDevice, st));
     total += bytes;

@@ -306,10 +306,10 @@ __global__ void k_permute(const float4* __restrict__ rec, const uint32_t* __rest
 }
 
 template <class T>
-cudaError_t put(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
-    cudaError_t e = b.ensure(v.size() * sizeof(T));
+cudaError_t put(DevBuf& b, const T& v, cudaStream_t st) {
+    cudaError_t e = b.ensure(v.size() * sizeof(v[0]));
     if (e != cudaSuccess || v.empty()) return e;
-    return cudaMemcpyAsync(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+    return cudaMemcpyAsync(b.ptr, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice, st);
 }
 
 template <int W>

@@ -11,7 +11,10 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
+#include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/gammaray.h"
@@ -54,9 +57,30 @@ struct DeviceScene {
 };
 
 // Host-side build products (kept for re-uploads and queries).
+// An allocator that leaves new elements uninitialised (resize without a fill), for
+// arrays that are written in full right after.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <class U>
+    NoInitAlloc(const NoInitAlloc<U>&) {}
+    template <class U>
+    void construct(U* p) {
+        ::new (static_cast<void*>(p)) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) {
+        ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+    }
+};
+
 struct HostBuild {
-    std::vector<float> nodes;         // raw node floats (child stored as int bits)
-    std::vector<float> prims;         // 12 floats per component
+    std::vector<float> nodes;                     // raw node floats (child stored as int bits)
+    std::vector<float, NoInitAlloc<float>> prims;  // 12 floats per component (every one written)
     std::vector<uint32_t> tri_normal_idx, tri_uv_idx;
     std::vector<float> normals, uvs;
     std::vector<uint32_t> prim_material;

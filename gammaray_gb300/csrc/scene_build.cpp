@@ -18,8 +18,12 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <memory>
 #include <numeric>
 #include <pthread.h>
+#include <unistd.h>
+#include <condition_variable>
+#include <mutex>
 #include <thread>
 
 #include "scene.hpp"
@@ -114,6 +118,104 @@ class BuildThread {
     bool ok_ = false;
 };
 
+// Worker threads for the build's data-parallel passes, started on first use and kept
+// for the life of the process (heap-allocated and detached: no destructor runs while a
+// worker waits).  run() splits a pass into parts taken by the workers and the calling
+// thread, so it completes even with no worker free; in a forked child (no workers) the
+// caller runs every part itself.
+class PassPool {
+  public:
+    static PassPool& get() {
+        static PassPool* pool = new PassPool();
+        return *pool;
+    }
+    void run(unsigned parts, const std::function<void(unsigned)>& fn) {
+        if (parts <= 1 || getpid() != pid_ || workers_ == 0) {
+            for (unsigned k = 0; k < parts; ++k) fn(k);
+            return;
+        }
+        Job job;
+        job.fn = &fn;
+        job.parts = parts;
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            jobs_.push_back(&job);
+            open_.fetch_add(1);
+        }
+        cv_.notify_all();
+        work(job);
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            for (size_t i = 0; i < jobs_.size(); ++i)
+                if (jobs_[i] == &job) {
+                    jobs_.erase(jobs_.begin() + static_cast<long>(i));
+                    break;
+                }
+        }
+        while (job.done.load() != parts || job.inside.load() != 0) std::this_thread::yield();
+    }
+
+  private:
+    struct Job {
+        const std::function<void(unsigned)>* fn = nullptr;
+        unsigned parts = 0;
+        std::atomic<unsigned> next{0}, done{0}, inside{0};
+    };
+    // Runs parts of j until none is left; the thread that first finds none closes it.
+    void work(Job& j) {
+        for (;;) {
+            unsigned k = j.next.fetch_add(1);
+            if (k >= j.parts) {
+                if (k == j.parts) open_.fetch_sub(1);
+                return;
+            }
+            (*j.fn)(k);
+            j.done.fetch_add(1);
+        }
+    }
+    PassPool() : pid_(getpid()) {
+        unsigned hw = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+        workers_ = hw - 1;
+        for (unsigned i = 0; i < workers_; ++i) std::thread([this] { loop(); }).detach();
+    }
+    // Takes a part of the first job that has parts left; spins a little before sleeping,
+    // as a build's passes follow one another closely.
+    void loop() {
+        for (;;) {
+            Job* j = nullptr;
+            for (int spin = 0; spin < 2000 && !j; ++spin) {
+                if (open_.load() != 0) j = take();
+                if (!j) std::this_thread::yield();
+            }
+            if (!j) {
+                std::unique_lock<std::mutex> l(mu_);
+                cv_.wait(l, [&] { return open_.load() != 0; });
+                l.unlock();
+                j = take();
+            }
+            if (j) {
+                work(*j);
+                j->inside.fetch_sub(1);  // the caller may return from run() after this
+            }
+        }
+    }
+    Job* take() {
+        std::lock_guard<std::mutex> g(mu_);
+        for (Job* j : jobs_)
+            if (j->next.load() < j->parts) {
+                j->inside.fetch_add(1);
+                return j;
+            }
+        return nullptr;
+    }
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::vector<Job*> jobs_;
+    std::atomic<int> open_{0};  // jobs with parts not yet taken
+    unsigned workers_ = 0;
+    pid_t pid_;
+};
+
 constexpr int ID_BITS = 31 - LEAF_COUNT_BITS;  // components < 2^ID_BITS (checked before the build)
 constexpr uint32_t ID_MASK = (1u << ID_BITS) - 1u;
 
@@ -135,6 +237,7 @@ class RefBuilder {
     };
 
     Rec* base;
+    std::unique_ptr<Rec[]> tmp;  // scratch for the parallel partition (same indexing as base)
     std::vector<BinNode> nodes;
     std::atomic<uint32_t> next{0};
     std::atomic<uint64_t> used{0};
@@ -148,18 +251,58 @@ class RefBuilder {
         if (threads == 1 || n < 2 * SPAWN_MIN) spawn_depth = 0;
         // At most 2n - 1 nodes, plus the unused tail of each thread's last chunk.
         nodes.resize(2 * n + (static_cast<size_t>(2) << spawn_depth) * CHUNK);
+        if (threads > 1 && n >= SPLIT_PASS) tmp.reset(new Rec[n]);
+    }
+
+    // The reference's swap partition computed on the pass pool, with the same result:
+    // the matches keep their order at the front; the others behave like a queue that
+    // moves its front element to its back at every later match.  So with p1 the first
+    // non-match, T the indices of the matches after it and R = |T|, the non-match at
+    // index p ends at k + pos - R, where pos starts at p - p1 and steps pos = T[pos] - p1
+    // while pos < R (k: the number of matches).
+    template <class P>
+    size_t partition_parallel(Rec* s, size_t n, const P& pred) {
+        const unsigned parts = threads;
+        std::vector<size_t> before(parts + 1, 0);  // matches before each part
+        in_parts(n, parts, [&](unsigned k, size_t b, size_t e) {
+            size_t c = 0;
+            for (size_t i = b; i < e; ++i) c += pred(s[i]) ? 1 : 0;
+            before[k + 1] = c;
+        });
+        for (unsigned k = 0; k < parts; ++k) before[k + 1] += before[k];
+        const size_t k_all = before[parts];
+        if (k_all == n || k_all == 0) return k_all;  // nothing moves
+        size_t p1 = 0;
+        while (pred(s[p1])) ++p1;  // the first non-match (all before it match)
+        const size_t R = k_all - p1;
+        std::vector<uint32_t> T(R);
+        Rec* out = tmp.get() + (s - base);
+        in_parts(n, parts, [&](unsigned k, size_t b, size_t e) {
+            size_t q = before[k];  // rank of the next match
+            for (size_t i = b; i < e; ++i)
+                if (pred(s[i])) {
+                    if (i > p1) T[q - p1] = static_cast<uint32_t>(i);
+                    out[q++] = s[i];
+                }
+        });
+        in_parts(n, parts, [&](unsigned, size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i)
+                if (!pred(s[i])) {
+                    size_t pos = i - p1;
+                    while (pos < R) pos = T[pos] - p1;
+                    out[k_all + pos - R] = s[i];
+                }
+        });
+        in_parts(n, parts, [&](unsigned, size_t b, size_t e) { std::memcpy(s + b, out + b, (e - b) * sizeof(Rec)); });
+        return k_all;
     }
 
     uint64_t node_count() const { return used.load(); }
 
-    // Runs fn(k, begin, end) over `parts` contiguous pieces of [0, n), on threads.
+    // Runs fn(k, begin, end) over `parts` contiguous pieces of [0, n), on the pass pool.
     template <class F>
     static void in_parts(size_t n, unsigned parts, const F& fn) {
-        std::vector<std::thread> th;
-        th.reserve(parts);
-        for (unsigned k = 1; k < parts; ++k) th.emplace_back([&, k] { fn(k, n * k / parts, n * (k + 1) / parts); });
-        fn(0u, size_t(0), n / parts);
-        for (auto& t : th) t.join();
+        PassPool::get().run(parts, [&](unsigned k) { fn(k, n * k / parts, n * (k + 1) / parts); });
     }
 
     static int bucket(const Box& cb, const float* c, int dim) {
@@ -316,7 +459,8 @@ class RefBuilder {
                 }
             if (n > 255 || min_cost < static_cast<float>(n)) {
                 const uint32_t mb = static_cast<uint32_t>(min_b);
-                mid = partition(s, n, [&](const Rec& x) { return (x.id >> ID_BITS) <= mb; });
+                auto left = [&](const Rec& x) { return (x.id >> ID_BITS) <= mb; };
+                mid = (n >= SPLIT_PASS && tmp) ? partition_parallel(s, n, left) : partition(s, n, left);
                 for (int b = 0; b < NB; ++b) {
                     Box* side = b <= min_b ? kids : kids + 2;
                     side[0].grow(bb[b]);
@@ -387,7 +531,6 @@ class Collapser {
     const std::vector<Box>& comp_box;  // per ordered component
     uint32_t W, L;
     std::vector<float>& out;  // node floats
-    uint32_t max_stack = 0;
 
     Collapser(const std::vector<BinNode>& b, const std::vector<Box>& cb, uint32_t w, uint32_t l,
               std::vector<float>& o)
@@ -411,10 +554,10 @@ class Collapser {
         }
     }
 
-    // Emits the node for `c` (which must be expandable, or the root) and returns its
-    // index and the worst-case stack use of its subtree.
-    uint32_t emit(const Cand& c, uint32_t& stack_use) {
-        Cand cands[8];
+    // The slot candidates of c's wide node: c's two halves (or c itself when it is a
+    // leaf), then the expandable slot of largest surface area split again until W slots
+    // are used.
+    uint32_t slots(const Cand& c, Cand (&cands)[8]) const {
         uint32_t nc = 0;
         if (expandable(c)) {
             expand(c, cands[0], cands[1]);
@@ -441,35 +584,131 @@ class Collapser {
             cands[best + 1] = b;
             ++nc;
         }
-        uint32_t idx = static_cast<uint32_t>(out.size() / (8 * W));
-        out.resize(out.size() + 8 * W, 0.0f);
+        return nc;
+    }
+
+    // Wide nodes in the subtree of candidate c (c expandable, or the root).
+    uint32_t count(const Cand& c) const {
+        Cand cs[8];
+        const uint32_t nc = slots(c, cs);
+        uint32_t n = 1;
+        for (uint32_t j = 0; j < nc; ++j)
+            if (expandable(cs[j])) n += count(cs[j]);
+        return n;
+    }
+
+    // Writes slot j of node idx: its box and reference (empty slots get an empty box).
+    void put_slot(uint32_t idx, uint32_t j, const Box& bx, int32_t ref) {
+        float* node = &out[static_cast<size_t>(idx) * 8 * W];
+        for (int a = 0; a < 3; ++a) {
+            node[a * W + j] = bx.lo[a];
+            node[(3 + a) * W + j] = bx.hi[a];
+        }
+        std::memcpy(&node[6 * W + j], &ref, 4);
+    }
+    static int32_t leaf_ref(const Cand& k) { return ~static_cast<int32_t>((k.first << LEAF_COUNT_BITS) | (k.count - 1)); }
+
+    // Writes c's wide node at `idx` and its subtree depth first from `next` (the order a
+    // serial emission gives); returns the subtree's worst-case stack use.
+    uint32_t emit_at(const Cand& c, uint32_t idx, uint32_t& next) {
+        Cand cs[8];
+        const uint32_t nc = slots(c, cs);
         uint32_t sub_max = 0;
         for (uint32_t j = 0; j < W; ++j) {
-            float* node = &out[static_cast<size_t>(idx) * 8 * W];
-            int32_t ref;
-            Box bx = Box::empty();  // empty slots never hit
-            if (j < nc) {
-                const Cand& k = cands[j];
-                bx = k.box;
-                if (!expandable(k)) {
-                    ref = ~static_cast<int32_t>((k.first << LEAF_COUNT_BITS) | (k.count - 1));
-                } else {
-                    uint32_t su = 0;
-                    ref = static_cast<int32_t>(emit(k, su));
-                    sub_max = std::max(sub_max, su);
-                    node = &out[static_cast<size_t>(idx) * 8 * W];  // out may have grown
-                }
+            if (j >= nc) {
+                put_slot(idx, j, Box::empty(), ~0);  // unused: its box is empty
+            } else if (!expandable(cs[j])) {
+                put_slot(idx, j, cs[j].box, leaf_ref(cs[j]));
             } else {
-                ref = ~0;  // unused: its box is empty
+                const uint32_t ci = next++;
+                sub_max = std::max(sub_max, emit_at(cs[j], ci, next));
+                put_slot(idx, j, cs[j].box, static_cast<int32_t>(ci));
             }
-            for (int a = 0; a < 3; ++a) {
-                node[a * W + j] = bx.lo[a];
-                node[(3 + a) * W + j] = bx.hi[a];
-            }
-            std::memcpy(&node[6 * W + j], &ref, 4);
         }
-        stack_use = nc - 1 + sub_max;
-        return idx;
+        return nc - 1 + sub_max;
+    }
+
+    // The whole tree from `root`; returns its worst-case stack use.  For large trees the
+    // top two levels are expanded first, the subtrees below them counted and written on
+    // the pass pool at the indices a serial emission would give them.
+    uint32_t build(const Cand& root, unsigned threads) {
+        if (threads <= 1 || root.count < RefBuilder::SPLIT_PASS) {
+            out.assign(static_cast<size_t>(count(root)) * 8 * W, 0.0f);
+            uint32_t next = 1;
+            return emit_at(root, 0, next);
+        }
+        struct Top {
+            Cand cs[8];
+            uint32_t nc = 0;
+            int32_t kid[8];  // >= 0: a top node; -1: a leaf; <= -2: frontier subtree -(kid + 2)
+        };
+        std::vector<Top> top;
+        std::vector<Cand> frontier;
+        std::function<uint32_t(const Cand&, int)> plan = [&](const Cand& c, int depth) -> uint32_t {
+            const uint32_t t = static_cast<uint32_t>(top.size());
+            top.emplace_back();
+            Top node;
+            node.nc = slots(c, node.cs);
+            for (uint32_t j = 0; j < node.nc; ++j) {
+                if (!expandable(node.cs[j])) {
+                    node.kid[j] = -1;
+                } else if (depth + 1 < 2) {
+                    node.kid[j] = static_cast<int32_t>(plan(node.cs[j], depth + 1));
+                } else {
+                    node.kid[j] = -2 - static_cast<int32_t>(frontier.size());
+                    frontier.push_back(node.cs[j]);
+                }
+            }
+            top[t] = node;
+            return t;
+        };
+        plan(root, 0);
+        const size_t nf = frontier.size();
+        std::vector<uint32_t> fcount(nf), fbase(nf), fsu(nf, 0), tidx(top.size());
+        RefBuilder::in_parts(nf, static_cast<unsigned>(nf), [&](unsigned, size_t b, size_t e) {
+            for (size_t f = b; f < e; ++f) fcount[f] = count(frontier[f]);
+        });
+        uint32_t next = 0;  // depth-first indices, as a serial emission assigns them
+        std::function<void(uint32_t)> number = [&](uint32_t t) {
+            tidx[t] = next++;
+            for (uint32_t j = 0; j < top[t].nc; ++j) {
+                const int32_t k = top[t].kid[j];
+                if (k >= 0) {
+                    number(static_cast<uint32_t>(k));
+                } else if (k <= -2) {
+                    fbase[-2 - k] = next;
+                    next += fcount[-2 - k];
+                }
+            }
+        };
+        number(0);
+        out.assign(static_cast<size_t>(next) * 8 * W, 0.0f);
+        RefBuilder::in_parts(nf, static_cast<unsigned>(nf), [&](unsigned, size_t b, size_t e) {
+            for (size_t f = b; f < e; ++f) {
+                uint32_t nx = fbase[f] + 1;
+                fsu[f] = emit_at(frontier[f], fbase[f], nx);
+            }
+        });
+        std::function<uint32_t(uint32_t)> write = [&](uint32_t t) -> uint32_t {
+            const Top& node = top[t];
+            uint32_t sub_max = 0;
+            for (uint32_t j = 0; j < W; ++j) {
+                if (j >= node.nc) {
+                    put_slot(tidx[t], j, Box::empty(), ~0);
+                } else if (node.kid[j] == -1) {
+                    put_slot(tidx[t], j, node.cs[j].box, leaf_ref(node.cs[j]));
+                } else if (node.kid[j] >= 0) {
+                    sub_max = std::max(sub_max, write(static_cast<uint32_t>(node.kid[j])));
+                    put_slot(tidx[t], j, node.cs[j].box, static_cast<int32_t>(tidx[node.kid[j]]));
+                } else {
+                    const size_t f = static_cast<size_t>(-2 - node.kid[j]);
+                    sub_max = std::max(sub_max, fsu[f]);
+                    put_slot(tidx[t], j, node.cs[j].box, static_cast<int32_t>(fbase[f]));
+                }
+            }
+            return node.nc - 1 + sub_max;
+        };
+        return write(0);
     }
 };
 
@@ -740,7 +979,7 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
 
     // Primitive records: in leaf order for the host build, in component order for the
     // device build (which sorts them itself, bvh_build.cu).
-    out.prims.resize(items.size() * 12, 0.0f);
+    out.prims.resize(items.size() * 12);  // not filled: put_record writes all 12 floats
     if (out.any_normals) out.tri_normal_idx.assign(items.size() * 3, NO_INDEX);
     if (out.any_uvs) out.tri_uv_idx.assign(items.size() * 3, NO_INDEX);
     auto put_record = [&](size_t k, const Item& it) {
@@ -752,7 +991,9 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
             r[2] = d.center[2];
             put_bits(r + 3, it.prim);
             r[4] = d.radius;
+            r[5] = r[6] = 0.0f;
             put_bits(r + 7, 0);
+            r[8] = r[9] = r[10] = 0.0f;
             put_bits(r + 11, PRIM_SPHERE);
         } else {
             const float* a = d.vertices + 3 * d.tri_vertices[3 * it.comp];
@@ -813,10 +1054,7 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
         else
             records(0, 0, recs.size());
         Collapser col(rb.nodes, comp_box, W, L, out.nodes);
-        uint32_t su = 0;
-        Cand rc = col.of_bin(root);
-        col.emit(rc, su);
-        out.stack_depth = su + 1;
+        out.stack_depth = col.build(col.of_bin(root), rb.threads) + 1;
         out.num_wide_nodes = out.nodes.size() / (8 * W);
     }
 
