@@ -269,6 +269,13 @@ struct ServerRequest {
 };
 
 constexpr uint32_t FIRST_CHECKPOINT = 8;
+// Aging of the shortest-remaining-work order.  On the saturated progressive serving
+// workload (24 requests, relMSE 1e-3) p50 / p95 / p99 latency measured 1540 / 4210 /
+// 5612 ms without aging, 1507 / 4120 / 4207 at 1000 ms and 1653 / 3693 / 4066 at 250 ms.
+#ifndef GR_SERVE_AGE_MS
+#define GR_SERVE_AGE_MS 1000.0
+#endif
+constexpr double SERVE_AGE_MS = GR_SERVE_AGE_MS;
 constexpr int EST_BLOCKS = 256;
 
 // Per-block sums of |a - b|^2 and |(accum_a + accum_b) / (weight_a + weight_b)|^2 over the
@@ -360,20 +367,25 @@ gr_status schedule(gr_server* s) {
     if (st != GR_OK) return st;
     uint64_t backlog = c.paths_total - c.gcur;
     const uint64_t want = 2ull * s->engine.capacity();
-    // Shortest remaining work first: passes of the request with the fewest samples left
-    // are appended first, so short requests that arrive behind long ones start within
-    // one backlog (about two pools) of work.
-    std::vector<ServerRequest*> order;
+    // Shortest remaining work first, aged: passes of the request with the fewest samples
+    // left, divided by 1 + (time since submission) / SERVE_AGE_MS, are appended first.
+    // Short requests that arrive behind long ones start within one backlog (about two
+    // pools) of work, and a long request's priority grows as it waits.
+    const double now = s->now_ms();
+    std::vector<std::pair<double, ServerRequest*>> order;
     for (auto& r : s->reqs)
-        if (r->state == GR_REQUEST_RUNNING && r->appended < r->cap()) order.push_back(r.get());
-    std::stable_sort(order.begin(), order.end(), [](ServerRequest* a, ServerRequest* b) {
-        uint64_t ra = static_cast<uint64_t>(a->cap() - a->appended) * a->req.width * a->req.height;
-        uint64_t rb = static_cast<uint64_t>(b->cap() - b->appended) * b->req.width * b->req.height;
-        return ra < rb;
-    });
+        if (r->state == GR_REQUEST_RUNNING && r->appended < r->cap()) {
+            const double left = static_cast<double>(r->cap() - r->appended) * r->req.width * r->req.height;
+            order.emplace_back(left / (1.0 + (now - r->submit_ms) / SERVE_AGE_MS), r.get());
+        }
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<double, ServerRequest*>& a, const std::pair<double, ServerRequest*>& b) {
+                         return a.first < b.first;
+                     });
     std::vector<std::pair<uint32_t, uint32_t>> batch;
     std::vector<ServerRequest*> owners;
-    for (ServerRequest* r : order) {
+    for (auto& o : order) {
+        ServerRequest* r = o.second;
         while (backlog < want && r->appended < r->cap()) {
             const bool odd = r->progressive && (r->appended & 1u);
             batch.emplace_back(odd ? r->job2 : r->job, r->req.params.first_pass + r->appended);
