@@ -21,11 +21,11 @@ constexpr int GATHER_BLOCKS = 512;
 // Path state.  The queue entry of a live path carries its ray, its job (o.w) and its
 // depth (d.w).  Global path p (the paths of all units, in unit order) keeps its state in
 // ring slot p & (ring - 1):
-//   s_hot[2 * slot]     = (throughput.xyz, radiance.x)
+//   s_hot[2 * slot]     = (throughput.xyz, radiance.x); once finished (radiance.xyz, 0)
 //   s_hot[2 * slot + 1] = (radiance.y, radiance.z, key low 32 bits, key high 32 bits)
 //   s_cold[slot]        = (unit, 0, film s bits, film t bits)
 // The hot record is read and written at every bounce and holds the finished sample's
-// radiance; the cold record is written when the path starts.  The gather reads a
+// radiance in its first half; the cold record is written when the path starts.  The gather reads a
 // finished unit's samples straight from its slots, so a slot is reused only once the
 // unit of its previous path is gathered: paths are issued up to `ring` past the oldest
 // ungathered one.  At most `capacity` paths are live (the queues' size).
@@ -136,10 +136,10 @@ struct RingSamples {
     uint32_t width, mask;
     GR_D void operator()(uint32_t r, uint32_t col, float2& st, V3& rgb) const {
         size_t slot = static_cast<size_t>((prefix + static_cast<unsigned long long>(r) * width + col) & mask);
-        float4 a = hot[2 * slot], b = hot[2 * slot + 1];
+        float4 a = hot[2 * slot];  // (radiance, 0) of the finished path
         uint4 cd = cold[slot];
         st = make_float2(__uint_as_float(cd.z), __uint_as_float(cd.w));
-        rgb = V3{a.w, b.x, b.y};
+        rgb = V3{a.x, a.y, a.z};
     }
 };
 
@@ -313,9 +313,15 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
                     }
                     alive = !is_zero(tp) && (J.max_depth == 0 || depth + 1 < J.max_depth);
                 }
-                // The hot record keeps the radiance of a finished path: the gather reads it.
-                s_hot[hs] = make_float4(tp.x, tp.y, tp.z, L.x);
-                s_hot[hs + 1] = make_float4(L.y, L.z, hb.z, hb.w);
+                // A live path keeps (throughput, radiance, key); a finished one leaves its
+                // radiance in the first half, which with the cold record's film position
+                // is all the gather reads.
+                if (alive) {
+                    s_hot[hs] = make_float4(tp.x, tp.y, tp.z, L.x);
+                    s_hot[hs + 1] = make_float4(L.y, L.z, hb.z, hb.w);
+                } else {
+                    s_hot[hs] = make_float4(L.x, L.y, L.z, 0.0f);
+                }
                 if (!alive) {
                     finished = true;
                     unit = s_cold[slot].x;
