@@ -317,6 +317,7 @@ SIGNATURES = {
     "gr_render_batch": (C.c_int, [C.POINTER(Job), C.c_uint32, C.POINTER(BatchOptions)]),
     "gr_batch_autotune": (C.c_int, [C.POINTER(Job), C.c_uint32, C.POINTER(BatchOptions)]),
     "gr_batch_last_stats": (C.c_int, [C.POINTER(RenderStats)]),
+    "gr_batch_release": (C.c_int, []),
     "gr_server_create": (C.c_int, [C.POINTER(ServerOptions), C.POINTER(_VP)]),
     "gr_server_destroy": (C.c_int, [_VP]),
     "gr_server_submit": (C.c_int, [_VP, C.POINTER(Request), C.POINTER(C.c_uint64)]),

@@ -48,6 +48,11 @@ def render_batch(jobs, lib, path_capacity: int = 0, block_size: int = 0) -> _abi
     return st
 
 
+def release(lib):
+    """gr_batch_release: frees the engines kept for reuse between batches."""
+    lib.call("gr_batch_release")
+
+
 def autotune(jobs, lib) -> _abi.BatchOptions:
     arr = _descs(jobs)
     opt = _abi.BatchOptions()

@@ -171,6 +171,13 @@ gr_status gr_render_batch(const gr_job* jobs, uint32_t n, const gr_batch_options
     return GR_OK;
 }
 
+gr_status gr_batch_release(void) {
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    g_cache.clear();  // each engine waits for its stream, then frees its buffers
+    g_cache_used.clear();
+    return GR_OK;
+}
+
 gr_status gr_batch_last_stats(gr_render_stats* out) {
     if (!out) {
         set_error("null argument");

@@ -399,6 +399,10 @@ gr_status gr_render_batch(const gr_job* jobs, uint32_t n, const gr_batch_options
 gr_status gr_batch_autotune(const gr_job* jobs, uint32_t n, gr_batch_options* out);
 /* Counters of the last gr_render_batch on this thread. */
 gr_status gr_batch_last_stats(gr_render_stats* out);
+/* Frees the engines gr_render_batch keeps for reuse (the two most recently used
+ * configurations; an engine of 64 M paths holds about 18 GB of device memory).  The
+ * next batch sets its engine up again.  No counterpart in the reference. */
+gr_status gr_batch_release(void);
 
 /* -------------------------------------------------------------------- serving */
 

@@ -583,6 +583,8 @@ gr_status gr_batch_autotune(const gr_job*, uint32_t, gr_batch_options* out) {
     return GR_OK;
 }
 
+gr_status gr_batch_release(void) { return GR_OK; }  // the CPU restatement caches nothing
+
 gr_status gr_batch_last_stats(gr_render_stats* out) {
     if (!out) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
     std::memset(out, 0, sizeof(*out));

@@ -38,6 +38,21 @@ def test_batch_equals_per_image(gpu):
         assert j.film.passes() == j.spp
 
 
+def test_batch_release_frees_the_engine(gpu):
+    import torch
+    ws = small_workloads(2)
+    jobs = [batch.Job(g.Stage(w.prims, lib=gpu, environment=w.environment), w.camera, w.integrator,
+                      g.Film(w.width, w.height, lib=gpu), w.spp) for w in ws]
+    batch.render_batch(jobs, gpu, path_capacity=1 << 23)  # about 2.4 GB of queues and ring
+    torch.cuda.synchronize()
+    held = torch.cuda.mem_get_info()[0]
+    batch.release(gpu)
+    freed = torch.cuda.mem_get_info()[0] - held
+    assert freed > 1 << 30, freed
+    batch.render_batch(jobs, gpu, path_capacity=1 << 23)  # set up again
+    assert all(j.film.passes() == 2 * j.spp for j in jobs)
+
+
 def test_batch_autotune_and_display(gpu):
     ws = small_workloads(3)
     jobs = []
