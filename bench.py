@@ -59,6 +59,8 @@ def parse():
                     help="relMSE target of the progressive serving leg (0: skip it)")
     ap.add_argument("--profile-bdpt", action="store_true",
                     help="with --profile-case: the BDPT workload (512x512, MIS + light tracing)")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="with --profile-case: the 64-scene batch, rendered per image and then in one batch")
     ap.add_argument("--profile-case", action="store_true",
                     help="render the workload once (untimed, --spp passes) and exit: the small case for ncu")
     return ap.parse_args()
@@ -564,9 +566,22 @@ def run_bdpt(lib, cpu_seconds):
 
 def profile_case(args):
     import gammaray_gb300 as g
-    from gammaray_gb300 import scenes
+    from gammaray_gb300 import batch, scenes
 
     lib = g.load()
+    if args.profile_batch:  # the batch line's 64 scenes: per image, then one batch (64 M paths)
+        ws = scenes.batch_scenes(64)
+        stages = [g.Stage(w.prims, lib=lib, environment=w.environment, seed=k) for k, w in enumerate(ws)]
+
+        def jobs():
+            return [batch.Job(st, w.camera, w.integrator, g.Film(w.width, w.height, lib=lib), w.spp)
+                    for st, w in zip(stages, ws)]
+
+        dev = batch.render_individually(jobs(), lib)
+        st = batch.render_batch(jobs(), lib, 1 << 26, 256)
+        print(json.dumps({"profile_case": "batch_64_scenes", "per_image_device_ms": dev, "batch_device_ms": st.device_ms,
+                          "samples": int(st.samples), "rays": int(st.extension_rays)}))
+        return
     if args.profile_bdpt:  # the BDPT line's scene and integrator (MIS + light tracing)
         w = scenes.displaced_sphere(512, 512, args.spp or 1, bdpt=True)
         w.integrator = g.BdptIntegrator(max_depth=10, rr_depth=4, mis=1, light_tracing=1)
