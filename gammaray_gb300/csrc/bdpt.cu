@@ -9,10 +9,13 @@
 //   shade     random_walk (integrators.rs:138-229) for both walks: Material::sample_world,
 //             throughput, shading-normal correction on light paths, roulette from
 //             length rr_len; each vertex is stored SoA, the escape vertex too
+//   order     paths counting-sorted by (camera, light) walk length, so the connection
+//             kernels' warps run loops of equal trip counts
 //   connect   per path, every strategy (c >= 1, l >= 0, c + l <= max) in the reference's
 //             loop order: connect() (integrators.rs:269-343) without the visibility test,
-//             times its weight; terms that need one queue a shadow ray.  With light
-//             tracing, every light-walk vertex inside the image also gets a camera term.
+//             times its weight; terms that need one queue a shadow ray
+//   light_trace  with light tracing, every light-walk vertex inside the image gets a
+//             camera term (its own kernel)
 //   shadow    Bvh::visibility (bvh.rs:460-477) as an any-hit query
 //   gather    per path, sums the weighted strategy terms in loop order (deterministic,
 //             same order as the reference); visible light-tracing terms are added to
@@ -341,7 +344,8 @@ GR_D uint32_t num_entries(uint32_t cs, uint32_t ls, uint32_t max_len) {
 // side (arev), ratios of neighbouring strategies' pdfs chained outwards from the
 // connection, delta (specular) vertices skipped and zero pdfs counted as 1.  The
 // strategies are (c camera-walk, l light-walk vertices), c + l <= max_len, and with
-// light tracing also c = 0.  The oracle states the same function (orender.hpp).
+// light tracing also c = 0.  The oracle states the same weight as a loop over the
+// strategies (orender.hpp, mis_weight); WalkMis below regroups it.
 
 // Area pdf with which Bvh::sample_light picks a point of light prim `prim`
 // (bvh.rs:481-496, mesh.rs:310-327, sphere.rs:103-111).
