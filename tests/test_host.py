@@ -89,6 +89,28 @@ def test_threaded_host_build_is_the_reference_tree(oracle):
         assert a.tree_hash == b.tree_hash != 0
 
 
+def test_concurrent_host_builds_share_the_pass_pool(oracle):
+    # Two host threads building at once (ctypes releases the GIL) share the library's
+    # pass pool; each tree must still be the serial restatement's.
+    import threading
+
+    lib = gpu_lib()
+    scenes_ = [scenes.displaced_sphere(8, 8, 1, tris=90_000).prims, scenes.displaced_sphere(8, 8, 1, tris=60_000).prims]
+    want = [g.api.plan_scene(p, lib=oracle).tree_hash for p in scenes_]
+    got = [[], []]
+
+    def worker(k):
+        for _ in range(3):
+            got[k].append(g.api.plan_scene(scenes_[k], lib=lib).tree_hash)
+
+    th = [threading.Thread(target=worker, args=(k,)) for k in (0, 1)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert got[0] == [want[0]] * 3 and got[1] == [want[1]] * 3
+
+
 def test_wide_collapse_shrinks_with_width():
     lib = gpu_lib()
     w = scenes.displaced_sphere(8, 8, 1, tris=20_000)
