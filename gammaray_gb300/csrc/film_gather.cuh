@@ -40,9 +40,15 @@ GR_D float mitchell1(float x) {
 // increasing sample index, the reference's order.
 constexpr int FILM_WIN = 2 * FILM_HALO + 1;                      // 9
 constexpr int FILM_MASK_WORDS = (FILM_WIN * FILM_WIN + 31) / 32;  // 3
+// A sample's footprint spans at most 5 columns and 5 rows (film.rs:90-97); its Mitchell
+// factors for the tile columns and rows it covers are evaluated once when it is staged:
+// mx[j][k] = mitchell1((cb + j - col_discr) / 2) for tile column cb + j, and my likewise,
+// so a pixel's weight is mx * my, the reference's product of the same two factors.
+constexpr int FILM_FOOT = 5;
 struct StagedSample {
-    float cd[FILM_SPAN * FILM_SPAN], rd[FILM_SPAN * FILM_SPAN];  // col_discr, row_discr
     float r[FILM_SPAN * FILM_SPAN], g[FILM_SPAN * FILM_SPAN], b[FILM_SPAN * FILM_SPAN];
+    float mx[FILM_FOOT][FILM_SPAN * FILM_SPAN], my[FILM_FOOT][FILM_SPAN * FILM_SPAN];
+    uint8_t cb[FILM_SPAN * FILM_SPAN], rb[FILM_SPAN * FILM_SPAN];  // first covered tile column / row
     uint32_t mask[FILM_TILE * FILM_TILE][FILM_MASK_WORDS];
 };
 
@@ -101,8 +107,6 @@ GR_D void gather_passes(StagedSample& sm, uint32_t width, uint32_t height, int o
             float col_cont = lerp(0.0f, wf, 0.5f * (s.x + 1.0f));
             float row_cont = lerp(0.0f, hf, 0.5f * (s.y + 1.0f));
             float cd = col_cont - 0.5f, rd = row_cont - 0.5f;
-            sm.cd[k] = cd;
-            sm.rd[k] = rd;
             sm.r[k] = rc[j].x;
             sm.g[k] = rc[j].y;
             sm.b[k] = rc[j].z;
@@ -118,6 +122,16 @@ GR_D void gather_passes(StagedSample& sm, uint32_t width, uint32_t height, int o
             mxr = mxr < 0 ? 0 : (mxr > last_row ? last_row : mxr);
             int c0 = max(0, static_cast<int>(mnc) - ox), c1 = min(FILM_TILE - 1, static_cast<int>(mxc) - ox);
             int r0 = max(0, static_cast<int>(mnr) - oy), r1 = min(FILM_TILE - 1, static_cast<int>(mxr) - oy);
+            if (c0 > c1 || r0 > r1) continue;  // covers no pixel of this tile
+            sm.cb[k] = static_cast<uint8_t>(c0);
+            sm.rb[k] = static_cast<uint8_t>(r0);
+            // film.rs:100-106 factors, the arguments as the pixel loop below forms them
+#pragma unroll
+            for (int f = 0; f < FILM_FOOT; ++f)
+                if (f <= c1 - c0) sm.mx[f][k] = mitchell1((static_cast<float>(ox + c0 + f) - cd) / 2.0f);
+#pragma unroll
+            for (int f = 0; f < FILM_FOOT; ++f)
+                if (f <= r1 - r0) sm.my[f][k] = mitchell1((static_cast<float>(oy + r0 + f) - rd) / 2.0f);
             for (int py = r0; py <= r1; ++py)
                 for (int px = c0; px <= c1; ++px) {
                     int bit = (ky - py) * FILM_WIN + (kx - px);
@@ -135,8 +149,7 @@ GR_D void gather_passes(StagedSample& sm, uint32_t width, uint32_t height, int o
                 m &= m - 1;
                 int dy = bit / FILM_WIN, dx = bit - dy * FILM_WIN;
                 int k = (ty + dy) * FILM_SPAN + (tx + dx);
-                float wgt = mitchell1((static_cast<float>(x) - sm.cd[k]) / 2.0f) *
-                            mitchell1((static_cast<float>(y) - sm.rd[k]) / 2.0f);
+                float wgt = sm.mx[tx - sm.cb[k]][k] * sm.my[ty - sm.rb[k]][k];
                 acc.x = acc.x + sm.r[k] * wgt;
                 acc.y = acc.y + sm.g[k] * wgt;
                 acc.z = acc.z + sm.b[k] * wgt;
