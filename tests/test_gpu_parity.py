@@ -284,6 +284,47 @@ def test_bdpt_image_statistics(gpu, oracle):
     assert gpu.backend == "cuda-sm_103a"
 
 
+def test_bdpt_groups_do_not_change_the_film(gpu, monkeypatch):
+    # Paths in flight only decide how passes are grouped: random streams are keyed by
+    # pass, and each path's strategies are summed in loop order, so with MIS (and no
+    # light-tracing splats, whose atomics add in any order) the film is bit-identical
+    # whether a render runs as one group or as many.
+    w = scenes.cornell_spheres(32, 32, 6)
+    st = g.Stage(w.prims, lib=gpu, seed=12)
+    films = []
+    for paths in (None, "1024"):
+        if paths is None:
+            monkeypatch.delenv("GR_BDPT_PATHS_IN_FLIGHT", raising=False)
+        else:
+            monkeypatch.setenv("GR_BDPT_PATHS_IN_FLIGHT", paths)  # one 32x32 pass per group
+        st._pass = 0
+        f = g.Film(32, 32, lib=gpu)
+        st.render(w.camera, g.BdptIntegrator(max_depth=8, mis=1), f, 6)
+        films.append(f.read())
+    np.testing.assert_array_equal(films[0][0], films[1][0])
+    np.testing.assert_array_equal(films[0][1], films[1][1])
+
+
+def test_pt_groups_do_not_change_the_film(gpu, monkeypatch):
+    # The path tracer's film is bit-identical whether the passes run as one group of
+    # paths in flight or one pass per group (the deterministic gather adds them in pass
+    # order either way).
+    w = scenes.displaced_sphere(40, 40, 5)
+    st = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=4)
+    films = []
+    for paths in (None, "1600"):
+        if paths is None:
+            monkeypatch.delenv("GR_PATHS_IN_FLIGHT", raising=False)
+        else:
+            monkeypatch.setenv("GR_PATHS_IN_FLIGHT", paths)
+        st._pass = 0
+        f = g.Film(40, 40, lib=gpu)
+        st.render(w.camera, w.integrator, f, 5)
+        films.append(f.read())
+    np.testing.assert_array_equal(films[0][0], films[1][0])
+    np.testing.assert_array_equal(films[0][1], films[1][1])
+
+
 def test_bdpt_counts_shadow_rays(gpu):
     w = scenes.cornell_spheres(32, 32, 2)
     st = g.Stage(w.prims, lib=gpu, seed=1)
