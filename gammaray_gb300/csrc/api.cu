@@ -51,6 +51,7 @@ gr_status sync_check(cudaStream_t st, const char* what, uint32_t bounce, uint32_
             std::string msg = std::string(what) + " did not finish within " + std::to_string(limit) + " s (bounce " +
                               std::to_string(bounce) + ", capacity " + std::to_string(n) + ")";
             std::fprintf(stderr, "gammaray: %s\n", msg.c_str());
+            cudaEventDestroy(ev);  // released once the work before it completes
             return fail(GR_ERR_TIMEOUT, msg);
         }
         std::this_thread::sleep_for(std::chrono::microseconds(200));

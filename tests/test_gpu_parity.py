@@ -325,6 +325,37 @@ def test_pt_groups_do_not_change_the_film(gpu, monkeypatch):
     np.testing.assert_array_equal(films[0][1], films[1][1])
 
 
+def test_sync_check_reports_a_slow_launch(gpu):
+    # GR_SYNC_CHECK bounds every host wait of a render.  With a limit no launch can meet,
+    # the render returns GR_ERR_TIMEOUT naming the kernel, the work in flight finishes
+    # normally, and the context stays usable.  (A subprocess: the limit is read once.)
+    import os
+    import subprocess
+    import sys
+
+    code = """
+import torch
+import gammaray_gb300 as g
+from gammaray_gb300 import _abi, scenes
+w = scenes.displaced_sphere(256, 256, 4)
+st = g.Stage(w.prims, environment=w.environment)
+f = g.Film(256, 256)
+try:
+    st.render(w.camera, w.integrator, f, 4)
+    print("NO_TIMEOUT")
+except _abi.GrError as e:
+    print("TIMEOUT", e)
+torch.cuda.synchronize()
+print("OK", torch.ones(1024, device="cuda").sum().item())
+"""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GR_SYNC_CHECK="1e-9", PYTHONPATH=root)
+    r = subprocess.run([sys.executable, "-c", code], env=env, cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "TIMEOUT" in r.stdout and "did not finish" in r.stdout, r.stdout
+    assert "OK 1024.0" in r.stdout, r.stdout
+
+
 def test_bdpt_counts_shadow_rays(gpu):
     w = scenes.cornell_spheres(32, 32, 2)
     st = g.Stage(w.prims, lib=gpu, seed=1)
