@@ -109,6 +109,8 @@ class SceneInfo(C.Structure):
         ("bvh_width", C.c_uint32),
         ("build_seconds", C.c_double),
         ("tree_hash", C.c_uint64),
+        ("stack_depth", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 

@@ -257,6 +257,7 @@ gr_status gr_scene_plan(const gr_scene_desc* desc, gr_scene_info* o) {
     o->bvh_width = h.width;
     o->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     o->tree_hash = h.tree_hash;
+    o->stack_depth = h.stack_depth;
     return GR_OK;
 }
 
@@ -281,6 +282,7 @@ gr_status gr_scene_get_info(const gr_scene* s, gr_scene_info* o) {
     o->num_lights = static_cast<uint32_t>(s->host.lights.size());
     o->bvh_width = s->host.width;
     o->build_seconds = s->build_seconds;
+    o->stack_depth = s->host.stack_depth;
     return GR_OK;
 }
 

@@ -165,6 +165,9 @@ constexpr int PRIM_SPHERE = 1;
 
 // Leaf reference in a wide node child slot: child < 0, ~child = (first << 4) | (count - 1).
 constexpr int LEAF_COUNT_BITS = 4;
+// Traversal stack entries a ray may need (the tree's worst case); the host and device
+// builds reject trees that exceed it.
+constexpr int MAX_STACK = 96;
 constexpr int MAX_LEAF_PRIMS = 1 << LEAF_COUNT_BITS;
 
 }  // namespace gr

@@ -1055,6 +1055,11 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
             records(0, 0, recs.size());
         Collapser col(rb.nodes, comp_box, W, L, out.nodes);
         out.stack_depth = col.build(col.of_bin(root), rb.threads) + 1;
+        if (out.stack_depth > static_cast<uint32_t>(MAX_STACK)) {
+            err = "BVH too deep: traversal needs " + std::to_string(out.stack_depth) + " stack entries (limit " +
+                  std::to_string(MAX_STACK) + ")";
+            return false;
+        }
         out.num_wide_nodes = out.nodes.size() / (8 * W);
     }
 

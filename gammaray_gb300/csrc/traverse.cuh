@@ -198,8 +198,7 @@ namespace gr {
 // its first SMEM_STACK entries in this thread's shared-memory column and spills deeper
 // entries to a per-thread local array (rarely touched, cached in L1), so the shared
 // footprint no longer scales with the tree's worst-case depth.
-constexpr int SMEM_STACK = 16;
-constexpr int MAX_STACK = 96;  // the build rejects trees whose worst case exceeds this
+constexpr int SMEM_STACK = 16;  // MAX_STACK (common.cuh): both builds reject deeper trees
 
 struct TravState {
     V3 o, d, inv;

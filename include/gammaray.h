@@ -158,6 +158,10 @@ typedef struct gr_scene_info {
     uint64_t tree_hash;        /* gr_scene_plan only: FNV-1a over the binary tree in depth-first
                                   order (each node's box; each leaf's prim and component ids);
                                   equal for equal trees.  0 elsewhere and for device builds. */
+    uint32_t stack_depth;      /* worst-case traversal stack entries of the wide BVH (at most
+                                  96: deeper trees are rejected); 0 for the CPU restatement
+                                  and in gr_scene_plan for device builds */
+    uint32_t reserved;
 } gr_scene_info;
 
 /* Replaces Stage::new / Bvh::build (render/stage.rs:15-20, geom/bvh.rs:339-382):

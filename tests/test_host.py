@@ -129,6 +129,23 @@ def test_plan_rejects_bad_input():
         g.api.plan_scene([m], lib=lib)
 
 
+def test_plan_reports_and_bounds_the_stack_depth():
+    # The build reports the wide tree's worst-case traversal stack and rejects trees
+    # deeper than the traversal's 96 entries (the reference itself panics past its
+    # 64-entry binary stack, geom/bvh.rs:156): spheres at x = r^k split one at a time.
+    lib = gpu_lib()
+    mat = g.Material.disney().build()
+
+    def spheres(r, n):
+        return [g.Sphere(mat, g.Mat.translation((float(x), 0.0, 0.0)), float(x) * 1e-3) for x in r ** np.arange(n)]
+
+    info = g.api.plan_scene(spheres(1.05, 600), lib=lib)
+    assert 0 < info.stack_depth <= 96
+    assert g.api.plan_scene(scenes.cornell_spheres().prims, lib=lib).stack_depth > 0
+    with pytest.raises(_abi.GrError, match="too deep"):
+        g.api.plan_scene(spheres(1.1, 600), lib=lib)
+
+
 def test_large_mesh_reports_the_first_bad_triangle(oracle):
     # A mesh this large is validated on threads; the error is still the first failing
     # triangle's (here a uv index at triangle 5,000 before a vertex index at 30,000).
