@@ -504,6 +504,10 @@ gr_status gr_server_submit(gr_server* s, const gr_request* r, uint64_t* id) {
         set_error("request scene has a different BVH width than the server");
         return GR_ERR_INVALID_ARGUMENT;
     }
+    if (static_cast<uint64_t>(r->width) * r->height * 2 > s->engine.ring()) {
+        set_error("request image too large for the server's path ring (raise path_capacity)");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
     std::lock_guard<std::mutex> g(s->mu);
     std::unique_ptr<ServerRequest> q(new ServerRequest());
     q->id = s->next_id++;

@@ -98,6 +98,7 @@ class Engine {
     const std::vector<DevUnit>& units() const { return h_units_; }
     const std::vector<DevJob>& jobs() const { return h_jobs_; }
     uint32_t capacity() const { return cfg_.capacity; }
+    uint32_t ring() const { return ring_; }  // path state slots; an image may use half
     const EngineConfig& config() const { return cfg_; }
     uint64_t rays() const { return last_rays_; }
     uint64_t device_bytes() const { return bytes_; }

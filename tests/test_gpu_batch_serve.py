@@ -94,6 +94,19 @@ def test_server_alone_equals_mixed(gpu):
     np.testing.assert_allclose(ref.read()[0], a_acc, rtol=1e-6, atol=1e-7)
 
 
+def test_server_rejects_an_image_too_large_for_its_ring(gpu):
+    # The check is at submission: an oversized request must not fail the steps that
+    # serve the others.  A 64 k-path server keeps an 8 M-slot ring (images up to 4 M px).
+    w = small_workloads(1)[0]
+    st = g.Stage(w.prims, lib=gpu, environment=w.environment)
+    s = serve.Server(gpu, path_capacity=1 << 16)
+    ok = s.submit(st, w.camera, w.integrator, w.width, w.height, 2)
+    with pytest.raises(Exception, match="path ring"):
+        s.submit(st, w.camera, w.integrator, 4096, 2048, 1)
+    s.run_until_done([ok])
+    assert s.poll(ok).state == 2
+
+
 def test_server_admission_and_cancel(gpu):
     w = small_workloads(1)[0]
     st = g.Stage(w.prims, lib=gpu, environment=w.environment)
