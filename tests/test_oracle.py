@@ -156,6 +156,56 @@ def test_sampling_matches_pdf(oracle, name):
     assert abs(est.mean() - math.pi) < 5 * se + 2e-3, (est.mean(), se)
 
 
+def sampling_chi2(oracle, m, n=200_000, nt=16, nph=32, sub=6):
+    """The directions sample_world draws, binned over the sphere (16 in cos(theta) x 32
+    in phi, equal solid angle), against pdf_world integrated over each bin on a 6 x 6
+    grid.  Draws that leave the hemisphere are rejected (pdf 0) and pdf_world is the
+    density of the rest, so the bins follow n * mass.  Returns (total pdf mass, accepted
+    fraction, Pearson chi-square p-value)."""
+    from scipy import stats
+
+    fr = np.zeros(1, _abi.FRAME_DTYPE)
+    fr["normal"], fr["tangent"], fr["binormal"], fr["geom_normal"] = (0, 0, 1), (1, 0, 0), (0, 1, 0), (0, 0, 1)
+    wi = np.array([[math.sin(0.6), 0.0, math.cos(0.6)]], np.float32)
+    u = np.random.default_rng(3).random((n, 3), dtype=np.float32)
+    s = g.bsdf_sample(m, np.repeat(fr, n), np.repeat(wi, n, axis=0), u, lib=oracle)
+    ok = (s["kind"] != 0) & (s["pdf"] > 0)
+    o = s["outgoing"][ok].astype(np.float64)
+    o /= np.linalg.norm(o, axis=1, keepdims=True)
+    ci = np.clip(((o[:, 2] + 1.0) * 0.5 * nt).astype(int), 0, nt - 1)
+    pi = np.clip((np.mod(np.arctan2(o[:, 1], o[:, 0]), 2 * math.pi) / (2 * math.pi) * nph).astype(int), 0, nph - 1)
+    counts = np.bincount(ci * nph + pi, minlength=nt * nph).astype(np.float64)
+    cz = -1.0 + (np.arange(nt * sub) + 0.5) * (2.0 / (nt * sub))
+    ph = (np.arange(nph * sub) + 0.5) * (2 * math.pi / (nph * sub))
+    zz, pp = np.meshgrid(cz, ph, indexing="ij")
+    rr = np.sqrt(np.maximum(0.0, 1.0 - zz * zz))
+    wo = np.stack([rr * np.cos(pp), rr * np.sin(pp), zz], axis=-1).reshape(-1, 3).astype(np.float32)
+    k = len(wo)
+    pdf = g.bsdf_pdf(m, np.repeat(fr, k), np.repeat(wi, k, axis=0), wo, lib=oracle).reshape(nt, sub, nph, sub)
+    mass = pdf.mean(axis=(1, 3)).reshape(-1) * (4 * math.pi / (nt * nph))
+    expected = mass * n
+    big = expected >= 20.0
+    e = np.append(expected[big], expected[~big].sum())
+    c = np.append(counts[big], counts[~big].sum())
+    keep = e > 0
+    chi2 = float(((c[keep] - e[keep]) ** 2 / e[keep]).sum())
+    return float(mass.sum()), float(ok.mean()), float(stats.chi2.sf(chi2, int(keep.sum()) - 1))
+
+
+@pytest.mark.parametrize("name", ["disney_default", "rough_sheen", "metal_aniso", "perfect_diffuse"])
+def test_sampling_histogram_chi2(oracle, name):
+    mass, accepted, p = sampling_chi2(oracle, REFLECTION_MATERIALS[name]())
+    assert abs(mass - accepted) < 0.01, (mass, accepted)
+    assert p > 1e-4, p
+
+
+def test_sampling_chi2_detects_the_gtr1_pdf_quirk(oracle):
+    # The same check on the clearcoat lobe, whose pdf lacks cos(theta_h)
+    # (material/util.rs:305-308): its pdf mass no longer matches the accepted draws.
+    mass, accepted, p = sampling_chi2(oracle, REFLECTION_MATERIALS["clearcoat"]())
+    assert abs(mass - accepted) > 0.01 or p < 1e-6, (mass, accepted, p)
+
+
 def test_clearcoat_pdf_quirk(oracle):
     # GTR1 samples the half vector with density D(h) cos(theta_h), but its pdf() returns
     # D(h) alone (material/util.rs:291-308), so pdf_world over-states the density by
