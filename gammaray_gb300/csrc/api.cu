@@ -484,7 +484,7 @@ static gr_status run_render(gr_scene* s, const gr_camera* c, const gr_render_par
     if (cnt[CNT_ERROR] == 2)
         return fail(GR_ERR_TIMEOUT, "traversal step budget exceeded (ray " + std::to_string(cnt[CNT_ERROR + 1]) + ")");
     if (cnt[CNT_ERROR]) return fail(GR_ERR_STACK_OVERFLOW, "traversal stack bound exceeded");
-    return GR_OK;
+    return p->integrator == GR_INTEGRATOR_BDPT ? bdpt_index_check() : pt_index_check();
 }
 
 gr_status gr_render(gr_scene* s, const gr_camera* c, const gr_render_params* p, gr_film* f) {

@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams
         }
         flags[i] = fl;
     }
-    push_warp(cam_alive, count_out, 2 * i, co, cd, nslot, no, nd);
-    push_warp(light_alive, count_out, 2 * i + 1, lo, ld, nslot, no, nd);
+    push_warp(cam_alive, count_out, 2 * i, co, cd, nslot, no, nd, p.nslots);
+    push_warp(light_alive, count_out, 2 * i + 1, lo, ld, nslot, no, nd, p.nslots);
 }
 
 constexpr uint32_t BSHADE_PER_THREAD = SHADE_PER_THREAD;
@@ -326,11 +326,16 @@ __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts 
                     if (alive) tp_buf[slot] = make_float4(ntp.x, ntp.y, ntp.z, delta ? 0.0f : ms.pdf);
                 }
             }
-            push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
+            push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd, p.nslots);
         }
         __syncthreads();  // sm is reused by the next chunk
     }
 }
+
+// Capacities of the strategy entries and of the shadow queue, as BdptState::ensure sizes
+// them (checked builds test every write against them).
+GR_D size_t entry_cap(const BdptParams& p) { return static_cast<size_t>(p.n) * (p.max_len * (p.max_len + 1) / 2); }
+GR_D size_t shadow_cap(const BdptParams& p) { return entry_cap(p) + (p.lt ? static_cast<size_t>(p.n) * p.max_len : 0); }
 
 GR_D uint32_t num_entries(uint32_t cs, uint32_t ls, uint32_t max_len) {
     uint32_t e = 0;
@@ -601,8 +606,9 @@ __global__ void __launch_bounds__(BLOCK, GR_CONNECT_MIN_BLOCKS) k_bdpt_connect(D
                         flag = E_PENDING;
                         uint32_t sq = agg_inc(counters + CNT_SHADOWQ);
                         // float4 index of field 0 (point) of each vertex
-                        shadow_q[sq] = make_uint4(j, (c - 1) * VREC * p.nslots + 2 * i,
-                                                  (l - 1) * VREC * p.nslots + 2 * i + 1, 0);
+                        if (GR_IN_RANGE(sq, shadow_cap(p)))
+                            shadow_q[sq] = make_uint4(j, (c - 1) * VREC * p.nslots + 2 * i,
+                                                      (l - 1) * VREC * p.nslots + 2 * i + 1, 0);
                     }
                 }
             }
@@ -610,7 +616,7 @@ __global__ void __launch_bounds__(BLOCK, GR_CONNECT_MIN_BLOCKS) k_bdpt_connect(D
             if (!p.mis) w = 1.0f / static_cast<float>(c + l + extra);  // integrators.rs:345-354
             else w = is_zero(term) ? 0.0f : strategy_weight(s, vs, i, cw, lw, c, l, cv, l ? &lv : nullptr, ez, ey);
             term = term * w;
-            entries[j] = make_float4(term.x, term.y, term.z, flag);
+            if (GR_IN_RANGE(j, entry_cap(p))) entries[j] = make_float4(term.x, term.y, term.z, flag);
             ++j;
         }
     }
@@ -671,7 +677,8 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_light_trace(DeviceScene s, BdptP
                     pix = row * p.width + col;
                     out = make_float4(L.x, L.y, L.z, E_PENDING);
                     uint32_t sq = agg_inc(counters + CNT_SHADOWQ);
-                    shadow_q[sq] = make_uint4(static_cast<uint32_t>(e), (l - 1) * VREC * p.nslots + 2 * i + 1, 0, 1);
+                    if (GR_IN_RANGE(sq, shadow_cap(p)))
+                        shadow_q[sq] = make_uint4(static_cast<uint32_t>(e), (l - 1) * VREC * p.nslots + 2 * i + 1, 0, 1);
                 }
             }
         }
@@ -967,6 +974,18 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     }
     sc->stats.samples += static_cast<uint64_t>(total) * npix;
     sc->stats.kernel_launches += launches;
+    return GR_OK;
+}
+
+gr_status bdpt_index_check() {
+#if GR_CHECKED
+    bool bad = false;
+    GR_CUDA_TRY(take_bad_index(bad));
+    if (bad) {
+        set_error("BDPT: a queue or entry index was out of range (checked build)");
+        return GR_ERR_INTERNAL;
+    }
+#endif
     return GR_OK;
 }
 

@@ -14,7 +14,30 @@
 #define GR_HD __host__ __device__ __forceinline__
 #define GR_D __device__ __forceinline__
 
+// Checked build (-DGR_CHECKED=1, the stand-in for a memory checker): every queue, entry
+// and shadow-queue write tests its index against its buffer's capacity, skips the write
+// when it is out of range and sets this file's flag, which the host reads after the
+// render (GR_ERR_INTERNAL).  Off by default; then GR_IN_RANGE is `true`.
+#ifndef GR_CHECKED
+#define GR_CHECKED 0
+#endif
+
 namespace gr {
+
+#if GR_CHECKED && defined(__CUDACC__)
+static __device__ unsigned int g_bad_index = 0u;
+#define GR_IN_RANGE(i, n) ((i) < (n) || (atomicExch(&g_bad_index, 1u), false))
+// Reads and clears this file's flag (host).
+static inline cudaError_t take_bad_index(bool& bad) {
+    unsigned int v = 0u, z = 0u;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_bad_index, sizeof(v));
+    if (e == cudaSuccess && v) e = cudaMemcpyToSymbol(g_bad_index, &z, sizeof(z));
+    bad = v != 0u;
+    return e;
+}
+#else
+#define GR_IN_RANGE(i, n) true
+#endif
 
 constexpr float EPS = FLT_EPSILON;
 constexpr float PI = 3.14159265358979323846f;

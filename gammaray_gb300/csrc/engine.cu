@@ -30,7 +30,7 @@ constexpr int GATHER_BLOCKS = 512;
 // unit of its previous path is gathered: paths are issued up to `ring` past the oldest
 // ungathered one.  At most `capacity` paths are live (the queues' size).
 GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t job, uint32_t depth,
-                   uint32_t* __restrict__ nslot, float4* __restrict__ no, float4* __restrict__ nd) {
+                   uint32_t* __restrict__ nslot, float4* __restrict__ no, float4* __restrict__ nd, uint32_t cap) {
     const unsigned lane = threadIdx.x & 31;
     unsigned m = __ballot_sync(0xffffffffu, alive);
     if (!m) return;
@@ -40,6 +40,7 @@ GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, u
     base = __shfl_sync(0xffffffffu, base, leader);
     if (alive) {
         uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
+        if (!GR_IN_RANGE(pos, cap)) return;
         nslot[pos] = slot;
         no[pos] = make_float4(o.x, o.y, o.z, __uint_as_float(job));
         nd[pos] = make_float4(d.x, d.y, d.z, __uint_as_float(depth));
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob*
                                                      const DevUnit* __restrict__ units, uint32_t mask,
                                                      float4* __restrict__ s_hot, uint4* __restrict__ s_cold,
                                                      uint32_t* __restrict__ q_slot, float4* __restrict__ q_o,
-                                                     float4* __restrict__ q_d) {
+                                                     float4* __restrict__ q_d, uint32_t cap) {
     const uint32_t n = c->fill_n, qbase = c->fill_qbase;
     const unsigned long long base = c->fill_base;
     const uint32_t ulo = c->fill_ulo, uhi = c->fill_uhi + 1;
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob*
         s_hot[2 * static_cast<size_t>(slot) + 1] = make_float4(
             0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(key)), __uint_as_float(static_cast<uint32_t>(key >> 32)));
         s_cold[slot] = make_uint4(u, 0, __float_as_uint(s), __float_as_uint(t));
+        if (!GR_IN_RANGE(qbase + i, cap)) continue;
         q_slot[qbase + i] = slot;
         q_o[qbase + i] = make_float4(o.x, o.y, o.z, __uint_as_float(U.job));
         q_d[qbase + i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
@@ -240,7 +242,7 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
                 const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
                 const float4* __restrict__ q_d, const float4* __restrict__ q_hit, float4* __restrict__ s_hot,
                 const uint4* __restrict__ s_cold, uint32_t* __restrict__ nslot, float4* __restrict__ no,
-                float4* __restrict__ nd) {
+                float4* __restrict__ nd, uint32_t cap) {
     extern __shared__ unsigned char dsmem[];
     const SortView sm = sort_view<EBLOCK, ESHADE_PER_THREAD>(dsmem);
     const int nxt = cur ^ 1;
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
                 if (finished && lane == static_cast<unsigned>(__ffs(same) - 1))
                     atomicAdd(unit_done + unit, static_cast<uint32_t>(__popc(same)));
             }
-            push_ray(alive, &c->q[nxt], slot, new_o, new_d, job, depth + 1, nslot, no, nd);
+            push_ray(alive, &c->q[nxt], slot, new_o, new_d, job, depth + 1, nslot, no, nd, cap);
         }
         __syncthreads();  // sm is reused by the next chunk
     }
@@ -440,7 +442,7 @@ gr_status Engine::enqueue_iteration(int cur) {
     int fgrid = grid_for(reinterpret_cast<const void*>(k_eng_fill), EBLOCK, 0, C);
     k_eng_fill<<<fgrid, EBLOCK, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), ring_ - 1,
                                           s_hot_.as<float4>(), s_cold_.as<uint4>(), q_slot_[cur].as<uint32_t>(),
-                                          q_o_[cur].as<float4>(), q_d_[cur].as<float4>());
+                                          q_o_[cur].as<float4>(), q_d_[cur].as<float4>(), C);
     GR_CUDA_TRY(cudaGetLastError());
     switch (cfg_.width) {
         case 2:
@@ -462,7 +464,7 @@ gr_status Engine::enqueue_iteration(int cur) {
                                            q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>(),
                                            q_hit_.as<float4>(), s_hot_.as<float4>(), s_cold_.as<uint4>(),
                                            q_slot_[nxt].as<uint32_t>(), q_o_[nxt].as<float4>(),
-                                           q_d_[nxt].as<float4>());
+                                           q_d_[nxt].as<float4>(), C);
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }
@@ -618,6 +620,14 @@ gr_status Engine::run(uint32_t max_pairs, bool& done) {
         set_error("engine: traversal stack bound exceeded");
         return GR_ERR_STACK_OVERFLOW;
     }
+#if GR_CHECKED
+    bool bad = false;
+    GR_CUDA_TRY(take_bad_index(bad));
+    if (bad) {
+        set_error("engine: a queue index was out of range (checked build)");
+        return GR_ERR_INTERNAL;
+    }
+#endif
     return GR_OK;
 }
 

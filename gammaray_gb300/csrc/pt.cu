@@ -40,6 +40,7 @@ struct PTParams {
     uint32_t first_pass;
     uint64_t seed;
     uint32_t max_depth, rr_depth, rr_aggr;
+    uint32_t qcap;  // queue capacity (paths of the group)
 };
 
 __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4* __restrict__ tp,
@@ -131,7 +132,7 @@ __global__ void GR_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t dept
                 }
                 L_buf[slot] = make_float4(L.x, L.y, L.z, 0.0f);
             }
-            push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd);
+            push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd, p.qcap);
         }
         __syncthreads();  // sm is reused by the next chunk
     }
@@ -250,6 +251,7 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     p.width = job.width;
     p.height = job.height;
     p.npix = npix;
+    p.qcap = static_cast<uint32_t>(static_cast<size_t>(group) * npix);
     p.seed = rp.seed;
     p.max_depth = display ? 1 : rp.max_depth;
     p.rr_depth = rp.rr_depth;
@@ -413,6 +415,18 @@ gr_status static_scratch(void** out) {
 
 }  // namespace
 
+gr_status pt_index_check() {
+#if GR_CHECKED
+    bool bad = false;
+    GR_CUDA_TRY(take_bad_index(bad));
+    if (bad) {
+        set_error("path tracer: a queue or entry index was out of range (checked build)");
+        return GR_ERR_INTERNAL;
+    }
+#endif
+    return GR_OK;
+}
+
 }  // namespace gr
 
 using namespace gr;
@@ -473,6 +487,7 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
     p.width = width;
     p.height = height;
     p.npix = npix;
+    p.qcap = npix;
     p.seed = rp->seed;
     p.max_depth = display ? 1 : rp->max_depth;
     p.rr_depth = rp->rr_depth;

@@ -146,6 +146,10 @@ struct RenderJob {
 
 gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st);
 gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st);
+// Checked builds (GR_CHECKED): whether a render's kernels wrote out of range (read after
+// the render's work has finished); GR_OK otherwise.
+gr_status pt_index_check();
+gr_status bdpt_index_check();
 gr_status film_gather(const float2* st_buf, const float4* color, uint32_t width, uint32_t height, uint32_t passes,
                       float4* film, cudaStream_t s);
 // Resolve and EXR packing add splat * splat_scale when splat is not null.

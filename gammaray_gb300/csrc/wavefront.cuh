@@ -99,7 +99,7 @@ __global__ void GR_EXTEND_BOUNDS k_extend(DeviceScene s, const uint32_t* __restr
 // Appends this lane's ray to the next queue with one atomic per warp (ballot + popc).
 // Every lane of the warp must call it (warp-uniform trip counts).
 GR_D void push_warp(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t* __restrict__ nslot,
-                    float4* __restrict__ no, float4* __restrict__ nd) {
+                    float4* __restrict__ no, float4* __restrict__ nd, uint32_t cap) {
     const unsigned lane = threadIdx.x & 31;
     unsigned m = __ballot_sync(0xffffffffu, alive);
     if (!m) return;
@@ -109,6 +109,7 @@ GR_D void push_warp(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, 
     base = __shfl_sync(0xffffffffu, base, leader);
     if (alive) {
         uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
+        if (!GR_IN_RANGE(pos, cap)) return;
         nslot[pos] = slot;
         no[pos] = make_float4(o.x, o.y, o.z, 0.0f);
         nd[pos] = make_float4(d.x, d.y, d.z, 0.0f);
