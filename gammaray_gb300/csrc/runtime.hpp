@@ -2,6 +2,9 @@
 // between the C ABI (api.cu) and the kernel files.
 #pragma once
 
+#include <atomic>
+#include <cstdlib>
+
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -26,6 +29,18 @@ void set_error(const std::string& msg);
     } while (0)
 
 // A device allocation that frees itself.
+// Host-side fault injection for tests (no GPU fault): GR_FAIL_ALLOC_AT=k makes the k-th
+// device allocation of the process report cudaErrorMemoryAllocation, once.
+inline bool alloc_should_fail() {
+    static const long at = [] {
+        const char* e = std::getenv("GR_FAIL_ALLOC_AT");
+        return e ? std::atol(e) : 0L;
+    }();
+    if (at <= 0) return false;
+    static std::atomic<long> count{0};
+    return count.fetch_add(1) + 1 == at;
+}
+
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -41,6 +56,7 @@ struct DevBuf {
     cudaError_t ensure(size_t n) {
         if (n <= bytes) return cudaSuccess;
         release();
+        if (alloc_should_fail()) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMalloc(&ptr, n);
         if (e == cudaSuccess) bytes = n;
         else ptr = nullptr;

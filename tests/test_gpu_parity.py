@@ -356,6 +356,42 @@ print("OK", torch.ones(1024, device="cuda").sum().item())
     assert "OK 1024.0" in r.stdout, r.stdout
 
 
+@pytest.mark.parametrize("at", [1, 3, 6, 9, 12, 15])
+def test_allocation_refusal_is_reported_and_recovered(gpu, at):
+    # Host-side fault injection (GR_FAIL_ALLOC_AT=k: the k-th device allocation reports
+    # out of memory, once).  Wherever it lands (scene creation, film, the render's path
+    # state), the call fails with an error, nothing crashes, and the same work then
+    # succeeds in the same process.  (A subprocess: the setting is read once.)
+    import os
+    import subprocess
+    import sys
+
+    code = """
+import numpy as np
+import gammaray_gb300 as g
+from gammaray_gb300 import _abi, scenes
+w = scenes.cornell_spheres(32, 32, 2)
+def attempt():
+    st = g.Stage(w.prims, environment=w.environment, seed=3)
+    f = g.Film(32, 32)
+    st.render(w.camera, w.integrator, f, 2)
+    return f.resolve()
+try:
+    attempt()
+    print("FIRST_OK")
+except _abi.GrError as e:
+    print("FIRST_ERROR", e)
+img = attempt()
+print("RECOVERED", bool(np.isfinite(img).all()), float(img.mean()) > 0.0)
+"""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GR_FAIL_ALLOC_AT=str(at), PYTHONPATH=root)
+    r = subprocess.run([sys.executable, "-c", code], env=env, cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "FIRST_ERROR" in r.stdout and "memory" in r.stdout.lower(), r.stdout
+    assert "RECOVERED True True" in r.stdout, r.stdout
+
+
 def test_bdpt_counts_shadow_rays(gpu):
     w = scenes.cornell_spheres(32, 32, 2)
     st = g.Stage(w.prims, lib=gpu, seed=1)
