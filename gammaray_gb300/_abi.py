@@ -327,6 +327,7 @@ SIGNATURES = {
     "gr_server_poll": (C.c_int, [_VP, C.c_uint64, C.POINTER(RequestStatus)]),
     "gr_server_cancel": (C.c_int, [_VP, C.c_uint64]),
     "gr_server_take": (C.c_int, [_VP, C.c_uint64, _PF, _PF]),
+    "gr_server_snapshot": (C.c_int, [_VP, C.c_uint64, _PF, _PF, C.POINTER(C.c_uint32)]),
 }
 
 

@@ -606,6 +606,48 @@ gr_status gr_server_cancel(gr_server* s, uint64_t id) {
     return GR_OK;
 }
 
+// Copies a request's film to host arrays (accum: 3 floats per pixel, weight: 1; either
+// may be null), a progressive request's two half-films summed; zeros before admission.
+static gr_status copy_film(gr_server* s, const ServerRequest& r, float* accum, float* weight) {
+    if (!accum && !weight) return GR_OK;
+    const size_t n = static_cast<size_t>(r.req.width) * r.req.height;
+    std::vector<float4> px(n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    if (r.film.ptr) {
+        GR_CUDA_TRY(cudaStreamSynchronize(s->engine.stream()));
+        GR_CUDA_TRY(cudaMemcpy(px.data(), r.film.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
+        if (r.progressive && r.film2.ptr) {  // even + odd passes
+            std::vector<float4> p2(n);
+            GR_CUDA_TRY(cudaMemcpy(p2.data(), r.film2.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < n; ++i)
+                px[i] = make_float4(px[i].x + p2[i].x, px[i].y + p2[i].y, px[i].z + p2[i].z, px[i].w + p2[i].w);
+        }
+    }
+    for (size_t i = 0; i < n; ++i) {
+        if (accum) {
+            accum[3 * i] = px[i].x;
+            accum[3 * i + 1] = px[i].y;
+            accum[3 * i + 2] = px[i].z;
+        }
+        if (weight) weight[i] = px[i].w;
+    }
+    return GR_OK;
+}
+
+gr_status gr_server_snapshot(gr_server* s, uint64_t id, float* accum, float* weight, uint32_t* passes) {
+    if (!s) {
+        set_error("null server");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    ServerRequest* r = s->find(id);
+    if (!r) {
+        set_error("no such request");
+        return GR_ERR_NOT_FOUND;
+    }
+    if (passes) *passes = r->passes_done;
+    return copy_film(s, *r, accum, weight);
+}
+
 gr_status gr_server_take(gr_server* s, uint64_t id, float* accum, float* weight) {
     if (!s) {
         set_error("null server");
@@ -619,25 +661,8 @@ gr_status gr_server_take(gr_server* s, uint64_t id, float* accum, float* weight)
             set_error("request not finished");
             return GR_ERR_BUSY;
         }
-        size_t n = static_cast<size_t>(r->req.width) * r->req.height;
-        if (r->film.ptr && (accum || weight)) {
-            std::vector<float4> px(n);
-            GR_CUDA_TRY(cudaMemcpy(px.data(), r->film.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
-            if (r->progressive && r->film2.ptr) {  // even + odd passes
-                std::vector<float4> p2(n);
-                GR_CUDA_TRY(cudaMemcpy(p2.data(), r->film2.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
-                for (size_t i = 0; i < n; ++i)
-                    px[i] = make_float4(px[i].x + p2[i].x, px[i].y + p2[i].y, px[i].z + p2[i].z, px[i].w + p2[i].w);
-            }
-            for (size_t i = 0; i < n; ++i) {
-                if (accum) {
-                    accum[3 * i] = px[i].x;
-                    accum[3 * i + 1] = px[i].y;
-                    accum[3 * i + 2] = px[i].z;
-                }
-                if (weight) weight[i] = px[i].w;
-            }
-        }
+        gr_status cst = copy_film(s, *r, accum, weight);
+        if (cst != GR_OK) return cst;
         if (r->film.ptr) s->used -= r->bytes;
         s->reqs.erase(s->reqs.begin() + static_cast<long>(k));
         return GR_OK;

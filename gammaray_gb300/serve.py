@@ -66,6 +66,15 @@ class Server:
         self.lib.call("gr_server_take", self.handle, rid, _abi.fptr(acc), _abi.fptr(wt))
         return acc, wt
 
+    def snapshot(self, rid: int):
+        """gr_server_snapshot: the request's film so far, (accum, weight, passes)."""
+        w, h = self.sizes[rid]
+        acc = np.empty((h, w, 3), np.float32)
+        wt = np.empty((h, w), np.float32)
+        passes = C.c_uint32()
+        self.lib.call("gr_server_snapshot", self.handle, rid, _abi.fptr(acc), _abi.fptr(wt), C.byref(passes))
+        return acc, wt, passes.value
+
     def run_until_done(self, ids, budget_ms: float = 20.0, max_steps: int = 3000):
         pending = set(ids)
         for _ in range(max_steps):

@@ -463,6 +463,11 @@ gr_status gr_server_cancel(gr_server* server, uint64_t id);
 /* Copies the finished film (accum, weight) of a request and releases it (a progressive
  * request's two half-films are summed). */
 gr_status gr_server_take(gr_server* server, uint64_t id, float* accum, float* weight);
+/* Copies a request's film as rendered so far, without finishing it: `passes` (may be
+ * null) receives the passes it holds (the same film gr_server_take would return, were
+ * the request to stop there); zeros before admission.  No counterpart in the
+ * reference. */
+gr_status gr_server_snapshot(gr_server* server, uint64_t id, float* accum, float* weight, uint32_t* passes);
 
 #ifdef __cplusplus
 }

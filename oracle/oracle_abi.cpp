@@ -603,6 +603,9 @@ gr_status gr_server_poll(gr_server*, uint64_t, gr_request_status*) {
     return fail(GR_ERR_UNSUPPORTED, "serving is a device feature");
 }
 gr_status gr_server_cancel(gr_server*, uint64_t) { return fail(GR_ERR_UNSUPPORTED, "serving is a device feature"); }
+gr_status gr_server_snapshot(gr_server*, uint64_t, float*, float*, uint32_t*) {
+    return fail(GR_ERR_UNSUPPORTED, "serving is a device feature");
+}
 gr_status gr_server_take(gr_server*, uint64_t, float*, float*) {
     return fail(GR_ERR_UNSUPPORTED, "serving is a device feature");
 }

@@ -94,6 +94,37 @@ def test_server_alone_equals_mixed(gpu):
     np.testing.assert_allclose(ref.read()[0], a_acc, rtol=1e-6, atol=1e-7)
 
 
+def test_server_snapshot_shows_the_film_so_far(gpu):
+    w = small_workloads(1, seed=14)[0]
+    st = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=5)
+    s = serve.Server(gpu, path_capacity=1 << 16)
+    rid = s.submit(st, w.camera, w.integrator, w.width, w.height, 64)
+    acc0, wt0, n0 = s.snapshot(rid)  # not admitted yet: zeros
+    assert n0 == 0 and not wt0.any()
+    seen, part = [], {}
+    for _ in range(400):
+        s.step(0.5)
+        acc, wt, n = s.snapshot(rid)
+        seen.append(n)
+        if 0 < n < 64:
+            part[n] = (acc, wt)
+        if s.poll(rid).state == 2:
+            break
+    assert seen == sorted(seen) and seen[-1] == 64
+    assert part  # a film part-way through
+    acc, wt, n = s.snapshot(rid)
+    a2, w2 = s.take(rid)
+    np.testing.assert_array_equal(acc, a2)
+    np.testing.assert_array_equal(wt, w2)
+    # a part-way film is the film of the first k passes
+    k = min(part)
+    ref = g.Film(w.width, w.height, lib=gpu)
+    st.render(w.camera, w.integrator, ref, k)
+    racc, rwt = ref.read()
+    np.testing.assert_array_equal(part[k][1], rwt)
+    np.testing.assert_allclose(part[k][0], racc, rtol=1e-6, atol=1e-7)
+
+
 def test_server_rejects_an_image_too_large_for_its_ring(gpu):
     # The check is at submission: an oversized request must not fail the steps that
     # serve the others.  A 64 k-path server keeps an 8 M-slot ring (images up to 4 M px).
