@@ -78,6 +78,8 @@ struct BinNode {
     int32_t child[2];  // -1 for leaves
     uint32_t first, count;  // component range of the whole subtree
 };
+// Arrays written in full after they are sized: no zero fill.
+using BinNodes = std::vector<BinNode, NoInitAlloc<BinNode>>;
 
 // One component during the binary build: its box, centroid and item index.  The build
 // permutes these records in place (not an index array into the items), so each pass
@@ -238,7 +240,7 @@ class RefBuilder {
 
     Rec* base;
     std::unique_ptr<Rec[]> tmp;  // scratch for the parallel partition (same indexing as base)
-    std::vector<BinNode> nodes;
+    BinNodes nodes;
     std::atomic<uint32_t> next{0};
     std::atomic<uint64_t> used{0};
     unsigned threads = 1;
@@ -527,12 +529,12 @@ struct Cand {
 
 class Collapser {
   public:
-    const std::vector<BinNode>& bin;
-    const std::vector<Box>& comp_box;  // per ordered component
+    const BinNodes& bin;
+    const std::vector<Box, NoInitAlloc<Box>>& comp_box;  // per ordered component
     uint32_t W, L;
     std::vector<float>& out;  // node floats
 
-    Collapser(const std::vector<BinNode>& b, const std::vector<Box>& cb, uint32_t w, uint32_t l,
+    Collapser(const BinNodes& b, const std::vector<Box, NoInitAlloc<Box>>& cb, uint32_t w, uint32_t l,
               std::vector<float>& o)
         : bin(b), comp_box(cb), W(w), L(l), out(o) {}
 
@@ -808,7 +810,7 @@ static void put_bits(float* dst, uint32_t v) { std::memcpy(dst, &v, 4); }
 
 // FNV-1a over the binary tree in depth-first order, left child first: each node's box,
 // then a leaf's component count and (prim, component) ids, or an inner node's tag.
-static uint64_t tree_hash(const std::vector<BinNode>& nodes, int32_t root, const std::vector<Rec>& recs,
+static uint64_t tree_hash(const BinNodes& nodes, int32_t root, const std::vector<Rec, NoInitAlloc<Rec>>& recs,
                           const std::vector<Item>& items) {
     uint64_t h = 1469598103934665603ull;
     auto add = [&](const void* p, size_t n) {
@@ -1025,7 +1027,7 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
             }
         }
     } else {
-        std::vector<Rec> recs(items.size());
+        std::vector<Rec, NoInitAlloc<Rec>> recs(items.size());  // every element written below
         auto fill = [&](unsigned, size_t b, size_t e) {
             for (size_t k = b; k < e; ++k) {
                 recs[k].box = items[k].box;
@@ -1041,7 +1043,7 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
         int32_t root = rb.build(recs.data(), recs.size());
         out.num_binary_nodes = rb.node_count();
         if (want_tree_hash) out.tree_hash = tree_hash(rb.nodes, root, recs, items);
-        std::vector<Box> comp_box(items.size());
+        std::vector<Box, NoInitAlloc<Box>> comp_box(items.size());  // written by the records pass
         auto records = [&](unsigned, size_t b, size_t e) {
             for (size_t k = b; k < e; ++k) {
                 const Item& it = items[recs[k].id & ID_MASK];
