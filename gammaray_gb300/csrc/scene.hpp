@@ -100,7 +100,7 @@ struct HostBuild {
     // tree is made on the GPU from these boxes (lo.xyz, hi.xyz per component).
     bool device_build = false;
     uint32_t leaf_size = 0;
-    std::vector<float> item_boxes;
+    std::vector<float, NoInitAlloc<float>> item_boxes;  // every element written
 };
 
 // Evaluates DisneyMaterialBuilder::build and the lobe constructors

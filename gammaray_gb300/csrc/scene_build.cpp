@@ -1019,13 +1019,20 @@ bool build_scene(const gr_scene_desc& desc, HostBuild& out, std::string& err, bo
     if (out.device_build) {
         out.leaf_size = L;
         out.item_boxes.resize(items.size() * 6);
-        for (size_t k = 0; k < items.size(); ++k) {
-            put_record(k, items[k]);
-            for (int a = 0; a < 3; ++a) {
-                out.item_boxes[6 * k + a] = items[k].box.lo[a];
-                out.item_boxes[6 * k + 3 + a] = items[k].box.hi[a];
+        auto records = [&](unsigned, size_t b, size_t e) {
+            for (size_t k = b; k < e; ++k) {
+                put_record(k, items[k]);
+                for (int a = 0; a < 3; ++a) {
+                    out.item_boxes[6 * k + a] = items[k].box.lo[a];
+                    out.item_boxes[6 * k + 3 + a] = items[k].box.hi[a];
+                }
             }
-        }
+        };
+        const unsigned hw = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+        if (items.size() >= RefBuilder::SPLIT_PASS && hw > 1)
+            RefBuilder::in_parts(items.size(), hw, records);
+        else
+            records(0, 0, items.size());
     } else {
         std::vector<Rec, NoInitAlloc<Rec>> recs(items.size());  // every element written below
         auto fill = [&](unsigned, size_t b, size_t e) {
