@@ -8,6 +8,8 @@ restatement against analytic answers and physical invariants instead:
   - a diffuse plane under a white sky returns exactly its albedo (0.5) per path;
   - reflection-only BSDFs are reciprocal, sampling is consistent with pdf_world
     (E[cos/pdf] = pi) and the GGX / PerfectDiffuse albedo is at most 1;
+  - the transmission pdf equals a float64 restatement of lobes.rs:321-349 (quirks kept),
+    and glass samples follow the density the sampler really draws from (chi-square);
   - the film resolves a constant colour exactly, and the EXR layout of exr.rs.
 """
 from __future__ import annotations
@@ -156,12 +158,13 @@ def test_sampling_matches_pdf(oracle, name):
     assert abs(est.mean() - math.pi) < 5 * se + 2e-3, (est.mean(), se)
 
 
-def sampling_chi2(oracle, m, n=200_000, nt=16, nph=32, sub=6):
+def sampling_chi2(oracle, m, n=200_000, nt=16, nph=32, sub=6, density=None):
     """The directions sample_world draws, binned over the sphere (16 in cos(theta) x 32
     in phi, equal solid angle), against pdf_world integrated over each bin on a 6 x 6
     grid.  Draws that leave the hemisphere are rejected (pdf 0) and pdf_world is the
     density of the rest, so the bins follow n * mass.  Returns (total pdf mass, accepted
-    fraction, Pearson chi-square p-value)."""
+    fraction, Pearson chi-square p-value).  `density(wi, wo)` (float64, the local frame
+    is the identity) replaces pdf_world as the expected density when given."""
     from scipy import stats
 
     fr = np.zeros(1, _abi.FRAME_DTYPE)
@@ -181,7 +184,11 @@ def sampling_chi2(oracle, m, n=200_000, nt=16, nph=32, sub=6):
     rr = np.sqrt(np.maximum(0.0, 1.0 - zz * zz))
     wo = np.stack([rr * np.cos(pp), rr * np.sin(pp), zz], axis=-1).reshape(-1, 3).astype(np.float32)
     k = len(wo)
-    pdf = g.bsdf_pdf(m, np.repeat(fr, k), np.repeat(wi, k, axis=0), wo, lib=oracle).reshape(nt, sub, nph, sub)
+    if density is None:
+        pdf = g.bsdf_pdf(m, np.repeat(fr, k), np.repeat(wi, k, axis=0), wo, lib=oracle)
+    else:
+        pdf = density(np.repeat(wi, k, axis=0).astype(np.float64), wo.astype(np.float64))
+    pdf = pdf.reshape(nt, sub, nph, sub)
     mass = pdf.mean(axis=(1, 3)).reshape(-1) * (4 * math.pi / (nt * nph))
     expected = mass * n
     big = expected >= 20.0
@@ -221,6 +228,119 @@ def test_clearcoat_pdf_quirk(oracle):
     valid = (s["kind"] != 0) & (cos > 0)
     est = np.where(valid, cos / np.where(valid, s["pdf"], 1.0), 0.0)
     assert est.mean() < math.pi - 10 * est.std() / math.sqrt(n)
+
+
+def _trig(v):
+    """cos2/sin2(theta) and the clamped cos/sin(phi) of core/vector.rs:137-205; they take
+    z as cos(theta) even for a vector that is not of unit length."""
+    cos2 = v[:, 2] * v[:, 2]
+    sin2 = np.maximum(0.0, 1.0 - cos2)
+    sin = np.sqrt(sin2)
+    safe = np.where(sin == 0, 1.0, sin)
+    cphi = np.where(sin == 0, 1.0, np.clip(v[:, 0] / safe, -1, 1))
+    sphi = np.where(sin == 0, 0.0, np.clip(v[:, 1] / safe, -1, 1))
+    return cos2, sin2, cphi, sphi
+
+
+def _ggx_alpha(roughness, anisotropic):  # material/util.rs:128-133
+    aspect = math.sqrt(1.0 - anisotropic * 0.9)
+    return max(0.001, roughness * roughness / aspect), max(0.001, roughness * roughness * aspect)
+
+
+def _ggx_d(h, ax, ay):  # material/util.rs:198-208
+    cos2, sin2, cphi, sphi = _trig(h)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        tan2 = sin2 / cos2
+        e = (cphi ** 2 / ax ** 2 + sphi ** 2 / ay ** 2) * tan2
+        d = 1.0 / (math.pi * ax * ay * cos2 * cos2 * (1 + e) ** 2)
+    return np.where(np.isfinite(tan2), d, 0.0)
+
+
+def _ggx_g1(v, ax, ay):  # material/util.rs:135-150
+    _, sin2, cphi, sphi = _trig(v)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        tan = np.abs(np.sqrt(sin2) / v[:, 2])
+    alpha = np.sqrt(cphi ** 2 * ax * ax + sphi ** 2 * ay * ay)
+    lam = np.where(np.isfinite(tan), (-1 + np.sqrt(1 + (alpha * np.where(np.isfinite(tan), tan, 0)) ** 2)) * 0.5, 0.0)
+    return 1.0 / (1.0 + lam)
+
+
+def transmission_pdf(i, o, roughness, ior, anisotropic=0.0, as_reference=True):
+    """pdf of DisneySpecularTrans in float64 (local frame).  `as_reference` follows
+    material/lobes.rs:321-349 as written: the half vector i + eta*o is used unnormalised
+    when its z > 0, and backfacing microfacets are not excluded.  Otherwise it is the
+    density that sample_f (lobes.rs:351-388: visible-normal half vector, then refraction)
+    actually draws from: the half vector normalised, and zero where the microfacet faces
+    away from i or o."""
+    ior = max(ior, 1.01)  # lobes.rs:261
+    ax, ay = _ggx_alpha(roughness, anisotropic)
+    eta = np.where(i[:, 2] > 0, ior, 1.0 / ior)
+    hu = i + o * eta[:, None]
+    hn = hu / np.linalg.norm(hu, axis=1, keepdims=True)
+    if as_reference:
+        h = np.where(hu[:, 2:3] > 0, hu, -hn)
+    else:
+        h = np.where(hn[:, 2:3] > 0, hn, -hn)
+    ih, oh = (i * h).sum(1), (o * h).sum(1)
+    den = ih + eta * oh
+    with np.errstate(divide="ignore", invalid="ignore"):
+        p = _ggx_d(h, ax, ay) * _ggx_g1(i, ax, ay) * np.abs(ih) / np.abs(i[:, 2]) * np.abs(eta * eta * oh / den ** 2)
+    zero = i[:, 2] * o[:, 2] > 0
+    if not as_reference:
+        zero |= (ih * i[:, 2] < 0) | (oh * o[:, 2] < 0)
+    return np.where(zero, 0.0, p)
+
+
+@pytest.mark.parametrize("rough,ior,aniso", [(0.3, 1.5, 0.0), (0.7, 1.33, 0.0), (0.5, 1.5, 0.8), (0.05, 2.0, 0.0)])
+def test_transmission_pdf_is_the_reference_formula(oracle, rough, ior, aniso):
+    # With i and o in opposite hemispheres the reflection lobe's pdf is 0 and
+    # pdf_world = transmission pdf / 2 (material.rs:113-118): compare it with the
+    # float64 restatement of lobes.rs:321-349, quirks included, entering and exiting.
+    rng = np.random.default_rng(5)
+    n = 4096
+    i = rng.normal(size=(n, 3))
+    o = rng.normal(size=(n, 3))
+    i /= np.linalg.norm(i, axis=1, keepdims=True)
+    o /= np.linalg.norm(o, axis=1, keepdims=True)
+    o[:, 2] = -np.sign(i[:, 2]) * np.abs(o[:, 2])
+    i32, o32 = i.astype(np.float32), o.astype(np.float32)
+    fr = np.zeros(n, _abi.FRAME_DTYPE)
+    fr["normal"], fr["tangent"], fr["binormal"], fr["geom_normal"] = (0, 0, 1), (1, 0, 0), (0, 1, 0), (0, 0, 1)
+    m = g.Material.disney().specular_trans(1.0).roughness(rough).ior(ior).anisotropic(aniso).build()
+    got = 2.0 * g.bsdf_pdf(m, fr, i32, o32, lib=oracle).astype(np.float64)
+    ref = transmission_pdf(i32.astype(np.float64), o32.astype(np.float64), rough, ior, aniso)
+    np.testing.assert_allclose(got, ref, rtol=2e-3)  # float32 against float64
+    eta = np.where(i32[:, 2] > 0, ior, 1.0 / ior)[:, None]
+    unnormalised = (i32 + o32 * eta)[:, 2] > 0
+    assert unnormalised.mean() > 0.2  # the quirk's branch is exercised
+    fixed = transmission_pdf(i32.astype(np.float64), o32.astype(np.float64), rough, ior, aniso, as_reference=False)
+    assert (np.abs(fixed - ref) > 0.01 * np.abs(ref))[unnormalised].mean() > 0.5
+
+
+def test_transmission_sampling_follows_the_microfacet_density(oracle):
+    # Glass = specular reflection + transmission, each picked with probability 1/2
+    # (material.rs:176-195).  The drawn directions follow 1/2 (reflection pdf + the
+    # transmission density sample_f really draws from); the reflection pdf is that of a
+    # metal of the same roughness, whose only lobe is the same reflection.  Against the
+    # reference's own pdf_world the histogram fails: lobes.rs:321-349's pdf is not the
+    # sampling density (unnormalised half vector, backfacing microfacets kept).
+    rough, ior = 0.5, 1.5
+    glass = g.Material.disney().specular_trans(1.0).roughness(rough).ior(ior).build()
+    metal = g.Material.disney().metallic(1.0).roughness(rough).ior(ior).build()
+    fr1 = np.zeros(1, _abi.FRAME_DTYPE)
+    fr1["normal"], fr1["tangent"], fr1["binormal"], fr1["geom_normal"] = (0, 0, 1), (1, 0, 0), (0, 1, 0), (0, 0, 1)
+
+    def true_density(wi, wo):
+        k = len(wo)
+        refl = g.bsdf_pdf(metal, np.repeat(fr1, k), wi.astype(np.float32), wo.astype(np.float32),
+                          lib=oracle).astype(np.float64)
+        return 0.5 * (refl + transmission_pdf(wi, wo, rough, ior, as_reference=False))
+
+    mass, accepted, p = sampling_chi2(oracle, glass, density=true_density)
+    assert abs(mass - accepted) < 0.01, (mass, accepted)
+    assert p > 1e-4, p
+    mass, accepted, p = sampling_chi2(oracle, glass)
+    assert abs(mass - accepted) > 0.01 or p < 1e-6, (mass, accepted, p)
 
 
 @pytest.mark.parametrize("name", ["metal_aniso", "perfect_diffuse"])
