@@ -20,6 +20,7 @@ import struct
 import numpy as np
 import pytest
 
+import bsdf_f64
 import gammaray_gb300 as g
 from gammaray_gb300 import _abi, scenes
 
@@ -230,65 +231,11 @@ def test_clearcoat_pdf_quirk(oracle):
     assert est.mean() < math.pi - 10 * est.std() / math.sqrt(n)
 
 
-def _trig(v):
-    """cos2/sin2(theta) and the clamped cos/sin(phi) of core/vector.rs:137-205; they take
-    z as cos(theta) even for a vector that is not of unit length."""
-    cos2 = v[:, 2] * v[:, 2]
-    sin2 = np.maximum(0.0, 1.0 - cos2)
-    sin = np.sqrt(sin2)
-    safe = np.where(sin == 0, 1.0, sin)
-    cphi = np.where(sin == 0, 1.0, np.clip(v[:, 0] / safe, -1, 1))
-    sphi = np.where(sin == 0, 0.0, np.clip(v[:, 1] / safe, -1, 1))
-    return cos2, sin2, cphi, sphi
-
-
-def _ggx_alpha(roughness, anisotropic):  # material/util.rs:128-133
-    aspect = math.sqrt(1.0 - anisotropic * 0.9)
-    return max(0.001, roughness * roughness / aspect), max(0.001, roughness * roughness * aspect)
-
-
-def _ggx_d(h, ax, ay):  # material/util.rs:198-208
-    cos2, sin2, cphi, sphi = _trig(h)
-    with np.errstate(divide="ignore", invalid="ignore"):
-        tan2 = sin2 / cos2
-        e = (cphi ** 2 / ax ** 2 + sphi ** 2 / ay ** 2) * tan2
-        d = 1.0 / (math.pi * ax * ay * cos2 * cos2 * (1 + e) ** 2)
-    return np.where(np.isfinite(tan2), d, 0.0)
-
-
-def _ggx_g1(v, ax, ay):  # material/util.rs:135-150
-    _, sin2, cphi, sphi = _trig(v)
-    with np.errstate(divide="ignore", invalid="ignore"):
-        tan = np.abs(np.sqrt(sin2) / v[:, 2])
-    alpha = np.sqrt(cphi ** 2 * ax * ax + sphi ** 2 * ay * ay)
-    lam = np.where(np.isfinite(tan), (-1 + np.sqrt(1 + (alpha * np.where(np.isfinite(tan), tan, 0)) ** 2)) * 0.5, 0.0)
-    return 1.0 / (1.0 + lam)
-
-
 def transmission_pdf(i, o, roughness, ior, anisotropic=0.0, as_reference=True):
-    """pdf of DisneySpecularTrans in float64 (local frame).  `as_reference` follows
-    material/lobes.rs:321-349 as written: the half vector i + eta*o is used unnormalised
-    when its z > 0, and backfacing microfacets are not excluded.  Otherwise it is the
-    density that sample_f (lobes.rs:351-388: visible-normal half vector, then refraction)
-    actually draws from: the half vector normalised, and zero where the microfacet faces
-    away from i or o."""
-    ior = max(ior, 1.01)  # lobes.rs:261
-    ax, ay = _ggx_alpha(roughness, anisotropic)
-    eta = np.where(i[:, 2] > 0, ior, 1.0 / ior)
-    hu = i + o * eta[:, None]
-    hn = hu / np.linalg.norm(hu, axis=1, keepdims=True)
-    if as_reference:
-        h = np.where(hu[:, 2:3] > 0, hu, -hn)
-    else:
-        h = np.where(hn[:, 2:3] > 0, hn, -hn)
-    ih, oh = (i * h).sum(1), (o * h).sum(1)
-    den = ih + eta * oh
-    with np.errstate(divide="ignore", invalid="ignore"):
-        p = _ggx_d(h, ax, ay) * _ggx_g1(i, ax, ay) * np.abs(ih) / np.abs(i[:, 2]) * np.abs(eta * eta * oh / den ** 2)
-    zero = i[:, 2] * o[:, 2] > 0
-    if not as_reference:
-        zero |= (ih * i[:, 2] < 0) | (oh * o[:, 2] < 0)
-    return np.where(zero, 0.0, p)
+    """DisneySpecularTrans's pdf in float64 from the independent restatement in
+    tests/bsdf_f64.py: as lobes.rs:321-349 is written (`as_reference`), or the density
+    sample_f actually draws from."""
+    return bsdf_f64.SpecularTrans(np.ones(3), roughness, anisotropic, ior).pdf(i, o, as_reference)
 
 
 @pytest.mark.parametrize("rough,ior,aniso", [(0.3, 1.5, 0.0), (0.7, 1.33, 0.0), (0.5, 1.5, 0.8), (0.05, 2.0, 0.0)])
