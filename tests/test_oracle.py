@@ -10,7 +10,8 @@ restatement against analytic answers and physical invariants instead:
     (E[cos/pdf] = pi) and the GGX / PerfectDiffuse albedo is at most 1;
   - the transmission pdf equals a float64 restatement of lobes.rs:321-349 (quirks kept),
     and glass samples follow the density the sampler really draws from (chi-square);
-  - the film resolves a constant colour exactly, and the EXR layout of exr.rs.
+  - the film resolves a constant colour exactly, equals a float32 restatement of the
+    serial Mitchell splat bit for bit, and the EXR layout of exr.rs.
 """
 from __future__ import annotations
 
@@ -320,6 +321,65 @@ def test_film_constant_colour(oracle):
     st.render(g.Camera.with_fov(60.0, 1.5), g.DisplayColorIntegrator(), f, 3)
     np.testing.assert_allclose(f.resolve(), np.broadcast_to([0.3, 0.5, 0.7], (16, 24, 3)), rtol=1e-5)
     assert f.passes() == 3
+
+
+def _mitchell1(x):
+    """core/math.rs:92-108 in float32 (B = C = 1/3), constants folded in float32 as Rust
+    folds them."""
+    f = np.float32
+    B = C = f(1.0) / f(3.0)
+    tx = np.abs(f(2.0) * x)
+    outer = ((-B - f(6.0) * C) * (tx * tx * tx) + (f(6.0) * B + f(30.0) * C) * (tx * tx)
+             + (f(-12.0) * B - f(48.0) * C) * tx + (f(8.0) * B + f(24.0) * C)) * (f(1.0) / f(6.0))
+    inner = ((f(12.0) - f(9.0) * B - f(6.0) * C) * (tx * tx * tx)
+             + (f(-18.0) + f(12.0) * B + f(6.0) * C) * (tx * tx) + (f(6.0) - f(2.0) * B)) * (f(1.0) / f(6.0))
+    return np.where(tx > f(1.0), outer, inner).astype(np.float32)
+
+
+def serial_splat(samples, width, height):
+    """Film::report_samples (render/film.rs:84-120) in float32, samples in the reference's
+    order (row-major), each splatted into the pixels within the filter width 2."""
+    f = np.float32
+    accum = np.zeros((height, width, 3), np.float32)
+    weight = np.zeros((height, width), np.float32)
+    wf, hf = f(width), f(height)
+    for s, t, *rgb in samples.reshape(-1, 5):
+        s, t = f(s), f(t)
+        col_d = f(0.0) + (f(0.5) * (s + f(1.0))) * (wf - f(0.0)) - f(0.5)  # lerp(0, w, .) - 0.5
+        row_d = f(0.0) + (f(0.5) * (t + f(1.0))) * (hf - f(0.0)) - f(0.5)
+        c0 = int(min(max(math.ceil(col_d - f(2.0)), 0), width - 1))
+        c1 = int(min(max(math.floor(col_d + f(2.0)), 0), width - 1))
+        r0 = int(min(max(math.ceil(row_d - f(2.0)), 0), height - 1))
+        r1 = int(min(max(math.floor(row_d + f(2.0)), 0), height - 1))
+        xs = np.arange(c0, c1 + 1, dtype=np.float32)
+        ys = np.arange(r0, r1 + 1, dtype=np.float32)
+        wx = _mitchell1((xs - col_d) / f(2.0))
+        wy = _mitchell1((ys - row_d) / f(2.0))
+        w = (wx[None, :] * wy[:, None]).astype(np.float32)
+        color = np.asarray(rgb, np.float32)
+        accum[r0:r1 + 1, c0:c1 + 1] += color[None, None, :] * w[:, :, None]
+        weight[r0:r1 + 1, c0:c1 + 1] += w
+    return accum, weight
+
+
+@pytest.mark.parametrize("width,height", [(32, 24), (7, 5), (1, 1)])
+def test_film_is_the_serial_mitchell_splat(oracle, width, height):
+    # The oracle's film after one pass equals a float32 restatement of report_samples fed
+    # with that pass's FilmSample records, bit for bit; and every sample's jitter lies in
+    # [-2, 2) pixels of its own pixel centre (film.rs:55-82).
+    w = scenes.cornell_spheres(width, height, 1)
+    st = g.Stage(w.prims, lib=oracle, seed=5)
+    samples = st.samples(w.camera, g.PathTracerIntegrator(), width, height, 0)
+    film = g.Film(width, height, lib=oracle)
+    st.render(w.camera, g.PathTracerIntegrator(), film, 1)
+    accum, weight = film.read()
+    ea, ew = serial_splat(samples, width, height)
+    np.testing.assert_array_equal(weight, ew)
+    np.testing.assert_array_equal(accum, ea)
+    col = (samples[..., 0].astype(np.float64) + 1) / 2 * width - (np.arange(width) + 0.5)[None, :]
+    row = (samples[..., 1].astype(np.float64) + 1) / 2 * height - (np.arange(height) + 0.5)[:, None]
+    for j in (col, row):
+        assert j.min() >= -2 - 1e-4 and j.max() < 2 + 1e-4
 
 
 def test_exr_layout(oracle, tmp_path):
