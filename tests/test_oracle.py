@@ -382,6 +382,59 @@ def test_film_is_the_serial_mitchell_splat(oracle, width, height):
         assert j.min() >= -2 - 1e-4 and j.max() < 2 + 1e-4
 
 
+def _rotation_rows(q):
+    """Mat::rotation (core/matrix.rs:95-121), applied to row vectors (xform.rs:41-54)."""
+    r, (x, y, z) = q.real, q.imaginary
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y + z * r), 2 * (z * x - y * r)],
+                     [2 * (x * y - z * r), 1 - 2 * (z * z + x * x), 2 * (y * z + x * r)],
+                     [2 * (z * x + y * r), 2 * (y * z - x * r), 1 - 2 * (y * y + x * x)]])
+
+
+def camera_rays(cam, s, t, rotated_origin=True):
+    """Camera::compute_ray (core/camera.rs:87-97) in float64.  The camera's matrix is
+    translation * rotation (camera.rs:50-52) applied to row vectors, so the origin is the
+    translation turned by the rotation (kept); `rotated_origin=False` is the plain
+    translation, for the control."""
+    wx = cam.horizontal_aperture / (cam.focal_length * 2.0)
+    wy = cam.vertical_aperture / (cam.focal_length * 2.0)
+    d = np.stack([wx * s, wy * t, -np.ones_like(s)], -1)
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    R = _rotation_rows(cam.rotate)
+    T = np.asarray(cam.translate, np.float64)
+    origin = T @ R if rotated_origin else T
+    return np.concatenate([np.broadcast_to(origin, d.shape), d @ R], -1)
+
+
+def test_camera_rays_are_the_reference_transform(oracle):
+    # DisplayColorIntegrator (integrators.rs:18-34) returns the display colour of the
+    # first hit: rays restated from each FilmSample's (s, t), traced by the oracle, give
+    # every sample's colour.  The plain-translation origin does not.
+    rng = np.random.default_rng(4)
+    prims, colors = [], []
+    for _ in range(6):
+        c = tuple(float(x) for x in rng.uniform(0.1, 0.9, 3))
+        colors.append(c)
+        prims.append(g.Sphere(g.Material.disney().base_color(c).build(),
+                              g.Mat.translation(tuple(rng.uniform(-2, 2, 3))), float(rng.uniform(0.4, 1.0))))
+    colors.append((0.2, 0.7, 0.3))
+    prims.append(g.Mesh(g.Material.disney().base_color(colors[-1]).build(), None,
+                        *scenes.quad((-6, -2.5, -6), (0, 0, 12), (12, 0, 0))))
+    colors = np.array(colors, np.float32)
+    cam = g.Camera(2.0, 2.2, 1.6, 8.0, g.Quat.axis_angle((0.3, 1.0, 0.2), 0.5), (0.5, 1.0, 7.0))
+    st = g.Stage(prims, lib=oracle, seed=3)
+    smp = st.samples(cam, g.DisplayColorIntegrator(), 64, 48)
+    s, t = smp[..., 0].astype(np.float64).ravel(), smp[..., 1].astype(np.float64).ravel()
+    seen = smp[..., 2:].reshape(-1, 3)
+    match = {}
+    for rotated in (True, False):
+        h = st.intersect(camera_rays(cam, s, t, rotated).astype(np.float32))
+        col = np.where((h["prim"] >= 0)[:, None], colors[np.maximum(h["prim"], 0)], 0.0)
+        match[rotated] = (col == seen).all(axis=1).mean()
+    assert match[True] > 0.999, match
+    assert match[False] < 0.9, match
+    assert (seen != 0).any(axis=1).mean() > 0.2  # enough of the image sees the scene
+
+
 def test_exr_layout(oracle, tmp_path):
     st = g.Stage([g.Sphere(g.Material.disney().base_color((0.3, 0.5, 0.7)).build(), None, 10.0)], lib=oracle)
     f = g.Film(5, 3, lib=oracle)
