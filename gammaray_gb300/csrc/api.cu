@@ -137,6 +137,36 @@ using namespace gr;
         if (s__ != GR_OK) return s__;     \
     } while (0)
 
+namespace {
+std::mutex g_scene_holders_mu;  // gr_scene::holders and destroy_pending
+
+void scene_free(gr_scene* s) {
+    { std::lock_guard<std::mutex> busy(s->mu); }  // a render on another thread ends first
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    cudaStream_t st = s->stream;
+    delete s;
+    if (st) cudaStreamDestroy(st);
+}
+}  // namespace
+
+namespace gr {
+void scene_retain(gr_scene* s) {
+    std::lock_guard<std::mutex> g(g_scene_holders_mu);
+    ++s->holders;
+}
+
+void scene_release(gr_scene* s) {
+    bool last;
+    {
+        std::lock_guard<std::mutex> g(g_scene_holders_mu);
+        last = --s->holders == 0 && s->destroy_pending;
+    }
+    if (last) scene_free(s);
+}
+}  // namespace gr
+
 extern "C" {
 
 const char* gr_last_error(void) { return g_err.c_str(); }
@@ -263,12 +293,14 @@ gr_status gr_scene_plan(const gr_scene_desc* desc, gr_scene_info* o) {
 
 gr_status gr_scene_destroy(gr_scene* s) {
     if (!s) return GR_OK;
-    if (s->stream) cudaStreamSynchronize(s->stream);
-    if (s->ev0) cudaEventDestroy(s->ev0);
-    if (s->ev1) cudaEventDestroy(s->ev1);
-    cudaStream_t st = s->stream;
-    delete s;
-    if (st) cudaStreamDestroy(st);
+    {
+        std::lock_guard<std::mutex> g(g_scene_holders_mu);
+        if (s->holders) {  // freed by the server when its last request lets go
+            s->destroy_pending = true;
+            return GR_OK;
+        }
+    }
+    scene_free(s);
     return GR_OK;
 }
 

@@ -265,6 +265,7 @@ struct ServerRequest {
     uint32_t passes_done = 0;
     double submit_ms = 0, start_ms = 0, finish_ms = 0;
     uint64_t bytes = 0;
+    bool admitted = false;  // its job is in the engine
     // Progressive refinement: even passes go to `film` (job), odd passes to `film2`
     // (job2); passes are appended up to `limit`, the next checkpoint (8, 16, 32, ...).
     bool progressive = false;
@@ -323,6 +324,9 @@ struct gr_server {
     uint64_t budget = 0, used = 0;
     uint64_t next_id = 1;
     std::vector<std::unique_ptr<ServerRequest>> reqs;
+    // Scenes of taken requests that were cancelled while running: their paths may still
+    // be queued, so the scene is released once the engine reports all work gathered.
+    std::vector<gr_scene*> retired;
     std::chrono::steady_clock::time_point t0;
     double now_ms() const {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -365,6 +369,7 @@ gr_status schedule(gr_server* s) {
         }
         s->used += r->bytes;
         r->state = GR_REQUEST_RUNNING;
+        r->admitted = true;
         r->start_ms = s->now_ms();
         ++active;
     }
@@ -487,7 +492,16 @@ gr_status gr_server_create(const gr_server_options* o, gr_server** out) {
 }
 
 gr_status gr_server_destroy(gr_server* s) {
-    delete s;
+    if (!s) return GR_OK;
+    std::vector<gr_scene*> held;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        if (s->engine.stream()) cudaStreamSynchronize(s->engine.stream());
+        held = s->retired;
+        for (auto& r : s->reqs) held.push_back(r->req.scene);
+    }
+    delete s;  // the engine's buffers go first; then no path can reach the scenes
+    for (gr_scene* sc : held) scene_release(sc);
     return GR_OK;
 }
 
@@ -529,6 +543,7 @@ gr_status gr_server_submit(gr_server* s, const gr_request* r, uint64_t* id) {
         return GR_ERR_OUT_OF_MEMORY;
     }
     *id = q->id;
+    scene_retain(r->scene);  // until the request is taken (or the server destroyed)
     s->reqs.push_back(std::move(q));
     return GR_OK;
 }
@@ -549,6 +564,11 @@ gr_status gr_server_step(gr_server* s, double budget_ms) {
         bool done = false;
         st = s->engine.run(4, done);
         if (st != GR_OK) return st;
+        if (done && !s->retired.empty()) {  // every appended unit gathered: no path left
+            GR_CUDA_TRY(cudaStreamSynchronize(s->engine.stream()));
+            for (gr_scene* sc : s->retired) scene_release(sc);
+            s->retired.clear();
+        }
         st = progress(s);
         if (st != GR_OK) return st;
         if (s->now_ms() >= t_end) return GR_OK;
@@ -664,6 +684,15 @@ gr_status gr_server_take(gr_server* s, uint64_t id, float* accum, float* weight)
         gr_status cst = copy_film(s, *r, accum, weight);
         if (cst != GR_OK) return cst;
         if (r->film.ptr) s->used -= r->bytes;
+        // A finished request's units are all gathered (copy_film synchronised the stream),
+        // and one never admitted has no paths: its scene can go.  One cancelled while
+        // running may still have paths draining.
+        if (r->state == GR_REQUEST_DONE || !r->admitted) {
+            GR_CUDA_TRY(cudaStreamSynchronize(s->engine.stream()));
+            scene_release(r->req.scene);
+        } else {
+            s->retired.push_back(r->req.scene);
+        }
         s->reqs.erase(s->reqs.begin() + static_cast<long>(k));
         return GR_OK;
     }

@@ -122,6 +122,11 @@ struct gr_scene {
     double build_seconds = 0.0;
     uint64_t device_bytes = 0;
     std::mutex mu;
+    // Server requests that hold the scene (gr::scene_retain); gr_scene_destroy of a held
+    // scene only marks it, and the last gr::scene_release frees it.  Both fields are
+    // guarded by one library-wide mutex.
+    uint32_t holders = 0;
+    bool destroy_pending = false;
 };
 
 struct gr_film {
@@ -164,6 +169,11 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st);
 gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st);
 // Checked builds (GR_CHECKED): whether a render's kernels wrote out of range (read after
 // the render's work has finished); GR_OK otherwise.
+// Scene lifetime across server requests: a request retains its scene from submission
+// until no queued path can reach it any more; gr_scene_destroy waits for the last release.
+void scene_retain(gr_scene* s);
+void scene_release(gr_scene* s);
+
 gr_status pt_index_check();
 gr_status bdpt_index_check();
 gr_status film_gather(const float2* st_buf, const float4* color, uint32_t width, uint32_t height, uint32_t passes,

@@ -168,6 +168,10 @@ typedef struct gr_scene_info {
  * copies the prims, runs the reference SAH build on the host and (GPU library)
  * uploads a wide BVH.  The descriptors may be freed when this returns. */
 gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out);
+/* The handle is dead when this returns.  A scene that server requests still use
+ * (gr_server_submit) is freed when the last of them lets go: at gr_server_take, or for a
+ * request cancelled while running once the server has drained its paths, or at
+ * gr_server_destroy. */
 gr_status gr_scene_destroy(gr_scene* scene);
 /* Host-only dry run of gr_scene_create: validates the descriptor and runs the BVH
  * build, without touching a device.  Fills the counts and the device bytes the scene

@@ -251,3 +251,35 @@ def test_server_progressive_cancel_and_budget(gpu):
     s.take(b)
     with pytest.raises(Exception):
         s.submit(st, w.camera, w.integrator, w.width, w.height, 4, target_rel_mse=-1.0)
+
+
+def test_server_keeps_a_closed_scene_until_its_requests_let_go(gpu):
+    # gr_scene_destroy of a scene that server requests still use defers the free: a
+    # request queued when its scene is closed still renders the same image, and one
+    # cancelled while running drains against the scene before it is freed.
+    w = small_workloads(1, seed=15)[0]
+    keep = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=2)
+    ref = g.Film(w.width, w.height, lib=gpu)
+    keep.render(w.camera, w.integrator, ref, 3)
+    ref_acc, ref_w = ref.read()
+    s = serve.Server(gpu, path_capacity=1 << 16)
+    st = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=2)
+    a = s.submit(st, w.camera, w.integrator, w.width, w.height, 3)
+    st.close()  # queued: the request holds the scene
+    s.run_until_done([a])
+    acc, wt = s.take(a)  # the last holder: the scene is freed here
+    np.testing.assert_array_equal(wt, ref_w)
+    np.testing.assert_allclose(acc, ref_acc, rtol=1e-6, atol=1e-7)
+    st2 = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=3)
+    b = s.submit(st2, w.camera, w.integrator, w.width, w.height, 1024)
+    s.step(0.5)
+    assert s.poll(b).state == 1  # running
+    s.cancel(b)
+    st2.close()
+    s.take(b)  # its paths may still be queued: the scene waits for the engine to drain
+    c = s.submit(keep, w.camera, w.integrator, w.width, w.height, 3)
+    s.run_until_done([c])
+    acc, wt = s.take(c)
+    np.testing.assert_array_equal(wt, ref_w)
+    np.testing.assert_allclose(acc, ref_acc, rtol=1e-6, atol=1e-7)
+    s.close()
