@@ -4,7 +4,9 @@ The reference ships no tests, golden vectors or fixtures, and it cannot be built
 (Rust, no toolchain): the oracle's parity with it is unpinned.  These tests pin the
 restatement against analytic answers and physical invariants instead:
   - ray/sphere and ray/triangle hits with closed-form distances and barycentrics;
-  - BVH traversal equal to the brute-force Bvh::intersect_naive (geom/bvh.rs:385-400);
+  - BVH traversal equal to the brute-force Bvh::intersect_naive (geom/bvh.rs:385-400),
+    and closest hits equal to a float32 numpy brute force of mesh.rs:270-308 and
+    sphere.rs:70-101 at bit-identical distances;
   - a diffuse plane under a white sky returns exactly its albedo (0.5) per path;
   - reflection-only BSDFs are reciprocal, sampling is consistent with pdf_world
     (E[cos/pdf] = pi) and the GGX / PerfectDiffuse albedo is at most 1;
@@ -80,6 +82,98 @@ def test_sah_leaves_hold_one_component(oracle):
     m = g.Mesh(g.Material.disney().build(), None, v, np.arange(len(v)).reshape(-1, 3))
     info = g.Stage([m], lib=oracle).info()
     assert info.num_binary_nodes == 2 * info.num_components - 1
+
+
+_F32_EPS = np.float32(np.finfo(np.float32).eps)
+
+
+def _cross(a, b):  # core/vector.rs:45-50, float32
+    return np.stack([a[..., 1] * b[..., 2] - a[..., 2] * b[..., 1],
+                     a[..., 2] * b[..., 0] - a[..., 0] * b[..., 2],
+                     a[..., 0] * b[..., 1] - a[..., 1] * b[..., 0]], axis=-1)
+
+
+def _dot(a, b):  # core/vector.rs:52-54, left to right
+    return a[..., 0] * b[..., 0] + a[..., 1] * b[..., 1] + a[..., 2] * b[..., 2]
+
+
+def triangle_hits(o, d, a, b, c):
+    """Mesh::intersect_world (geom/mesh.rs:270-308) in float32 for rays (R, 3) against
+    triangles (T, 3): distance (R, T), NaN where there is no hit."""
+    one = np.float32(1.0)
+    e1, e2 = a - c, b - c
+    p = _cross(d[:, None, :], e2[None])
+    det = _dot(e1[None], p)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        inv = one / det
+        t = o[:, None, :] - c[None]
+        u = _dot(t, p) * inv
+        q = _cross(t, e1[None])
+        v = _dot(d[:, None, :], q) * inv
+        dist = _dot(e2[None], q) * inv
+    ok = ~(np.abs(det) < _F32_EPS) & (u >= 0) & (u <= one) & (v >= 0) & ((u + v) <= one) & (dist > _F32_EPS)
+    return np.where(ok, dist, np.float32(np.nan))
+
+
+def sphere_hits(o, d, center, radius):
+    """Sphere::intersect_world (geom/sphere.rs:70-101) in float32: distance (R,), NaN on a miss."""
+    oc = o - center
+    a, b = _dot(d, d), _dot(d, oc)
+    c = _dot(oc, oc) - radius * radius
+    disc = b * b - a * c
+    with np.errstate(invalid="ignore"):
+        s = np.sqrt(disc)
+    neg, pos = -b - s, -b + s
+    hit = np.where(neg > _F32_EPS, neg, np.where(pos > _F32_EPS, pos, np.float32(np.nan)))
+    return np.where(disc > 0, hit, np.float32(np.nan))
+
+
+def test_closest_hits_equal_a_float32_brute_force(oracle):
+    # Every ray against every triangle and sphere with the reference's own arithmetic,
+    # restated in numpy: the oracle's BVH finds the same closest primitive (ties within 1e-6
+    # of the distance excepted) at the bit-identical distance.
+    w = scenes.displaced_sphere(8, 8, 1, tris=3000)
+    mesh = w.prims[0]
+    rng = np.random.default_rng(21)
+    spheres = [g.Sphere(g.Material.disney().build(), g.Mat.translation(tuple(rng.uniform(-2.5, 2.5, 3))),
+                        float(rng.uniform(0.2, 0.6))) for _ in range(4)]
+    st = g.Stage([mesh] + spheres, lib=oracle)
+    n = 2048
+    o = rng.uniform(-3.5, 3.5, (n, 3))
+    dd = rng.normal(size=(n, 3)) * 0.7 - o
+    dd /= np.linalg.norm(dd, axis=1, keepdims=True)
+    rays = np.concatenate([o, dd], 1).astype(np.float32)
+    h = st.intersect(rays)
+    o32, d32 = rays[:, :3], rays[:, 3:]
+    v = np.asarray(mesh.vertices, np.float32)
+    tri = np.asarray(mesh.triangles, np.int64)
+    a, b, c = v[tri[:, 0]], v[tri[:, 1]], v[tri[:, 2]]
+    best_t = np.full(n, np.inf, np.float32)
+    best_prim = np.full(n, -1)
+    best_comp = np.full(n, -1)
+    for r0 in range(0, n, 256):
+        sl = slice(r0, r0 + 256)
+        tt = triangle_hits(o32[sl], d32[sl], a, b, c)
+        k = np.nanargmin(np.where(np.isnan(tt), np.inf, tt), axis=1)
+        tk = tt[np.arange(len(k)), k]
+        hit = ~np.isnan(tk)
+        best_t[sl] = np.where(hit, tk, np.inf)
+        best_prim[sl] = np.where(hit, 0, -1)
+        best_comp[sl] = np.where(hit, k, -1)
+    for j, sp in enumerate(spheres, start=1):
+        center = np.asarray(sp.center, np.float32)
+        ts = sphere_hits(o32, d32, center, np.float32(sp.radius))
+        closer = ~np.isnan(ts) & (ts < best_t)
+        best_t = np.where(closer, ts, best_t)
+        best_prim = np.where(closer, j, best_prim)
+        best_comp = np.where(closer, 0, best_comp)
+    hit_b = best_prim >= 0
+    assert ((h["prim"] >= 0) == hit_b).all()
+    assert hit_b.mean() > 0.3 and (best_prim > 0).sum() > 20  # the mesh and the spheres
+    same = (h["prim"] == best_prim) & (h["component"] == best_comp)
+    tie = np.abs(h["t"] - best_t) <= 1e-6 * np.abs(best_t)
+    assert (same | tie | ~hit_b).all()
+    assert (h["t"][same & hit_b] == best_t[same & hit_b]).all()
 
 
 def test_visibility(oracle):
