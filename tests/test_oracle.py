@@ -407,6 +407,47 @@ def test_light_one_sided(oracle):
     assert L[0].tolist() == [3, 2, 1] and L[1].tolist() == [0, 0, 0]
 
 
+def test_light_sampling_known_answers(oracle):
+    # Bvh::sample_light (geom/bvh.rs:481-496) over a mesh light and a sphere light (a
+    # diffuse sphere is not a light): the light is picked uniformly, the mesh's triangle by
+    # area (mesh.rs:310-327), the point lies on the surface, point_pdf = 1 / (area * lights)
+    # and dir_pdf = cos(direction, geometric normal) / pi (prim.rs:37-51, sphere.rs:103-111).
+    sides = np.array([1.0, 2.0, 3.0])
+    v = np.array([[[s, 0, k], [0, s, k], [0, 0, k]] for k, s in enumerate(sides)], np.float32).reshape(-1, 3)
+    mesh = g.Mesh(g.Material.diffuse_light((4, 4, 4)), None, v, np.arange(9).reshape(3, 3))
+    lamp = g.Sphere(g.Material.diffuse_light((2, 2, 2)), g.Mat.translation((5, 0, 0)), 0.5)
+    other = g.Sphere(g.Material.disney().build(), g.Mat.translation((-5, 0, 0)), 1.0)
+    st = g.Stage([other, mesh, lamp], lib=oracle)
+    n = 40_000
+    s = st.sample_light(np.random.default_rng(9).random((n, 6), dtype=np.float32))
+    assert set(np.unique(s["prim"])) == {1, 2}
+    on_mesh = s["prim"] == 1
+    assert abs(on_mesh.mean() - 0.5) < 5 * math.sqrt(0.25 / n)
+    areas = sides ** 2 / 2
+    np.testing.assert_allclose(s["point_pdf"][on_mesh], 1.0 / (areas.sum() * 2), rtol=1e-5)
+    np.testing.assert_allclose(s["point_pdf"][~on_mesh], 1.0 / (4 * math.pi * 0.25 * 2), rtol=1e-5)
+    p = s["origin"].astype(np.float64)
+    # Mesh points: on one of the three triangles (z = its index), chosen in proportion to area.
+    k = np.rint(p[on_mesh, 2]).astype(int)
+    assert np.abs(p[on_mesh, 2] - k).max() < 1e-6
+    side = sides[k]
+    x, y = p[on_mesh, 0], p[on_mesh, 1]
+    assert (x >= -1e-5).all() and (y >= -1e-5).all() and (x + y <= side + 1e-4).all()
+    counts = np.bincount(k, minlength=3)
+    expect = on_mesh.sum() * areas / areas.sum()
+    assert (np.abs(counts - expect) < 5 * np.sqrt(expect)).all(), (counts, expect)
+    np.testing.assert_allclose(s["geom_normal"][on_mesh], np.broadcast_to([0, 0, 1], (on_mesh.sum(), 3)), atol=1e-6)
+    # Sphere points: on the sphere, with the outward normal.
+    r = p[~on_mesh] - np.array([5.0, 0, 0])
+    np.testing.assert_allclose(np.linalg.norm(r, axis=1), 0.5, rtol=1e-5)
+    np.testing.assert_allclose(s["geom_normal"][~on_mesh], r / 0.5, atol=1e-5)
+    # Directions: cosine-distributed about the geometric normal.
+    cos = (s["direction"].astype(np.float64) * s["geom_normal"]).sum(1)
+    assert cos.min() > -1e-6
+    np.testing.assert_allclose(s["dir_pdf"], np.maximum(cos, 0) / math.pi, atol=2e-6)
+    assert abs(cos.mean() - 2.0 / 3.0) < 5 * cos.std() / math.sqrt(n)  # E[cos] under cos/pi
+
+
 def test_film_constant_colour(oracle):
     # Camera inside a big sphere of one display colour: accum / weight is that colour.
     mat = g.Material.disney().base_color((0.3, 0.5, 0.7)).build()
