@@ -448,6 +448,73 @@ def test_light_sampling_known_answers(oracle):
     assert abs(cos.mean() - 2.0 / 3.0) < 5 * cos.std() / math.sqrt(n)  # E[cos] under cos/pi
 
 
+def _coord_system(n):  # core/vector.rs:91-104
+    big_x = np.abs(n[:, 0]) > np.abs(n[:, 1])
+    inv_x = 1.0 / np.sqrt(n[:, 0] ** 2 + n[:, 2] ** 2)
+    inv_y = 1.0 / np.sqrt(n[:, 1] ** 2 + n[:, 2] ** 2)
+    zero = np.zeros(len(n))
+    v2 = np.where(big_x[:, None], np.stack([-n[:, 2] * inv_x, zero, n[:, 0] * inv_x], 1),
+                  np.stack([zero, n[:, 2] * inv_y, -n[:, 1] * inv_y], 1))
+    return v2, np.cross(n, v2)
+
+
+def surface_frame(a, b, c, bary, normals=None, uvs=None, uv_sign=1.0):
+    """Mesh::compute_surface_props (geom/mesh.rs:190-241) in float64 for one triangle at
+    barycentrics (n, 3) = (u, v, w).  As written there: the uv determinant adds its two
+    products, and dpdu combines the uv differences, not the position edges.  `uv_sign` = -1
+    gives the textbook determinant, for a control."""
+    unit = lambda x: x / np.linalg.norm(x, axis=-1, keepdims=True)
+    gn = unit(np.cross(a - c, b - c))
+    if normals is None:
+        nrm = np.broadcast_to(gn, bary.shape).copy()
+    else:
+        nrm = unit(bary[:, :1] * normals[0] + bary[:, 1:2] * normals[1] + bary[:, 2:] * normals[2])
+    at, bt, ct = uvs if uvs is not None else (np.zeros(2),) * 3
+    uv1, uv2 = np.append(at - ct, 0.0), np.append(bt - ct, 0.0)  # uvs are Vecs (u, v, 0)
+    det = uv1[0] * uv2[1] + uv_sign * uv1[1] * uv2[0]
+    if det == 0.0:
+        t, bn = _coord_system(nrm)
+    else:
+        dpdu = (uv2[1] * uv1 - uv1[1] * uv2) / det  # from the uv differences (mesh.rs:232)
+        bn = unit(np.cross(nrm, dpdu))
+        t = np.cross(bn, nrm)
+    return nrm, t, bn, gn
+
+
+def test_light_surface_frames_are_the_reference_mesh_frames(oracle):
+    # The frame sample_light returns at a point of a mesh light is compute_surface_props at
+    # that point's barycentrics: interpolated shading normals, tangents from the uvs with
+    # the reference's determinant (uv1.x uv2.y + uv1.y uv2.x, mesh.rs:222), and without
+    # uvs coord_system(normal) (vector.rs:91-104).
+    a, b, c = (np.array(x, np.float64) for x in ([2, 0, 0], [0, 2, 0], [0, 0, 0]))
+    normals = np.array([[0.3, 0, 1], [0, 0.4, 1], [-0.2, -0.1, 1]], np.float64)
+    normals /= np.linalg.norm(normals, axis=1, keepdims=True)
+    # uv1 = (0.1, 0.8), uv2 = (0.7, 0.2): the reference determinant 0.58, the textbook -0.54
+    uvs = np.array([[0.2, 0.9], [0.8, 0.3], [0.1, 0.1]], np.float64)
+    lit = g.Material.diffuse_light((1, 1, 1))
+    with_attrs = g.Mesh(lit, None, np.stack([a, b, c]), [[0, 1, 2]], normals=normals, tri_normals=[[0, 1, 2]],
+                        uvs=uvs, tri_uvs=[[0, 1, 2]])
+    shifted = [a + [5, 0, 0], b + [5, 0, 0], c + [5, 0, 0]]
+    plain = g.Mesh(lit, None, np.stack(shifted), [[0, 1, 2]])
+    st = g.Stage([with_attrs, plain], lib=oracle)
+    s = st.sample_light(np.random.default_rng(12).random((4000, 6), dtype=np.float32))
+    for prim, (pa, pb, pc), kw in ((0, (a, b, c), dict(normals=normals, uvs=uvs)), (1, shifted, {})):
+        m = s["prim"] == prim
+        assert m.sum() > 1000
+        p = s["origin"][m].astype(np.float64)
+        # barycentrics of the point: p = u a + v b + w c in the triangle's plane (z = 0)
+        M = np.array([[pa[0] - pc[0], pb[0] - pc[0]], [pa[1] - pc[1], pb[1] - pc[1]]])
+        uv = np.linalg.solve(M, (p[:, :2] - pc[:2]).T).T
+        bary = np.column_stack([uv, 1 - uv.sum(1)])
+        nrm, t, bn, gn = surface_frame(np.asarray(pa, float), np.asarray(pb, float), np.asarray(pc, float), bary, **kw)
+        for got, want in ((s["normal"][m], nrm), (s["tangent"][m], t), (s["binormal"][m], bn),
+                          (s["geom_normal"][m], np.broadcast_to(gn, nrm.shape))):
+            np.testing.assert_allclose(got, want, atol=1e-4)
+        if prim == 0:  # the control: with the textbook determinant's sign the tangent flips
+            _, t_book, _, _ = surface_frame(a, b, c, bary, normals=normals, uvs=uvs, uv_sign=-1.0)
+            assert np.abs(s["tangent"][m] + t_book).max() < 1e-4
+
+
 def test_film_constant_colour(oracle):
     # Camera inside a big sphere of one display colour: accum / weight is that colour.
     mat = g.Material.disney().base_color((0.3, 0.5, 0.7)).build()
