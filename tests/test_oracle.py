@@ -440,7 +440,15 @@ def test_light_sampling_known_answers(oracle):
     # Sphere points: on the sphere, with the outward normal.
     r = p[~on_mesh] - np.array([5.0, 0, 0])
     np.testing.assert_allclose(np.linalg.norm(r, axis=1), 0.5, rtol=1e-5)
-    np.testing.assert_allclose(s["geom_normal"][~on_mesh], r / 0.5, atol=1e-5)
+    nrm = r / np.linalg.norm(r, axis=1, keepdims=True)
+    np.testing.assert_allclose(s["geom_normal"][~on_mesh], nrm, atol=1e-5)
+    # Sphere::compute_surface_props (sphere.rs:28-45): tangent (-n.z, 0, n.x) normalised,
+    # binormal n x tangent (the poles' x-axis branch has probability zero here).
+    tan = np.stack([-nrm[:, 2], np.zeros(len(nrm)), nrm[:, 0]], 1)
+    tan /= np.linalg.norm(tan, axis=1, keepdims=True)
+    np.testing.assert_allclose(s["normal"][~on_mesh], nrm, atol=1e-5)
+    np.testing.assert_allclose(s["tangent"][~on_mesh], tan, atol=1e-4)
+    np.testing.assert_allclose(s["binormal"][~on_mesh], np.cross(nrm, tan), atol=1e-4)
     # Directions: cosine-distributed about the geometric normal.
     cos = (s["direction"].astype(np.float64) * s["geom_normal"]).sum(1)
     assert cos.min() > -1e-6
