@@ -8,8 +8,11 @@
 // is compiled with -ffp-contract=off because Rust never fuses a*b+c into an FMA.
 //
 // Parity unpinned: the reference ships no tests, golden vectors or fixtures, and cannot
-// be built here (no Rust toolchain).  This restatement is checked by analytic
-// known-answer tests and physical invariants in tests/.
+// be built here (no Rust toolchain).  This restatement is checked in tests/ by analytic
+// known-answer tests and physical invariants, against independent numpy restatements
+// of the reference's code, and against golden vectors it wrote
+// (tests/golden/oracle_golden.npz).  Those restatements cover the Disney material,
+// intersection, shading frames, light sampling, camera and film.
 //
 // Random numbers.  The reference seeds XorShift from thread_rng (core/random.rs:13-20)
 // and is not reproducible.  Here every random number is a pure function of
