@@ -675,6 +675,25 @@ def test_bdpt_runs_and_agrees_with_pt(oracle):
     assert abs(a - b) / a < 0.2  # the reference BDPT's uniform weights are close to, not equal to, PT
 
 
+@pytest.mark.parametrize("integrator", ["bdpt", "pt"])
+def test_a_visible_light_is_its_emission(oracle, integrator):
+    # A camera facing the emitting side of a lone quad light.  With the reference BDPT
+    # (integrators.rs:343-418) the camera path hits the light and stops (no lobes): the
+    # (1, 0) strategy has weight 1/1 and returns Le, the (1, 1) connection joins two
+    # points of a lobe-less light (value 0) and the light walk escapes.  The path tracer
+    # (integrators.rs:42-100) returns the same Le.  So every sample is Le or, on a miss, 0.
+    Le = (2.0, 3.0, 4.0)
+    v, t = scenes.quad((-1, -1, 0), (2, 0, 0), (0, 2, 0))  # normal +z
+    st = g.Stage([g.Mesh(g.Material.diffuse_light(Le), None, v, t)], lib=oracle, seed=4)
+    cam = g.Camera.with_fov(50.0, translate=(0.2, -0.1, 2.5))
+    integ = g.BdptIntegrator() if integrator == "bdpt" else g.PathTracerIntegrator()
+    s = st.samples(cam, integ, 32, 32)[..., 2:].reshape(-1, 3)
+    lit = (s == np.float32(Le)).all(axis=1)
+    dark = (s == 0).all(axis=1)
+    assert (lit | dark).all()
+    assert 0.3 < lit.mean() < 0.95  # the light fills part of the view
+
+
 def test_invalid_inputs(oracle):
     with pytest.raises(_abi.GrError):
         g.Stage([g.Sphere(g.Material.disney().build(), None, -1.0)], lib=oracle)
