@@ -92,6 +92,23 @@ def check(err, q999, worst, what):
 
 @pytest.mark.parametrize("k", range(len(MATERIALS)))
 def test_eval_and_pdf_match_the_float64_restatement(oracle, k):
+    check_eval_and_pdf(oracle, k)
+
+
+@pytest.mark.parametrize("k", range(len(MATERIALS)))
+def test_sample_world_matches_the_float64_restatement(oracle, k):
+    check_sample_world(oracle, k)
+
+
+@pytest.mark.gpu
+def test_gpu_bsdf_matches_the_float64_restatement(gpu):
+    # The CUDA library's BSDF queries against the same restatement and bars.
+    for k in range(len(MATERIALS)):
+        check_eval_and_pdf(gpu, k)
+        check_sample_world(gpu, k, max_disagree=1e-3)
+
+
+def check_eval_and_pdf(lib, k):
     M = MATERIALS[k]
     m = M.build(g)
     rng = np.random.default_rng(100 + k)
@@ -99,16 +116,18 @@ def test_eval_and_pdf_match_the_float64_restatement(oracle, k):
     wi, wo = unit(N, rng), unit(N, rng)
     lobes = M.lobes()
     for c2l in (True, False):
-        got = g.bsdf_eval(m, fr, wi, wo, c2l, lib=oracle)
+        got = g.bsdf_eval(m, fr, wi, wo, c2l, lib=lib)
         ref = R.f_world(lobes, fr, wi.astype(np.float64), wo.astype(np.float64), c2l)
         check(rel_err(got, ref), 5e-3, 5e-2, f"f camera_to_light={c2l}")
-    got = g.bsdf_pdf(m, fr, wi, wo, lib=oracle)
+    got = g.bsdf_pdf(m, fr, wi, wo, lib=lib)
     ref = R.pdf_world(lobes, fr, wi.astype(np.float64), wo.astype(np.float64))
     check(rel_err(got, ref), 5e-3, 5e-2, "pdf")
 
 
-@pytest.mark.parametrize("k", range(len(MATERIALS)))
-def test_sample_world_matches_the_float64_restatement(oracle, k):
+def check_sample_world(lib, k, max_disagree=0.0):
+    """`max_disagree`: the fraction of queries allowed to differ in the discrete choices
+    (valid or not, which lobe): 0 for the oracle, the GPU-vs-oracle parity bar for the
+    CUDA library, whose float32 rounding can flip a decision at a boundary."""
     M = MATERIALS[k]
     m = M.build(g)
     rng = np.random.default_rng(200 + k)
@@ -117,14 +136,16 @@ def test_sample_world_matches_the_float64_restatement(oracle, k):
     u = rng.random((N, 3), dtype=np.float32)
     c2l = bool(k % 3)
     lobes = M.lobes()
-    s = g.bsdf_sample(m, fr, wi, u, c2l, lib=oracle)
+    s = g.bsdf_sample(m, fr, wi, u, c2l, lib=lib)
     rad, o_w, pdf, r, valid = R.sample_world(lobes, fr, wi.astype(np.float64), u, c2l)
-    np.testing.assert_array_equal(s["kind"] != 0, valid)
-    if not valid.any():
-        assert not lobes  # a material without lobes samples nothing (material.rs:166-174)
+    if not lobes:  # a material without lobes samples nothing (material.rs:166-174)
+        assert not (s["kind"] != 0).any() and not valid.any()
         return
     bits = np.array([lobe_kind_bits(x) for x in lobes], np.uint32)[r]
-    np.testing.assert_array_equal(s["kind"][valid], bits[valid])  # the lobe u[0] picks
+    agree = (s["kind"] != 0) == valid
+    agree &= ~valid | (s["kind"] == bits)  # the lobe u[0] picks
+    assert (~agree).mean() <= max_disagree, (~agree).sum()
+    valid &= agree
     # The sampled direction: away from normal incidence, where the float32 azimuth of a
     # nearly normal stretched vector (sin(theta) from 1 - cos2) is not defined to float64.
     i_loc = R.to_local(wi.astype(np.float64), fr)
