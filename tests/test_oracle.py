@@ -716,6 +716,53 @@ def test_a_visible_light_is_its_emission(oracle, integrator):
     assert 0.3 < lit.mean() < 0.95  # the light fills part of the view
 
 
+def roulette_ladder(max_bounces=400):
+    """Throughput after k bounces off PerfectDiffuse (f cos / pdf = 0.5 each) under the
+    path tracer's Russian roulette (integrators.rs:64-86): from depth 11 a surviving
+    path is divided by clamped_lerp(0.25, 1, luminance), from depth 21 by
+    clamped_lerp(0.10, 0.75, luminance)."""
+    t, out = 1.0, [1.0]
+    for depth in range(max_bounces):
+        t *= 0.5
+        if depth > 10 or t < np.finfo(np.float32).eps:
+            lo, hi = (0.10, 0.75) if depth > 20 else (0.25, 1.0)
+            t /= lo + min(max(t, 0.0), 1.0) * (hi - lo)
+        out.append(t)
+    return np.array(out)
+
+
+def test_path_radiance_follows_the_roulette_ladder(oracle):
+    # A closed box of PerfectDiffuse walls with one quad light facing in.  A path that
+    # reaches the light after k diffuse bounces carries exactly ladder[k] * Le; every
+    # other path ends at 0 (roulette, or the light's back).
+    walls = []
+    for axis in range(3):
+        for side in (-1.0, 1.0):
+            o = np.full(3, -1.0)
+            o[axis] = side
+            e1, e2 = np.zeros(3), np.zeros(3)
+            e1[(axis + 1) % 3], e2[(axis + 2) % 3] = 2.0, 2.0
+            walls.append(g.Mesh(g.Material.diffuse(), None, *scenes.quad(tuple(o), tuple(e1), tuple(e2))))
+    light = g.Mesh(g.Material.diffuse_light((1, 1, 1)), None,
+                   *scenes.quad((-0.5, 0.99, -0.5), (1, 0, 0), (0, 0, 1)))  # normal x * z = -y, into the box
+    st = g.Stage(walls + [light], lib=oracle, seed=6)
+    cam = g.Camera.with_fov(70.0, translate=(0.0, -0.2, 0.8))
+    s = st.samples(cam, g.PathTracerIntegrator(), 64, 64)[..., 2:].reshape(-1, 3).astype(np.float64)
+    assert (s[:, 0] == s[:, 1]).all() and (s[:, 1] == s[:, 2]).all()  # grey all the way
+    L = s[:, 0]
+    ladder = roulette_ladder()
+    lit = L > 0
+    dist = np.abs(np.log(L[lit])[:, None] - np.log(ladder)[None, :])
+    k = dist.argmin(axis=1)
+    np.testing.assert_allclose(L[lit], ladder[k], rtol=1e-4)
+    # The match is unambiguous: the next-nearest rung is far off, except where the ladder
+    # has converged to the aggressive roulette's fixed point (beyond ~26 bounces, rare).
+    second = np.partition(dist, 1, axis=1)[:, 1]
+    assert (second < 5e-4).sum() <= 2
+    assert lit.mean() > 0.05
+    assert (k >= 12).sum() >= 20  # paths past the roulette depth reach the light too
+
+
 def test_invalid_inputs(oracle):
     with pytest.raises(_abi.GrError):
         g.Stage([g.Sphere(g.Material.disney().build(), None, -1.0)], lib=oracle)
