@@ -683,16 +683,16 @@ gr_status gr_server_take(gr_server* s, uint64_t id, float* accum, float* weight)
         }
         gr_status cst = copy_film(s, *r, accum, weight);
         if (cst != GR_OK) return cst;
+        // A finished request's units are all gathered, and one never admitted has no
+        // paths: its scene can go.  One cancelled while running may still have paths
+        // draining.  (Nothing is changed before the last call that can fail.)
+        const bool drained = r->state == GR_REQUEST_DONE || !r->admitted;
+        if (drained) GR_CUDA_TRY(cudaStreamSynchronize(s->engine.stream()));
         if (r->film.ptr) s->used -= r->bytes;
-        // A finished request's units are all gathered (copy_film synchronised the stream),
-        // and one never admitted has no paths: its scene can go.  One cancelled while
-        // running may still have paths draining.
-        if (r->state == GR_REQUEST_DONE || !r->admitted) {
-            GR_CUDA_TRY(cudaStreamSynchronize(s->engine.stream()));
+        if (drained)
             scene_release(r->req.scene);
-        } else {
+        else
             s->retired.push_back(r->req.scene);
-        }
         s->reqs.erase(s->reqs.begin() + static_cast<long>(k));
         return GR_OK;
     }
