@@ -668,22 +668,30 @@ def test_camera_rays_are_the_reference_transform(oracle):
 
 
 def test_exr_layout(oracle, tmp_path):
-    st = g.Stage([g.Sphere(g.Material.disney().base_color((0.3, 0.5, 0.7)).build(), None, 10.0)], lib=oracle)
-    f = g.Film(5, 3, lib=oracle)
-    st.render(g.Camera.with_fov(60.0), g.DisplayColorIntegrator(), f, 1)
+    # ExrWriter (render/exr.rs:138-199): magic and version, then after the header a line
+    # offset table and one uncompressed scanline per row, bottom row first, each holding
+    # its y, its byte count and the B, G and R planes of float32.  Every line is decoded.
+    W, H = 7, 5
+    w = scenes.cornell_spheres(W, H, 1)
+    st = g.Stage(w.prims, lib=oracle, seed=1)
+    f = g.Film(W, H, lib=oracle)
+    st.render(w.camera, g.DisplayColorIntegrator(), f, 2)
     path = tmp_path / "o.exr"
     f.write_exr(str(path))
     b = path.read_bytes()
     assert struct.unpack("<ii", b[:8]) == (20000630, 2)
-    line = 8 + 5 * 12
-    offsets = [struct.unpack("<Q", b[len(b) - 3 * line - 8 * 3 + 8 * k:][:8])[0] for k in range(3)]
-    assert offsets == [len(b) - 3 * line + k * line for k in range(3)]
+    line = 8 + W * 12
+    table = len(b) - H * line - 8 * H
+    offsets = [struct.unpack("<Q", b[table + 8 * k:table + 8 * k + 8])[0] for k in range(H)]
+    assert offsets == [len(b) - H * line + k * line for k in range(H)]
     rgb = f.resolve()
-    first = b[offsets[0]:offsets[0] + line]
-    assert struct.unpack("<iI", first[:8]) == (0, line - 8)
-    planes = np.frombuffer(first[8:], "<f4").reshape(3, 5)
-    np.testing.assert_array_equal(planes[0], rgb[2, :, 2])  # B plane of the bottom row
-    np.testing.assert_array_equal(planes[2], rgb[2, :, 0])  # R plane
+    assert len(np.unique(rgb.reshape(-1, 3), axis=0)) > 3  # a varied image, so order matters
+    for y, off in enumerate(offsets):
+        assert struct.unpack("<iI", b[off:off + 8]) == (y, line - 8)
+        planes = np.frombuffer(b[off + 8:off + line], "<f4").reshape(3, W)
+        row = rgb[H - 1 - y]
+        for plane, channel in zip(planes, (2, 1, 0)):  # B, G, R
+            np.testing.assert_array_equal(plane, row[:, channel])
 
 
 def test_bdpt_runs_and_agrees_with_pt(oracle):
