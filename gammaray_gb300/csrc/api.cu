@@ -1,6 +1,7 @@
 // C ABI of libgammaray_gpu.so (include/gammaray.h): handle management, uploads and
 // the host side of every entry point.  All device work of a scene runs on the
 // scene's own stream; host-buffer calls copy in, launch and copy out on that stream.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -103,7 +104,7 @@ DevCamera make_camera(const gr_camera& c) {
     return d;
 }
 
-static gr_status check_params(const gr_render_params* p) {
+gr_status check_render_params(const gr_render_params* p) {
     if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "null params");
     if (p->integrator < 0 || p->integrator > 2) return fail(GR_ERR_INVALID_ARGUMENT, "unknown integrator");
     if (p->integrator == GR_INTEGRATOR_BDPT && p->max_depth > 16)
@@ -252,6 +253,11 @@ gr_status gr_scene_create(const gr_scene_desc* desc, gr_scene** out) {
     d.num_components = static_cast<uint32_t>(h.num_components);
     d.width = h.width;
     d.stack_depth = h.stack_depth;
+    d.step_budget = 8u * d.num_components + 4096u;
+    if (const char* e = std::getenv("GR_STEP_BUDGET")) {
+        long v = std::atol(e);
+        if (v > 0) d.step_budget = static_cast<uint32_t>(std::min<long>(v, 0x7FFFFFFFL));
+    }
     d.env[0] = desc->environment[0];
     d.env[1] = desc->environment[1];
     d.env[2] = desc->environment[2];
@@ -521,7 +527,7 @@ static gr_status run_render(gr_scene* s, const gr_camera* c, const gr_render_par
 
 gr_status gr_render(gr_scene* s, const gr_camera* c, const gr_render_params* p, gr_film* f) {
     if (!s || !c || !f) return fail(GR_ERR_INVALID_ARGUMENT, "null argument");
-    GR_TRY(check_params(p));
+    GR_TRY(check_render_params(p));
     std::lock_guard<std::mutex> g(s->mu);
     float4* splat = nullptr;
     if (p->integrator == GR_INTEGRATOR_BDPT && p->light_tracing) {
@@ -540,7 +546,7 @@ gr_status gr_render(gr_scene* s, const gr_camera* c, const gr_render_params* p, 
 gr_status gr_render_samples(gr_scene* s, const gr_camera* c, const gr_render_params* p, uint32_t w, uint32_t h,
                             float* out) {
     if (!s || !c || !out || w == 0 || h == 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad argument");
-    GR_TRY(check_params(p));
+    GR_TRY(check_render_params(p));
     std::lock_guard<std::mutex> g(s->mu);
     size_t bytes = static_cast<size_t>(w) * h * 5 * sizeof(float);
     DevBuf dev;

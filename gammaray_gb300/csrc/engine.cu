@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(BS) k_eng_extend(EngineCtl* c, int cur, const 
         const DeviceScene& s = jobs[__float_as_uint(o4.w)].scene;
         TravState t;
         trav_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX);
-        const uint32_t budget = 8u * s.num_components + 4096u;
+        const uint32_t budget = s.step_budget;
         uint32_t steps = 0;
         while (!trav_step<W, false, false>(s, t, stk, &c->err, nullptr)) {
             if (++steps > budget) {

@@ -362,24 +362,29 @@ int device_sm_count() {
 // ---------------------------------------------------------------------------
 // Render entry point that allocates nothing.
 //
-// Some callers cannot let a library allocate device memory: a host that owns all GPU
-// memory through its own pool and forbids hidden allocations, a real-time frame loop
-// where cudaMalloc / cudaFree would stall it (they synchronise the device), or code
-// that enqueues work on a stream it does not want the library to synchronise.  For
-// them, gr_render_static runs the same wavefront kernels as gr_render, with the path
-// state and queues in one fixed device array of this library instead of buffers of
-// the scene.  The caller passes the inputs (scene, camera, settings) and the output
+// Some callers cannot let a library allocate device memory: an application that owns
+// all GPU memory through its own pool and forbids hidden allocations (a host program
+// that embeds this renderer under a fixed memory budget), or a real-time frame loop
+// that a cudaMalloc / cudaFree would stall, since both synchronise the whole device.
+// For them, gr_render_static runs the same wavefront kernels as gr_render, with the
+// path state and queues in one fixed device array of this library instead of buffers
+// of the scene.  The caller passes the inputs (scene, camera, settings) and the output
 // (a device film of width * height float4 {accum.rgb, weight}, accumulated into).
 //
 // Limits and sharing:
 //   - at most STATIC_MAX_PATHS (131072) pixels per image; larger sizes are rejected;
 //   - the array (STATIC_SCRATCH_BYTES, about 18 MB) is held by every GPU that loads the
 //     library until the process exits;
-//   - every call uses the same array and it keeps the last call's contents, so calls
-//     that overlap on the GPU (other threads, other streams) race: serialise them;
+//   - every call uses the same array and it keeps the last call's contents (each call
+//     clears the counters it needs), so calls that overlap on the GPU (other threads,
+//     other streams) race: serialise them;
 //   - the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call before any
-//     stream capture.
+//     stream capture;
+//   - the call returns once its work on the stream has finished: it waits for the
+//     stream at the end to read the traversal status (GR_ERR_TIMEOUT,
+//     GR_ERR_STACK_OVERFLOW, as gr_render reports them), and with max_depth == 0 (the
+//     reference's unbounded depth) also every 4 bounces to see whether any path is left.
 namespace gr {
 namespace {
 
@@ -390,6 +395,10 @@ constexpr size_t STATIC_PER_PATH = 16 + 16 + 8 + 8 + 2 * 4 + 2 * 16 + 2 * 16 + 1
 constexpr size_t STATIC_SCRATCH_BYTES = STATIC_MAX_PATHS * STATIC_PER_PATH + 256;
 
 static __device__ __align__(256) unsigned char g_static_scratch[STATIC_SCRATCH_BYTES];
+
+// Writes a pass's starting queue length (the copy from a host variable it replaces
+// would stage through pageable memory).
+__global__ void k_set_count(uint32_t* c, uint32_t n) { *c = n; }
 
 constexpr int STATIC_MAX_DEVICES = 64;
 std::mutex g_static_mu;
@@ -437,6 +446,7 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
         set_error("gr_render_static: null argument or empty image");
         return GR_ERR_INVALID_ARGUMENT;
     }
+    GR_TRY_S(check_render_params(rp));
     if (rp->integrator != GR_INTEGRATOR_PATH_TRACER && rp->integrator != GR_INTEGRATOR_DISPLAY_COLOR) {
         set_error("gr_render_static: only the path tracer and the display-colour integrator are supported");
         return GR_ERR_UNSUPPORTED;
@@ -448,6 +458,9 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
         return GR_ERR_INVALID_ARGUMENT;
     }
     if (rp->spp == 0) return GR_OK;
+    // Held for the whole call, which ends after its device work: gr_scene_destroy on
+    // another thread waits for it.
+    std::lock_guard<std::mutex> scene_lock(sc->mu);
     void* base = nullptr;
     GR_TRY_S(static_scratch(&base));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -497,7 +510,7 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
     for (uint32_t pass = 0; pass < rp->spp; ++pass) {
         p.first_pass = rp->first_pass + pass;
         uint32_t n = npix;
-        GR_CUDA_TRY(cudaMemcpyAsync(cnt + CNT_QUEUE0, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        k_set_count<<<1, 1, 0, st>>>(cnt + CNT_QUEUE0, n);
         k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, tp, light, key, stb, q_slot[0], q_o[0], q_d[0]);
         GR_CUDA_TRY(cudaGetLastError());
         for (uint32_t depth = 0;; ++depth) {
@@ -528,5 +541,18 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
         }
         GR_TRY_S(film_gather(stb, light, width, height, 1, reinterpret_cast<float4*>(film_dev), st));
     }
-    return GR_OK;
+    // The traversal status of every pass, read like gr_render reads it: a ray over the
+    // step budget (2) or the stack bound (1), and the ray index.
+    int status[2] = {0, 0};
+    GR_CUDA_TRY(cudaMemcpyAsync(status, err, sizeof(status), cudaMemcpyDeviceToHost, st));
+    GR_CUDA_TRY(cudaStreamSynchronize(st));
+    if (status[0] == 2) {
+        set_error("gr_render_static: traversal step budget exceeded (ray " + std::to_string(status[1]) + ")");
+        return GR_ERR_TIMEOUT;
+    }
+    if (status[0]) {
+        set_error("gr_render_static: traversal stack bound exceeded");
+        return GR_ERR_STACK_OVERFLOW;
+    }
+    return pt_index_check();
 }

@@ -192,6 +192,10 @@ int device_sm_count();
 // kernel is reported instead of blocking the caller forever.
 gr_status sync_check(cudaStream_t st, const char* what, uint32_t bounce, uint32_t n);
 
+// Validates a gr_render_params (integrator kind, BDPT depth, extensions that apply to
+// BDPT only); sets the error text and returns GR_ERR_INVALID_ARGUMENT when it fails.
+gr_status check_render_params(const gr_render_params* p);
+
 // Camera::new (core/camera.rs:42-61) evaluated on the host.
 DevCamera make_camera(const gr_camera& c);
 

@@ -52,6 +52,11 @@ struct DeviceScene {
     uint32_t num_components;
     uint32_t width;        // BVH width
     uint32_t stack_depth;  // worst-case traversal stack (entries)
+    // Traversal steps (node or leaf visits) after which an extension ray is abandoned and
+    // the render reports GR_ERR_TIMEOUT: 8 per component + 4096, more than any ray of a
+    // valid tree needs.  GR_STEP_BUDGET=<n> in the environment at scene creation sets
+    // it instead (a host-side way to test that report; no GPU fault is involved).
+    uint32_t step_budget;
     float env[3];
     int32_t has_env;
 };

@@ -50,7 +50,7 @@ __global__ void GR_EXTEND_BOUNDS k_extend(DeviceScene s, const uint32_t* __restr
     const uint32_t n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
     uint32_t counts[2] = {0, 0};
-    const uint32_t budget = 8u * s.num_components + 4096u;
+    const uint32_t budget = s.step_budget;
     auto trace = [&](uint32_t q) {
         float4 o4 = q_o[q], d4 = q_d[q];
         TravState t;

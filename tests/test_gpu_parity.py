@@ -229,17 +229,74 @@ def test_converged_render_within_rel_mse(gpu, oracle):
     assert rel_mse <= 1e-3, rel_mse
 
 
+def _exr_lines(b, W, H):
+    """Decodes an ExrWriter file (render/exr.rs:138-199): the magic and version, the line
+    offset table after the header, and per line its y, byte count and B, G, R float32
+    planes.  Returns the image as (H, W, 3) RGB with row 0 first, like Film::pixels."""
+    import struct
+
+    assert struct.unpack("<ii", b[:8]) == (20000630, 2)
+    line = 8 + W * 12
+    table = len(b) - H * line - 8 * H
+    offsets = [struct.unpack("<Q", b[table + 8 * k:table + 8 * k + 8])[0] for k in range(H)]
+    assert offsets == [len(b) - H * line + k * line for k in range(H)]
+    img = np.empty((H, W, 3), np.float32)
+    for y, off in enumerate(offsets):
+        assert struct.unpack("<iI", b[off:off + 8]) == (y, line - 8)
+        planes = np.frombuffer(b[off + 8:off + line], "<f4").reshape(3, W)
+        img[H - 1 - y] = planes[::-1].T  # B, G, R planes; line y holds film row H - 1 - y
+    return img
+
+
 def test_exr_matches_oracle(gpu, oracle, tmp_path):
-    w = scenes.cornell_spheres(20, 12, 1)
+    # A varied display-colour image of odd width: the GPU's file is the oracle's, byte for
+    # byte (header, offset table, and every line's B, G, R planes, rows flipped), and it
+    # decodes to the GPU film's own resolve.
+    W, H = 21, 13
+    w = scenes.cornell_spheres(W, H, 1)
     out = []
     for L, name in ((gpu, "g.exr"), (oracle, "o.exr")):
         st = g.Stage(w.prims, lib=L, seed=3)
-        f = g.Film(20, 12, lib=L)
+        f = g.Film(W, H, lib=L)
         st.render(w.camera, g.DisplayColorIntegrator(), f, 2)
         f.write_exr(str(tmp_path / name))
-        out.append((tmp_path / name).read_bytes())
-    assert len(out[0]) == len(out[1])
-    assert out[0][:400] == out[1][:400]  # header and offset table identical
+        out.append(((tmp_path / name).read_bytes(), f.resolve()))
+    (bg, rg), (bo, ro) = out
+    assert len(np.unique(rg.reshape(-1, 3), axis=0)) > 3  # varied, so a misplaced line shows
+    np.testing.assert_array_equal(_exr_lines(bg, W, H), rg)
+    np.testing.assert_array_equal(_exr_lines(bo, W, H), ro)
+    assert bg == bo
+
+
+def test_exr_adds_the_light_tracing_splats(gpu, tmp_path):
+    # A BDPT film with light-tracing splats: every EXR line decodes to the film's resolve
+    # (accum / weight + splat / passes), bit for bit.
+    W, H = 19, 11
+    w = scenes.cornell_spheres(W, H, 1)
+    st = g.Stage(w.prims, lib=gpu, seed=8)
+    f = g.Film(W, H, lib=gpu)
+    st.render(w.camera, g.BdptIntegrator(max_depth=8, mis=1, light_tracing=1), f, 3)
+    assert f.read_splat().sum() > 0
+    f.write_exr(str(tmp_path / "s.exr"))
+    np.testing.assert_array_equal(_exr_lines((tmp_path / "s.exr").read_bytes(), W, H), f.resolve())
+
+
+def test_step_budget_is_reported(gpu, monkeypatch):
+    # A traversal step budget that the rays exceed (set on the host, GR_STEP_BUDGET, read at
+    # scene creation; no GPU fault): the render returns GR_ERR_TIMEOUT naming the budget,
+    # and a render of a scene with the normal budget then works.
+    w = scenes.cornell_spheres(32, 32, 1)
+    monkeypatch.setenv("GR_STEP_BUDGET", "1")
+    st = g.Stage(w.prims, lib=gpu, seed=2)
+    monkeypatch.delenv("GR_STEP_BUDGET")
+    f = g.Film(32, 32, lib=gpu)
+    with pytest.raises(_abi.GrError) as e:
+        st.render(w.camera, w.integrator, f, 1)
+    assert e.value.status == 5 and "step budget" in str(e.value)
+    ok = g.Stage(w.prims, lib=gpu, seed=2)
+    f2 = g.Film(32, 32, lib=gpu)
+    ok.render(w.camera, w.integrator, f2, 1)
+    assert f2.read()[1].sum() > 0
 
 
 @pytest.mark.parametrize("scene", ["cornell", "displaced", "displaced_env_spheres", "no_lights"])
