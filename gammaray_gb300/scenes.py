@@ -232,6 +232,24 @@ def displaced_sphere(width=1024, height=1024, spp=64, seed=2, bdpt=False, tris=1
                     {"triangles": int(sum(p.num_components() for p in prims if isinstance(p, Mesh)))})
 
 
+def displaced_sphere_lobes(width=64, height=64, spp=1, bdpt=False) -> Workload:
+    """The 102,400-triangle displaced sphere with its seeded materials (a rough glass
+    sphere with clearcoat and sheen, a clearcoated ground with sheen), plus two analytic
+    spheres so that every Disney lobe is on screen: a rough metal (roughness 0.3) and a
+    rough dielectric with full sheen and a glossy clearcoat.  Both float 0.1 above the
+    ground (a contact point would put connection vertices arbitrarily close together)."""
+    w = displaced_sphere(width, height, spp, bdpt=bdpt)
+    D = Material.disney
+    metal = D().base_color((0.9, 0.6, 0.3)).metallic(1.0).roughness(0.3).build()
+    coat = D().base_color((0.2, 0.5, 0.8)).roughness(0.6).sheen(1.0).clearcoat(1.0).clearcoat_gloss(0.8).build()
+    s1, s2 = Sphere(metal, None, 0.4), Sphere(coat, None, 0.35)
+    s1.center = np.array([-1.55, -0.65, 0.9], np.float32)
+    s2.center = np.array([1.5, -0.7, 0.8], np.float32)
+    w.prims = w.prims + [s1, s2]
+    w.name += "_lobes"
+    return w
+
+
 def orbit_camera(rng, width, height, radius=4.6):
     """A random pose on a ring around the origin, looking at it.  The reference's
     camera origin is translate * rotation (core/camera.rs:50-52, row vectors), so the
