@@ -243,7 +243,26 @@ class ServerOptions(C.Structure):
         ("path_capacity", C.c_uint32),
         ("bvh_width", C.c_uint32),
         ("block_size", C.c_uint32),
+        ("policy", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [
+        ("queued", C.c_uint32),
+        ("running", C.c_uint32),
+        ("finished", C.c_uint32),
+        ("engine_jobs", C.c_uint32),
+        ("engine_units", C.c_uint64),
+        ("resets", C.c_uint64),
+        ("film_bytes", C.c_uint64),
+        ("memory_budget_bytes", C.c_uint64),
+    ]
+
+
+SERVE_ARRIVAL_ORDER = 0
+SERVE_SHORTEST_FIRST = 1
 
 
 class Request(C.Structure):
@@ -328,6 +347,7 @@ SIGNATURES = {
     "gr_server_cancel": (C.c_int, [_VP, C.c_uint64]),
     "gr_server_take": (C.c_int, [_VP, C.c_uint64, _PF, _PF]),
     "gr_server_snapshot": (C.c_int, [_VP, C.c_uint64, _PF, _PF, C.POINTER(C.c_uint32)]),
+    "gr_server_get_info": (C.c_int, [_VP, C.POINTER(ServerInfo)]),
 }
 
 

@@ -327,6 +327,7 @@ struct gr_server {
     // Scenes of taken requests that were cancelled while running: their paths may still
     // be queued, so the scene is released once the engine reports all work gathered.
     std::vector<gr_scene*> retired;
+    uint64_t resets = 0;  // times the engine's job and unit tables were cleared at idle
     std::chrono::steady_clock::time_point t0;
     double now_ms() const {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -379,16 +380,21 @@ gr_status schedule(gr_server* s) {
     if (st != GR_OK) return st;
     uint64_t backlog = c.paths_total - c.gcur;
     const uint64_t want = 2ull * s->engine.capacity();
-    // Shortest remaining work first, aged: passes of the request with the fewest samples
-    // left, divided by 1 + (time since submission) / SERVE_AGE_MS, are appended first.
-    // Short requests that arrive behind long ones start within one backlog (about two
-    // pools) of work, and a long request's priority grows as it waits.
+    // Which request's passes go first (gr_server_options.policy):
+    //   arrival order: the oldest request's; a later request's passes are appended only
+    //     when the older ones have nothing left to append within the backlog, so they
+    //     fill the paths the older ones leave free (a FIFO with backfill);
+    //   shortest first: the request with the fewest samples left, divided by
+    //     1 + (time since submission) / SERVE_AGE_MS, so a long request's priority grows
+    //     as it waits.
     const double now = s->now_ms();
+    const bool shortest = s->opts.policy == GR_SERVE_SHORTEST_FIRST;
     std::vector<std::pair<double, ServerRequest*>> order;
     for (auto& r : s->reqs)
         if (r->state == GR_REQUEST_RUNNING && r->appended < r->cap()) {
             const double left = static_cast<double>(r->cap() - r->appended) * r->req.width * r->req.height;
-            order.emplace_back(left / (1.0 + (now - r->submit_ms) / SERVE_AGE_MS), r.get());
+            order.emplace_back(shortest ? left / (1.0 + (now - r->submit_ms) / SERVE_AGE_MS) : r->submit_ms,
+                               r.get());
         }
     std::stable_sort(order.begin(), order.end(),
                      [](const std::pair<double, ServerRequest*>& a, const std::pair<double, ServerRequest*>& b) {
@@ -439,6 +445,27 @@ gr_status half_film_rel_mse(gr_server* s, const ServerRequest& r, float& out) {
     return GR_OK;
 }
 
+// With no request running and every appended unit gathered, no path of any job is left
+// on the device: the scenes of retired requests are released and the engine's job and
+// unit tables are cleared, so a long-running server does not grow them with everything
+// it has served.  Finished requests keep their films (their own buffers) until taken.
+gr_status reset_if_idle(gr_server* s) {
+    if (s->engine.units().empty() && s->engine.jobs().empty()) return GR_OK;
+    for (auto& r : s->reqs)
+        if (r->state == GR_REQUEST_RUNNING) return GR_OK;
+    EngineCtl c;
+    gr_status st = s->engine.read_ctl(c);
+    if (st != GR_OK) return st;
+    if (c.g_lo != c.units_count) return GR_OK;
+    for (gr_scene* sc : s->retired) scene_release(sc);
+    s->retired.clear();
+    st = s->engine.reset();
+    if (st != GR_OK) return st;
+    for (auto& r : s->reqs) r->units.clear();  // indices into the cleared table
+    s->resets += 1;
+    return GR_OK;
+}
+
 // Marks passes gathered (every unit below the engine's g_lo is in its film).
 gr_status progress(gr_server* s) {
     EngineCtl c;
@@ -475,6 +502,10 @@ gr_status gr_server_create(const gr_server_options* o, gr_server** out) {
     }
     std::unique_ptr<gr_server> s(new gr_server());
     if (o) s->opts = *o;
+    if (s->opts.policy != GR_SERVE_ARRIVAL_ORDER && s->opts.policy != GR_SERVE_SHORTEST_FIRST) {
+        set_error("unknown serving policy");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
     EngineConfig cfg;
     // 64 M paths in flight (about 18 GB of queues and path ring): on the serving
     // scenes' requests 16 M -> 32 M -> 64 M measured 1505 -> 1654 -> 1728 Msamples/s.
@@ -560,7 +591,7 @@ gr_status gr_server_step(gr_server* s, double budget_ms) {
         if (st != GR_OK) return st;
         bool any = false;
         for (auto& r : s->reqs) any |= r->state == GR_REQUEST_RUNNING;
-        if (!any) return GR_OK;
+        if (!any) return reset_if_idle(s);
         bool done = false;
         st = s->engine.run(4, done);
         if (st != GR_OK) return st;
@@ -666,6 +697,26 @@ gr_status gr_server_snapshot(gr_server* s, uint64_t id, float* accum, float* wei
     }
     if (passes) *passes = r->passes_done;
     return copy_film(s, *r, accum, weight);
+}
+
+gr_status gr_server_get_info(gr_server* s, gr_server_info* out) {
+    if (!s || !out) {
+        set_error("null argument");
+        return GR_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    std::memset(out, 0, sizeof(*out));
+    for (auto& r : s->reqs) {
+        if (r->state == GR_REQUEST_QUEUED) out->queued += 1;
+        else if (r->state == GR_REQUEST_RUNNING) out->running += 1;
+        else out->finished += 1;
+    }
+    out->engine_jobs = static_cast<uint32_t>(s->engine.jobs().size());
+    out->engine_units = s->engine.units().size();
+    out->resets = s->resets;
+    out->film_bytes = s->used;
+    out->memory_budget_bytes = s->budget;
+    return GR_OK;
 }
 
 gr_status gr_server_take(gr_server* s, uint64_t id, float* accum, float* weight) {

@@ -14,9 +14,11 @@ STATE_NAMES = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"
 
 class Server:
     def __init__(self, lib, memory_budget_bytes: int = 0, max_active: int = 0, path_capacity: int = 0,
-                 bvh_width: int = 0, block_size: int = 0):
+                 bvh_width: int = 0, block_size: int = 0, policy: int = _abi.SERVE_ARRIVAL_ORDER):
+        """policy: _abi.SERVE_ARRIVAL_ORDER (the oldest request first, later ones fill the
+        paths it leaves free) or _abi.SERVE_SHORTEST_FIRST (fewest samples left, aged)."""
         self.lib = lib
-        o = _abi.ServerOptions(memory_budget_bytes, max_active, path_capacity, bvh_width, block_size)
+        o = _abi.ServerOptions(memory_budget_bytes, max_active, path_capacity, bvh_width, block_size, policy)
         h = C.c_void_p()
         lib.call("gr_server_create", C.byref(o), C.byref(h))
         self.handle = h
@@ -74,6 +76,12 @@ class Server:
         passes = C.c_uint32()
         self.lib.call("gr_server_snapshot", self.handle, rid, _abi.fptr(acc), _abi.fptr(wt), C.byref(passes))
         return acc, wt, passes.value
+
+    def info(self) -> _abi.ServerInfo:
+        """gr_server_get_info: requests by state, the engine's table sizes and resets."""
+        i = _abi.ServerInfo()
+        self.lib.call("gr_server_get_info", self.handle, C.byref(i))
+        return i
 
     def run_until_done(self, ids, budget_ms: float = 20.0, max_steps: int = 3000):
         pending = set(ids)

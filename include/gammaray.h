@@ -278,16 +278,23 @@ gr_status gr_render_samples(gr_scene* scene, const gr_camera* camera,
                             uint32_t height, float* samples);
 
 /* A render that allocates nothing, for callers that cannot let a library allocate
- * device memory (an application that owns all GPU memory through its own pool, or a
- * frame loop that cudaMalloc / cudaFree would stall by synchronising the device).
+ * device memory: an application that owns all GPU memory through its own pool (a host
+ * program embedding the renderer under a fixed memory budget), or a frame loop that a
+ * cudaMalloc / cudaFree would stall, since both synchronise the whole device.
  * No counterpart in the reference.  Runs the same path-tracer (or display-colour)
  * passes as gr_render on `stream` (a cudaStream_t, or 0) and accumulates them into
  * `film_dev`, caller-owned device memory of width * height float4 {accum.rgb, weight}.
  * Its scratch is one fixed array inside the library (about 18 MB, held by every GPU
  * that loads the library until exit): at most 131072 pixels per image, larger images
- * are rejected with GR_ERR_INVALID_ARGUMENT.  All calls share that array, so calls
- * that overlap on the GPU race.  The first call on a device resolves the array's
- * address; make it before any stream capture.  Exported by the GPU library only. */
+ * are rejected with GR_ERR_INVALID_ARGUMENT.  All calls share that array and each
+ * call clears the counters it uses, so calls that overlap on the GPU race: serialise
+ * them.  The first call on a device resolves the array's address; make it before any
+ * stream capture.  The call returns once its work on `stream` has finished: it waits
+ * for the stream at the end to read the traversal status, which it reports like
+ * gr_render (GR_ERR_TIMEOUT when a ray exceeds the traversal step budget,
+ * GR_ERR_STACK_OVERFLOW), and with max_depth == 0 (unbounded depth, the reference's
+ * default) it also waits every 4 bounces to see whether any path is left.  The scene
+ * is locked for the duration of the call.  Exported by the GPU library only. */
 gr_status gr_render_static(gr_scene* scene, const gr_camera* camera, const gr_render_params* params,
                            uint32_t width, uint32_t height, float* film_dev, void* stream);
 
@@ -416,13 +423,38 @@ gr_status gr_batch_release(void);
 
 typedef struct gr_server gr_server;
 
+/* Order in which the serving loop hands running requests' passes to the GPU. */
+/* The oldest request's passes first; later requests fill the paths it leaves free, so
+ * none waits behind requests that arrived after it (a FIFO with backfill). */
+#define GR_SERVE_ARRIVAL_ORDER 0u
+/* The request with the fewest samples left first, its priority growing with the time
+ * since submission (shortest remaining work with aging). */
+#define GR_SERVE_SHORTEST_FIRST 1u
+
 typedef struct gr_server_options {
     uint64_t memory_budget_bytes; /* admission limit for films; 0 = 90% of free device memory */
     uint32_t max_active;          /* concurrent renders; 0 = unlimited */
     uint32_t path_capacity;       /* paths in flight; 0 = 64 M (about 18 GB of queues and path state) */
     uint32_t bvh_width;           /* BVH width of the scenes served (2, 4, 8); 0 = 4 */
     uint32_t block_size;          /* extension kernel block size; 0 = 128 */
+    uint32_t policy;              /* GR_SERVE_*; 0 = GR_SERVE_ARRIVAL_ORDER */
+    uint32_t reserved;
 } gr_server_options;
+
+/* What a server holds (no counterpart in the reference). */
+typedef struct gr_server_info {
+    uint32_t queued;          /* requests waiting for admission */
+    uint32_t running;         /* admitted requests still rendering */
+    uint32_t finished;        /* done or cancelled, not yet taken */
+    uint32_t engine_jobs;     /* the engine's job table: one per admitted request since the
+                                 last reset, two when progressive */
+    uint64_t engine_units;    /* the engine's unit table: one per appended pass since the
+                                 last reset (16 bytes each) */
+    uint64_t resets;          /* times both tables were cleared: at a step that finds no
+                                 request running and every appended pass gathered */
+    uint64_t film_bytes;      /* device bytes of the films of admitted requests */
+    uint64_t memory_budget_bytes;
+} gr_server_info;
 
 typedef struct gr_request {
     gr_scene* scene;
@@ -472,6 +504,8 @@ gr_status gr_server_take(gr_server* server, uint64_t id, float* accum, float* we
  * the request to stop there); zeros before admission.  No counterpart in the
  * reference. */
 gr_status gr_server_snapshot(gr_server* server, uint64_t id, float* accum, float* weight, uint32_t* passes);
+/* Counts of what the server holds; see gr_server_info. */
+gr_status gr_server_get_info(gr_server* server, gr_server_info* out);
 
 #ifdef __cplusplus
 }

@@ -606,6 +606,9 @@ gr_status gr_server_cancel(gr_server*, uint64_t) { return fail(GR_ERR_UNSUPPORTE
 gr_status gr_server_snapshot(gr_server*, uint64_t, float*, float*, uint32_t*) {
     return fail(GR_ERR_UNSUPPORTED, "serving is a device feature");
 }
+gr_status gr_server_get_info(gr_server*, gr_server_info*) {
+    return fail(GR_ERR_UNSUPPORTED, "serving is a device feature");
+}
 gr_status gr_server_take(gr_server*, uint64_t, float*, float*) {
     return fail(GR_ERR_UNSUPPORTED, "serving is a device feature");
 }

@@ -29,6 +29,7 @@ STRUCTS = {
     "gr_job": _abi.Job,
     "gr_batch_options": _abi.BatchOptions,
     "gr_server_options": _abi.ServerOptions,
+    "gr_server_info": _abi.ServerInfo,
     "gr_request": _abi.Request,
     "gr_request_status": _abi.RequestStatus,
 }

@@ -283,3 +283,60 @@ def test_server_keeps_a_closed_scene_until_its_requests_let_go(gpu):
     np.testing.assert_array_equal(wt, ref_w)
     np.testing.assert_allclose(acc, ref_acc, rtol=1e-6, atol=1e-7)
     s.close()
+
+
+@pytest.mark.parametrize("policy", [0, 1])
+def test_server_resets_its_tables_at_idle(gpu, policy):
+    # The step that finds nothing running and every appended pass gathered clears the
+    # engine's job and unit tables (in the same gr_server_step that finishes the last
+    # request); a request served after the reset gets the same film as a plain render,
+    # under either scheduling policy.
+    ws = small_workloads(3, seed=21)
+    stages = [g.Stage(w.prims, lib=gpu, environment=w.environment, seed=k) for k, w in enumerate(ws)]
+    s = serve.Server(gpu, path_capacity=1 << 16, policy=policy)
+    ids = [s.submit(stages[k], ws[k].camera, ws[k].integrator, ws[k].width, ws[k].height, 3) for k in range(2)]
+    # 256 passes of 3072 pixels need at least 12 fills of the 64 k-path pool, more than
+    # the 8 iterations of one step: the request is still running after it.
+    w2 = ws[2]
+    long_id = s.submit(stages[2], w2.camera, w2.integrator, 64, 48, 256)
+    s.step(0.0)
+    during = s.info()
+    assert during.running >= 1 and during.engine_jobs == 3 and during.engine_units > 0 and during.resets == 0
+    s.run_until_done(ids + [long_id])
+    after = s.info()
+    assert after.engine_jobs == 0 and after.engine_units == 0 and after.resets == 1
+    assert after.finished == 3 and after.running == 0  # finished films stay until taken
+    for rid in ids + [long_id]:
+        s.take(rid)
+    w = ws[1]
+    rid = s.submit(stages[1], w.camera, w.integrator, w.width, w.height, 4)
+    s.run_until_done([rid])
+    assert s.info().resets == 2
+    acc, wt = s.take(rid)
+    ref = g.Film(w.width, w.height, lib=gpu)
+    stages[1].render(w.camera, w.integrator, ref, 4)
+    racc, rwt = ref.read()
+    np.testing.assert_array_equal(wt, rwt)
+    np.testing.assert_allclose(acc, racc, rtol=1e-6, atol=1e-7)
+
+
+def test_progressive_estimate_matches_the_actual_error(gpu):
+    # A progressive request stops at the first checkpoint whose half-film estimate of its
+    # relMSE is at most the target.  The estimate is checked against the relMSE its image
+    # actually has against a converged render of the same view (65536 spp, other random
+    # streams, whose own noise is about 1.6e-5 here): within a factor of 1.5.
+    w = scenes.cornell_spheres(64, 64, 1)
+    st = g.Stage(w.prims, lib=gpu, seed=3)
+    s = serve.Server(gpu, path_capacity=1 << 20)
+    rid = s.submit(st, w.camera, w.integrator, 64, 64, 4096, target_rel_mse=2e-3)
+    s.run_until_done([rid])
+    stat = s.poll(rid)
+    acc, wt = s.take(rid)
+    assert stat.state == 2 and 0 < stat.rel_mse <= 2e-3 and stat.passes_done < 4096
+    img = acc / wt[..., None]
+    conv_stage = g.Stage(w.prims, lib=gpu, seed=99)
+    conv = g.Film(64, 64, lib=gpu)
+    conv_stage.render(w.camera, w.integrator, conv, 65536)
+    ref = conv.resolve().astype(np.float64)
+    actual = float(np.mean((img - ref) ** 2) / np.mean(ref ** 2))
+    assert actual / 1.5 <= stat.rel_mse <= actual * 1.5, (stat.passes_done, stat.rel_mse, actual)
