@@ -29,9 +29,13 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-# DRAM bytes per extension ray of k_extend, measured with ncu on a 4-spp render of the
-# bench workload (profiles/extend_pt_displaced_sphere_1024.md).
+# DRAM bytes (read + written) per extension ray of k_extend: ncu's dram__bytes_read.sum +
+# dram__bytes_write.sum summed over every k_extend launch of a 4-spp render of this
+# workload (bench.py --profile-case --spp 4; its 4 M-ray queues exceed L2 as the timed
+# renders' do), divided by that render's extension rays.  Re-measured whenever k_extend
+# changes; EXTEND_DRAM_CAPTURE says which capture the figure comes from.
 EXTEND_DRAM_BYTES_PER_RAY = 46.4
+EXTEND_DRAM_CAPTURE = "ncu, 4-spp render of the bench workload, all 12 k_extend launches"
 sys.path.insert(0, ROOT)
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -196,17 +200,21 @@ def percentiles(xs):
 
 def run_batched(lib):
     """Config 4: 64 seeded scenes (1k-200k triangles, 0-8 spheres, random resolution, spp
-    4-64, depth 4-12) rendered (a) one gr_render per image and (b) in one batch."""
+    4-64, depth 4-12) rendered (a) one gr_render per image and (b) in one batch, with the
+    BVH width, path capacity and block size picked by the autotuner.  Then the same
+    comparison per resolution class (a batch of that class's images against their
+    per-image renders), which shows where the batch gains and where it cannot."""
     import gammaray_gb300 as g
     from gammaray_gb300 import batch, scenes
 
     ws = scenes.batch_scenes(64)
-    stages = [g.Stage(w.prims, lib=lib, environment=w.environment, seed=k) for k, w in enumerate(ws)]
+    width, width_rates, opt, stages = batch.autotune_workloads(ws, lib, seeds=list(range(len(ws))))
     samples = sum(w.width * w.height * w.spp for w in ws)
 
-    def jobs():
-        return [batch.Job(st, w.camera, w.integrator, g.Film(w.width, w.height, lib=lib), w.spp)
-                for st, w in zip(stages, ws)]
+    def jobs(idx=None):
+        idx = range(len(ws)) if idx is None else idx
+        return [batch.Job(stages[k], ws[k].camera, ws[k].integrator, g.Film(ws[k].width, ws[k].height, lib=lib),
+                          ws[k].spp) for k in idx]
 
     # plain per-image path (warm once, then timed)
     warm = jobs()
@@ -219,7 +227,6 @@ def run_batched(lib):
     t0 = time.perf_counter()
     batch.render_per_pass(qj, lib)
     per_pass_wall = time.perf_counter() - t0
-    opt = batch.autotune(jobs(), lib)
     batch.render_batch(jobs()[:8], lib, opt.path_capacity, opt.block_size)  # warm
     bj = jobs()
     t0 = time.perf_counter()
@@ -229,23 +236,50 @@ def run_batched(lib):
     a = bj[0].film.read()[0]
     b = pj[0].film.read()[0]
     same = bool(np.allclose(a, b, rtol=1e-6, atol=1e-7))
+    # Per resolution class, device time: the class's images per image, then as one batch.
+    classes = {}
+    for res in sorted({(w.width, w.height) for w in ws}):
+        idx = [k for k, w in enumerate(ws) if (w.width, w.height) == res]
+        n = sum(ws[k].width * ws[k].height * ws[k].spp for k in idx)
+        per_image_ms = batch.render_individually(jobs(idx), lib)
+        bs = batch.render_batch(jobs(idx), lib, opt.path_capacity, opt.block_size)
+        classes[f"{res[0]}x{res[1]}"] = {
+            "images": len(idx), "samples": n, "share_of_samples": n / samples,
+            "per_image_ms": per_image_ms, "batch_ms": bs.device_ms,
+            "per_image_msamples_per_s": n / (per_image_ms * 1e-3) / 1e6,
+            "batch_msamples_per_s": n / (bs.device_ms * 1e-3) / 1e6, "speedup": per_image_ms / bs.device_ms}
+    # The classes' batched times added up, against their per-image times; and the
+    # ceiling of any batching: every sample at the saturated per-image rate (the best
+    # class's, where one image fills the GPU), so the batch's time is at least its
+    # samples at that rate.
+    t_plain = sum(c["per_image_ms"] for c in classes.values())
+    t_batched = sum(c["batch_ms"] for c in classes.values())
+    sat_class = max(classes, key=lambda k: classes[k]["per_image_msamples_per_s"])
+    sat_rate = classes[sat_class]["per_image_msamples_per_s"]
+    ceiling = t_plain / (samples / sat_rate * 1e-3)
     return {"workload": "batch_64_scenes", "samples": samples,
             "msamples_per_s": samples / batch_wall / 1e6, "msamples_per_s_device": samples / (st.device_ms * 1e-3) / 1e6,
             "plain_msamples_per_s": samples / plain_wall / 1e6,
             "plain_msamples_per_s_device": samples / (plain_dev * 1e-3) / 1e6,
-            "speedup_vs_plain": plain_wall / batch_wall, "mrays_per_s": st.extension_rays / batch_wall / 1e6,
+            "speedup_vs_plain": plain_wall / batch_wall, "speedup_vs_plain_device": plain_dev / st.device_ms,
+            "mrays_per_s": st.extension_rays / batch_wall / 1e6,
             "plain_per_pass_msamples_per_s": samples / per_pass_wall / 1e6,
             "speedup_vs_per_pass": per_pass_wall / batch_wall,
-            "autotuned": {"path_capacity": opt.path_capacity, "block_size": opt.block_size},
-            "films_equal_plain": same}
+            "autotuned": {"bvh_width": width, "width_trial_msamples_per_s": {str(k): v for k, v in width_rates.items()},
+                          "path_capacity": opt.path_capacity, "block_size": opt.block_size},
+            "per_class": classes, "per_class_speedup_combined": t_plain / t_batched,
+            "speedup_ceiling_at_saturated_rate": ceiling,
+            "saturated_class": sat_class, "saturated_msamples_per_s": sat_rate, "films_equal_plain": same}
 
 
-def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3):
+def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3, other_policy=True):
     """Config 5: 16 resident scenes (10k-2M triangles); Poisson arrivals; random pose,
     resolution 256^2..1920x1080, spp 1-256, depth 4-16.  Served by the continuous-
-    batching loop vs a FIFO timeline of one gr_render per request on the same GPU."""
+    batching loop (arrival order with backfill, the default policy) vs a FIFO timeline of
+    one gr_render per request on the same GPU; then the same requests under the
+    shortest-remaining-work policy."""
     import gammaray_gb300 as g
-    from gammaray_gb300 import scenes, serve
+    from gammaray_gb300 import _abi, scenes, serve
 
     rng = np.random.default_rng(seed)
     scs = scenes.serving_scenes(16)
@@ -274,34 +308,43 @@ def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3):
         finish = start + d
         lat_plain.append((finish - r["arrival"]) * 1e3)
     plain_span = finish - reqs[0]["arrival"]
-    # served
-    srv = serve.Server(lib, max_active=16)
-    ids = {}
-    t0 = time.perf_counter()
-    nxt = 0
-    while nxt < len(reqs) or any(srv.poll(i).state < 2 for i in ids.values()):
-        now = time.perf_counter() - t0
-        while nxt < len(reqs) and reqs[nxt]["arrival"] <= now:
-            r = reqs[nxt]
-            ids[nxt] = srv.submit(stages[r["scene"]], r["cam"], g.PathTracerIntegrator(max_depth=r["depth"]),
-                                  r["res"][0], r["res"][1], r["spp"])
-            nxt += 1
-        if nxt < len(reqs) and not any(srv.poll(i).state < 2 for i in ids.values()):
-            time.sleep(max(0.0, reqs[nxt]["arrival"] - now))
-            continue
-        srv.step(2.0)
-    span = time.perf_counter() - t0 - reqs[0]["arrival"]
-    lat = []
-    for k, rid in ids.items():
-        st = srv.poll(rid)
-        lat.append(st.finish_ms - st.submit_ms)
-        srv.take(rid)
-    srv.close()
+    def serve_all(policy):
+        srv = serve.Server(lib, max_active=16, policy=policy)
+        ids = {}
+        t0 = time.perf_counter()
+        nxt = 0
+        while nxt < len(reqs) or any(srv.poll(i).state < 2 for i in ids.values()):
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and reqs[nxt]["arrival"] <= now:
+                r = reqs[nxt]
+                ids[nxt] = srv.submit(stages[r["scene"]], r["cam"], g.PathTracerIntegrator(max_depth=r["depth"]),
+                                      r["res"][0], r["res"][1], r["spp"])
+                nxt += 1
+            if nxt < len(reqs) and not any(srv.poll(i).state < 2 for i in ids.values()):
+                time.sleep(max(0.0, reqs[nxt]["arrival"] - now))
+                continue
+            srv.step(2.0)
+        span = time.perf_counter() - t0 - reqs[0]["arrival"]
+        lat = []
+        for k, rid in ids.items():
+            st = srv.poll(rid)
+            lat.append(st.finish_ms - st.submit_ms)
+            srv.take(rid)
+        srv.close()
+        return span, lat
+
+    span, lat = serve_all(_abi.SERVE_ARRIVAL_ORDER)
     out = {"workload": "serve_16_scenes", "requests": n_req, "rate_per_s": rate, "samples": samples,
+           "policy": "arrival order with backfill",
            "msamples_per_s": samples / span / 1e6, "latency_ms": percentiles(lat),
            "plain_fifo_msamples_per_s": samples / plain_span / 1e6, "plain_fifo_latency_ms": percentiles(lat_plain),
            "plain_busy_msamples_per_s": samples / sum(dur) / 1e6,
-           "speedup_vs_plain_fifo": plain_span / span}
+           "speedup_vs_plain_fifo": plain_span / span,
+           "requests_slower_than_fifo": int(sum(a > b for a, b in zip(lat, lat_plain)))}
+    if other_policy:
+        span2, lat2 = serve_all(_abi.SERVE_SHORTEST_FIRST)
+        out["shortest_first"] = {"msamples_per_s": samples / span2 / 1e6, "latency_ms": percentiles(lat2),
+                                 "speedup_vs_plain_fifo": plain_span / span2}
     if target_rel_mse > 0:
         out["progressive"] = run_progressive(lib, g, serve, stages, reqs, target_rel_mse)
     return out
@@ -491,13 +534,11 @@ def run_ours(args, rank, world, local):
                 "extend_share_of_device_time": ext_ms / total_ms if total_ms else None,
                 "shade_share_of_device_time": shade_ms / total_ms if total_ms else None,
                 "extend_ms_per_launch": ext_ms / max(1, ext_launch)}
-    # DRAM traffic of k_extend per ray, from one ncu capture (dram__bytes_read.sum +
-    # dram__bytes_write.sum over every extend launch of a 4-spp render of this workload,
-    # whose 4 M-ray queues exceed L2; profiles/extend_pt_displaced_sphere_1024.md),
-    # scaled to the average launch of the timed renders.
+    # DRAM traffic of k_extend per launch: the captured bytes per ray (see
+    # EXTEND_DRAM_BYTES_PER_RAY) times the rays of an average timed launch.
     roofline["traffic"] = EXTEND_DRAM_BYTES_PER_RAY * rays / max(1, ext_launch)
-    roofline["traffic_source"] = ("ncu dram bytes of all extend launches of a 4-spp render "
-                                  f"({EXTEND_DRAM_BYTES_PER_RAY} B/ray) x rays per timed launch")
+    roofline["traffic_source"] = (f"{EXTEND_DRAM_CAPTURE}: {EXTEND_DRAM_BYTES_PER_RAY} B/ray, "
+                                  "x rays per timed launch")
 
     batched = served = bdpt = None
     if rank == 0 and not args.no_bdpt:

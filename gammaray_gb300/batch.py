@@ -1,10 +1,12 @@
 """Batched rendering: many scenes, cameras and films in one multi-job wavefront.
 
 `render_batch(jobs)` calls gr_render_batch: every path-tracer job shares one pool of
-path slots, refilled as paths finish, under a captured CUDA graph.  `autotune(jobs)` picks
-the pool capacity and the extension block size by timing short trials
-(gr_batch_autotune); `choose_bvh_width` picks the BVH width by timing a trial batch of
-the same scenes built at widths 2, 4 and 8.
+path slots, refilled as paths finish, under a captured CUDA graph.  The autotuner picks
+all three of its settings by timing short trials:
+  - `choose_bvh_width` the BVH width: the scenes are built at widths 2, 4 and 8 (a
+    scene's wide BVH is fixed when it is built, so this needs the prims);
+  - `autotune(jobs)` the pool capacity and the extension block size (gr_batch_autotune);
+  - `autotune_workloads` both in turn, returning the width and the options.
 """
 from __future__ import annotations
 
@@ -86,6 +88,20 @@ def render_per_pass(jobs, lib) -> float:
             lib.call("gr_render", j.stage.handle, C.byref(cam), C.byref(p), j.film.handle)
             total += j.stage.last_stats().device_ms
     return total
+
+
+def autotune_workloads(workloads, lib, widths=(2, 4, 8), seeds=None):
+    """The width trial, then gr_batch_autotune on the scenes built at the chosen width.
+    Returns (width, {width: trial Msamples/s}, options, stages at that width)."""
+    width, rates = choose_bvh_width(workloads, lib, widths)
+    stages = [Stage(w.prims, lib=lib, environment=w.environment, bvh_width=width,
+                    seed=(seeds[k] if seeds is not None else 0)) for k, w in enumerate(workloads)]
+    jobs = [Job(st, w.camera, w.integrator, Film(w.width, w.height, lib=lib), w.spp)
+            for st, w in zip(stages, workloads)]
+    opt = autotune(jobs, lib)
+    for j in jobs:
+        j.film.close()
+    return width, rates, opt, stages
 
 
 def choose_bvh_width(workloads, lib, widths=(2, 4, 8), trial_spp: int = 2):
