@@ -575,6 +575,7 @@ gr_status gr_trace_rays(gr_scene* s, const float* rays, uint64_t n, gr_hit* hits
     int herr = 0;
     GR_CUDA_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     GR_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (herr == 2) return fail(GR_ERR_TIMEOUT, "traversal step budget exceeded");
     if (herr) return fail(GR_ERR_STACK_OVERFLOW, "traversal stack bound exceeded");
     return GR_OK;
 }
@@ -622,6 +623,7 @@ gr_status gr_visibility(gr_scene* s, const float* pairs, uint64_t n, uint8_t* vi
     int herr = 0;
     GR_CUDA_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     GR_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (herr == 2) return fail(GR_ERR_TIMEOUT, "traversal step budget exceeded");
     if (herr) return fail(GR_ERR_STACK_OVERFLOW, "traversal stack bound exceeded");
     return GR_OK;
 }

@@ -696,8 +696,8 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_shadow(DeviceScene s, const uint
                                                        float4* __restrict__ entries, float4* __restrict__ lt,
                                                        float3 cam, int* err, unsigned long long* shadow_rays) {
     extern __shared__ unsigned char smem[];
-    int32_t* sref = reinterpret_cast<int32_t*>(smem);
-    float* stt = reinterpret_cast<float*>(smem + sizeof(int32_t) * s.stack_depth * blockDim.x);
+    int2 spill[MAX_STACK - SMEM_STACK];
+    const StackView stk = thread_stack(smem, spill);
     const uint32_t n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(shadow_rays, static_cast<unsigned long long>(n));
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
@@ -719,8 +719,7 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_shadow(DeviceScene s, const uint
             V3 d = normalized(b - a);
             V3 o = nudge(a, d);
             float target = magnitude(b - o);
-            TraceResult r = trace_ray<W, true>(s, o, d, target - 1e-3f, sref + threadIdx.x, stt + threadIdx.x,
-                                               blockDim.x, err);
+            TraceResult r = trace_ray<W, true>(s, o, d, target - 1e-3f, stk, err);
             visible = r.k < 0;
         }
         (e.w == 1 ? lt : entries)[e.x].w = visible ? E_VISIBLE : E_OCCLUDED;
@@ -789,7 +788,7 @@ template <int W>
 gr_status shadow_launch(const DeviceScene& s, uint32_t cap, const uint32_t* count, const uint4* q, const float4* v0,
                         float4* entries, float4* lt, float3 cam, int* err, unsigned long long* shadow_rays,
                         cudaStream_t st) {
-    size_t smem = stack_smem_bytes(s.stack_depth, BLOCK);
+    size_t smem = step_stack_smem_bytes(BLOCK);
     GR_CUDA_TRY(
         cudaFuncSetAttribute(k_bdpt_shadow<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int grid = resident_grid(k_bdpt_shadow<W>, smem, cap);
@@ -904,7 +903,7 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         for (uint32_t depth = 0; depth < max_len; ++depth) {
             int cur = depth & 1, nxt = cur ^ 1;
             gr_status s1 = extend_any(job.scene, false, p.nslots, cnt + cur, ps.q_o[cur].as<float4>(),
-                                      ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(), err, rays, st);
+                                      ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(), err, rays, cnt + CNT_FETCH, st);
             if (s1 != GR_OK) return s1;
             GR_CUDA_TRY(cudaGetLastError());
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));

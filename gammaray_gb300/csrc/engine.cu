@@ -127,6 +127,7 @@ __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const 
     c->gcur += nf;
     c->done = c->g_lo == c->units_count ? 1u : 0u;
     c->iter += 1;
+    c->fetch = 0;  // the extension kernel of this iteration starts handing out rays at 0
 }
 
 // A unit's samples in their ring slots.
@@ -210,31 +211,74 @@ __global__ void __launch_bounds__(BS) k_eng_extend(EngineCtl* c, int cur, const 
                                                    const float4* __restrict__ q_o, const float4* __restrict__ q_d,
                                                    float4* __restrict__ q_hit) {
     extern __shared__ unsigned char smem[];
-    int32_t* sref = reinterpret_cast<int32_t*>(smem);
-    float* stt = reinterpret_cast<float*>(smem + sizeof(int32_t) * SMEM_STACK * blockDim.x);
     int2 spill[MAX_STACK - SMEM_STACK];
-    StackView stk{sref + threadIdx.x, stt + threadIdx.x, static_cast<int>(blockDim.x), spill};
+    const StackView stk = thread_stack(smem, spill);
     const uint32_t n = c->q[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c->rays, static_cast<unsigned long long>(n));
     auto trace = [&](uint32_t q) {
         float4 o4 = q_o[q], d4 = q_d[q];
         const DeviceScene& s = jobs[__float_as_uint(o4.w)].scene;
-        TravState t;
-        trav_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX);
-        const uint32_t budget = s.step_budget;
-        uint32_t steps = 0;
-        while (!trav_step<W, false, false>(s, t, stk, &c->err, nullptr)) {
-            if (++steps > budget) {
-                atomicExch(&c->err, 2);
-                t.hit = -1;
-                break;
-            }
-        }
-        q_hit[q] = make_float4(t.closest, __int_as_float(t.hit), t.hu, t.hv);
+        TraceResult r = trace_ray<W, false>(s, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX, stk, &c->err);
+        q_hit[q] = make_float4(r.t, __int_as_float(r.k), r.u, r.v);
     };
     // One ray per thread, grid-stride: grouping the engine's queue by direction (as
     // k_extend does) measured slower here (1264 -> 1207 Msamples/s on the batch).
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) trace(q);
+}
+
+// Refilling form of the engine's extension (GR_EXTEND_REFILL = k > 0), as k_extend_refill
+// in wavefront.cuh: a warp hands its idle lanes new rays from c->fetch (zeroed by the
+// plan) once at least k are idle; each lane keeps its ray's scene.  Every warp intrinsic
+// runs at warp-uniform control flow, and the loop ends on a ballot once no ray is left.
+template <int W, int BS>
+__global__ void __launch_bounds__(BS) k_eng_extend_refill(EngineCtl* c, int cur, const DevJob* __restrict__ jobs,
+                                                          const float4* __restrict__ q_o,
+                                                          const float4* __restrict__ q_d, float4* __restrict__ q_hit) {
+    extern __shared__ unsigned char smem[];
+    int2 spill[MAX_STACK - SMEM_STACK];
+    const StackView stk = thread_stack(smem, spill);
+    const uint32_t n = c->q[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c->rays, static_cast<unsigned long long>(n));
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned below = (1u << lane) - 1u;
+    TravState t;
+    const DeviceScene* s = nullptr;
+    uint32_t q = 0, steps = 0, budget = 0;
+    bool busy = false, exhausted = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !busy);
+        if (!exhausted && __popc(idle) >= (GR_EXTEND_REFILL > 32 ? 32 : GR_EXTEND_REFILL)) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&c->fetch, static_cast<uint32_t>(__popc(idle)));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            exhausted = static_cast<uint64_t>(base) + __popc(idle) >= n;
+            if (!busy) {
+                const uint32_t mine = base + __popc(idle & below);
+                if (mine < n) {
+                    float4 o4 = q_o[mine], d4 = q_d[mine];
+                    s = &jobs[__float_as_uint(o4.w)].scene;
+                    budget = s->step_budget;
+                    trav_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX);
+                    q = mine;
+                    steps = 0;
+                    busy = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, busy) == 0u) break;
+        if (busy) {
+            bool done = trav_step<W, false, false>(*s, t, stk, &c->err, nullptr);
+            if (!done && ++steps > budget) {
+                atomicExch(&c->err, 2);
+                t.hit = -1;
+                done = true;
+            }
+            if (done) {
+                q_hit[q] = make_float4(t.closest, __int_as_float(t.hit), t.hu, t.hv);
+                busy = false;
+            }
+        }
+    }
 }
 
 __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
@@ -344,7 +388,7 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
 }
 
 int grid_for(const void* kernel, int block, size_t smem, uint32_t n) {
-    static int sm = device_sm_count();
+    const int sm = device_sm_count();  // of the current device, asked at each launch
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
@@ -356,8 +400,13 @@ template <int W, int BS>
 gr_status launch_extend(EngineCtl* c, int cur, const DevJob* jobs, const float4* qo, const float4* qd, float4* qh,
                         uint32_t cap, cudaStream_t st) {
     size_t smem = step_stack_smem_bytes(BS);
-    int grid = grid_for(reinterpret_cast<const void*>(k_eng_extend<W, BS>), BS, smem, cap);
-    k_eng_extend<W, BS><<<grid, BS, smem, st>>>(c, cur, jobs, qo, qd, qh);
+    if (GR_EXTEND_REFILL > 0) {
+        int grid = grid_for(reinterpret_cast<const void*>(k_eng_extend_refill<W, BS>), BS, smem, cap);
+        k_eng_extend_refill<W, BS><<<grid, BS, smem, st>>>(c, cur, jobs, qo, qd, qh);
+    } else {
+        int grid = grid_for(reinterpret_cast<const void*>(k_eng_extend<W, BS>), BS, smem, cap);
+        k_eng_extend<W, BS><<<grid, BS, smem, st>>>(c, cur, jobs, qo, qd, qh);
+    }
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }

@@ -63,6 +63,7 @@ struct EngineCtl {
     uint32_t done;
     int32_t err;
     uint32_t iter;
+    uint32_t fetch;  // rays handed out by the refilling extension kernel this iteration
     uint32_t gather_units[GATHER_MAX];      // unit indices, each job's units contiguous and in pass order
     uint32_t gather_group_first[GATHER_MAX];  // per group: first entry in gather_units
     uint32_t gather_group_count[GATHER_MAX];

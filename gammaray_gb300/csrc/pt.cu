@@ -275,8 +275,9 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             int cur = depth & 1, nxt = cur ^ 1;
             int e0 = -1, e1 = -1;
             if (timed) GR_TRY_S(mark(e0));
-            gr_status s1 = extend_any(job.scene, (rp.flags & GR_RENDER_COUNT_TRAVERSAL) != 0, n, cnt + cur, ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
-                                      ps.q_hit.as<float4>(), err, rays, st);
+            gr_status s1 = extend_any(job.scene, (rp.flags & GR_RENDER_COUNT_TRAVERSAL) != 0, n, cnt + cur,
+                                      ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(), err,
+                                      rays, cnt + CNT_FETCH, st);
             if (s1 != GR_OK) return s1;
             GR_CUDA_TRY(cudaGetLastError());
             ++launches;
@@ -516,7 +517,8 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
         for (uint32_t depth = 0;; ++depth) {
             if (p.max_depth && depth >= p.max_depth) break;
             int cur = depth & 1, nxt = cur ^ 1;
-            GR_TRY_S(extend_any(sc->dev, false, n, cnt + cur, q_o[cur], q_d[cur], q_hit, err, rays, st));
+            GR_TRY_S(extend_any(sc->dev, false, n, cnt + cur, q_o[cur], q_d[cur], q_hit, err, rays, cnt + CNT_FETCH,
+                                st));
             GR_CUDA_TRY(cudaGetLastError());
             if (display) {
                 int grid = resident_grid(k_shade_display, 0, n);

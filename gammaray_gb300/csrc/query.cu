@@ -33,15 +33,15 @@ __global__ void __launch_bounds__(QUERY_BLOCK) k_trace(DeviceScene s, const floa
                                                        gr_hit* __restrict__ hits, const float* __restrict__ tmax,
                                                        int* err) {
     extern __shared__ unsigned char smem[];
-    int32_t* sref = reinterpret_cast<int32_t*>(smem);
-    float* st = reinterpret_cast<float*>(smem + sizeof(int32_t) * s.stack_depth * blockDim.x);
+    int2 spill[MAX_STACK - SMEM_STACK];
+    const StackView stk = thread_stack(smem, spill);
     uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* r = rays + 6 * i;
     V3 o = V3{r[0], r[1], r[2]};
     V3 d = V3{r[3], r[4], r[5]};
     float tm = tmax ? tmax[i] : FLT_MAX;
-    TraceResult res = trace_ray<W, ANY>(s, o, d, tm, sref + threadIdx.x, st + threadIdx.x, blockDim.x, err);
+    TraceResult res = trace_ray<W, ANY>(s, o, d, tm, stk, err);
     write_hit(s, hits + i, res);
 }
 
@@ -74,8 +74,8 @@ template <int W>
 __global__ void __launch_bounds__(QUERY_BLOCK) k_visibility(DeviceScene s, const float* __restrict__ pairs,
                                                             uint64_t n, uint8_t* __restrict__ vis, int* err) {
     extern __shared__ unsigned char smem[];
-    int32_t* sref = reinterpret_cast<int32_t*>(smem);
-    float* st = reinterpret_cast<float*>(smem + sizeof(int32_t) * s.stack_depth * blockDim.x);
+    int2 spill[MAX_STACK - SMEM_STACK];
+    const StackView stk = thread_stack(smem, spill);
     uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* p = pairs + 6 * i;
@@ -90,8 +90,7 @@ __global__ void __launch_bounds__(QUERY_BLOCK) k_visibility(DeviceScene s, const
     V3 d = normalized(b - a);
     V3 o = nudge(a, d);
     float target = magnitude(b - o);
-    TraceResult r = trace_ray<W, true>(s, o, d, target - 1e-3f, sref + threadIdx.x, st + threadIdx.x, blockDim.x,
-                                       err);
+    TraceResult r = trace_ray<W, true>(s, o, d, target - 1e-3f, stk, err);
     vis[i] = r.k < 0 ? 1 : 0;
 }
 
@@ -172,7 +171,7 @@ unsigned blocks_for(uint64_t n, int b) { return static_cast<unsigned>((n + b - 1
 template <int W>
 gr_status trace_w(const DeviceScene& s, const float* rays, uint64_t n, gr_hit* hits, bool any, const float* tmax,
                   int* err, cudaStream_t st) {
-    size_t smem = stack_smem_bytes(s.stack_depth, QUERY_BLOCK);
+    size_t smem = step_stack_smem_bytes(QUERY_BLOCK);
     if (any) {
         GR_CUDA_TRY(cudaFuncSetAttribute(k_trace<W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
@@ -188,7 +187,7 @@ gr_status trace_w(const DeviceScene& s, const float* rays, uint64_t n, gr_hit* h
 
 template <int W>
 gr_status vis_w(const DeviceScene& s, const float* pairs, uint64_t n, uint8_t* vis, int* err, cudaStream_t st) {
-    size_t smem = stack_smem_bytes(s.stack_depth, QUERY_BLOCK);
+    size_t smem = step_stack_smem_bytes(QUERY_BLOCK);
     GR_CUDA_TRY(
         cudaFuncSetAttribute(k_visibility<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     k_visibility<W><<<blocks_for(n, QUERY_BLOCK), QUERY_BLOCK, smem, st>>>(s, pairs, n, vis, err);

@@ -102,6 +102,7 @@ constexpr int CNT_RAYS = 4;    // 64-bit counter at index 4..5
 constexpr int CNT_SHADOW = 6;  // 64-bit counter at index 6..7
 constexpr int CNT_NODES = 8;   // 64-bit: BVH nodes visited (GR_RENDER_COUNT_TRAVERSAL)
 constexpr int CNT_PRIMS = 10;  // 64-bit: primitives tested
+constexpr int CNT_FETCH = 12;  // rays handed out by the refilling extension kernel (per launch)
 constexpr int NUM_COUNTERS = 16;
 
 struct SceneBuffers {

@@ -5,8 +5,11 @@
 // every child box is slab-tested (far distances inflated by 1 + 2 gamma(3) as in
 // core/bbox.rs:78-113), the hit children are ordered near-to-far by a sorting network
 // on (distance | slot) keys, and the farther ones go on a per-thread stack of
-// (child, entry distance) pairs kept in shared memory, column `threadIdx.x`.  Popped
-// entries whose entry distance is no longer below the closest hit are skipped.
+// (child, entry distance) pairs: the first SMEM_STACK entries in shared memory, column
+// `threadIdx.x`, deeper ones in a local array.  Popped entries whose entry distance is
+// no longer below the closest hit are skipped.  Every traversal (closest hit, shadow
+// rays, query kernels) runs the step functions below; visit_node and visit_leaf are the
+// only node and leaf tests.
 // Leaves hold up to 16 consecutive primitive records.  The primitive tests are the
 // reference's Moller-Trumbore (geom/mesh.rs:270-308) and sphere quadratic
 // (geom/sphere.rs:70-101) with the same operation order, so a hit distance is
@@ -85,109 +88,6 @@ GR_D void sort_keys(uint32_t (&k)[N]) {
     }
 }
 
-// Traces one ray.  ANY_HIT: stop at the first hit closer than t_max (shadow rays).
-// `stk_ref` / `stk_t` point at this thread's column of the shared stack (stride =
-// blockDim.x).  Sets *err = 1 if the stack bound is exceeded (cannot happen when
-// `stack_depth` comes from the build).
-// With COUNT, `counts[0]` / `counts[1]` accumulate nodes visited / primitives tested.
-template <int W, bool ANY_HIT, bool COUNT = false>
-GR_D TraceResult trace_ray(const DeviceScene& s, V3 o, V3 d, float t_max, int32_t* stk_ref, float* stk_t,
-                           int stride, int* err, uint32_t* counts = nullptr) {
-    const float inflate = 1.0f + 2.0f * gamma_n(3.0f);
-    V3 inv = V3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-    const bool nx = d.x < 0.0f, ny = d.y < 0.0f, nz = d.z < 0.0f;
-    TraceResult res{t_max, -1, 0.0f, 0.0f};
-    float closest = t_max;
-    int sp = 0;
-    int32_t ref = 0;  // root node
-    const int cap = static_cast<int>(s.stack_depth);
-    for (;;) {
-        if (ref >= 0) {
-            if (COUNT) counts[0] += 1;
-            const float4* nb = s.nodes + static_cast<size_t>(ref) * (2 * W);
-            float f[8 * W];
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) {
-                float4 x = __ldg(nb + q);
-                f[4 * q] = x.x;
-                f[4 * q + 1] = x.y;
-                f[4 * q + 2] = x.z;
-                f[4 * q + 3] = x.w;
-            }
-            uint32_t key[W];
-            int h = 0;
-#pragma unroll
-            for (int j = 0; j < W; ++j) {
-                float lx = f[0 * W + j], ly = f[1 * W + j], lz = f[2 * W + j];
-                float hx = f[3 * W + j], hy = f[4 * W + j], hz = f[5 * W + j];
-                float t0x = ((nx ? hx : lx) - o.x) * inv.x;
-                float t1x = ((nx ? lx : hx) - o.x) * inv.x;
-                float t0y = ((ny ? hy : ly) - o.y) * inv.y;
-                float t1y = ((ny ? ly : hy) - o.y) * inv.y;
-                float t0z = ((nz ? hz : lz) - o.z) * inv.z;
-                float t1z = ((nz ? lz : hz) - o.z) * inv.z;
-                float tmin = fmaxf(fmaxf(t0x, t0y), t0z);
-                float tmax = fminf(fminf(t1x, t1y), t1z) * inflate;
-                bool hit = tmin <= tmax && tmin < closest && tmax > 0.0f;
-                float te = fmaxf(tmin, 0.0f);
-                key[j] = hit ? ((__float_as_uint(te) & ~7u) | static_cast<uint32_t>(j)) : 0xFFFFFFFFu;
-                h += hit ? 1 : 0;
-            }
-            if (h > 0) {
-                sort_keys<W>(key);
-                if (sp + h - 1 > cap) {
-                    *err = 1;
-                    return TraceResult{t_max, -1, 0.0f, 0.0f};
-                }
-#pragma unroll
-                for (int j = W - 1; j >= 1; --j) {
-                    if (j < h) {
-                        stk_ref[sp * stride] = select_child<W>(f, key[j] & 7u);
-                        stk_t[sp * stride] = __uint_as_float(key[j] & ~7u);
-                        ++sp;
-                    }
-                }
-                ref = select_child<W>(f, key[0] & 7u);
-                continue;
-            }
-        } else {
-            uint32_t enc = ~static_cast<uint32_t>(ref);
-            uint32_t first = enc >> LEAF_COUNT_BITS;
-            uint32_t count = (enc & (MAX_LEAF_PRIMS - 1)) + 1;
-            if (COUNT) counts[1] += count;
-            for (uint32_t k = first; k < first + count; ++k) {
-                const float4* pr = s.prims + 3 * static_cast<size_t>(k);
-                float4 p0 = __ldg(pr), p1 = __ldg(pr + 1), p2 = __ldg(pr + 2);
-                float u, v;
-                float dist = intersect_prim(p0, p1, p2, o, d, u, v);
-                if (dist != 0.0f && dist < closest) {
-                    closest = dist;
-                    res = TraceResult{dist, static_cast<int32_t>(k), u, v};
-                    if (ANY_HIT) return res;
-                }
-            }
-        }
-        // pop
-        bool found = false;
-        while (sp > 0) {
-            --sp;
-            float te = stk_t[sp * stride];
-            if (te < closest) {
-                ref = stk_ref[sp * stride];
-                found = true;
-                break;
-            }
-        }
-        if (!found) break;
-    }
-    return res;
-}
-
-// Shared-memory stack bytes for a block of `threads` threads.
-inline size_t stack_smem_bytes(uint32_t stack_depth, int threads) {
-    return static_cast<size_t>(stack_depth) * threads * (sizeof(int32_t) + sizeof(float));
-}
-
 }  // namespace gr
 
 namespace gr {
@@ -199,6 +99,15 @@ namespace gr {
 // entries to a per-thread local array (rarely touched, cached in L1), so the shared
 // footprint no longer scales with the tree's worst-case depth.
 constexpr int SMEM_STACK = 16;  // MAX_STACK (common.cuh): both builds reject deeper trees
+
+// Extension kernels that refill their warps (k_extend_refill, k_eng_extend_refill): a
+// warp takes new rays for its idle lanes once at least this many are idle; 0 selects the
+// kernels with one ray per thread and no refill.  On the path-tracer workload (102,422
+// triangles, 1024 x 1024, 64 spp) 0 / 4 / 8 / 16 measured 1298 / 1511 / 1565 / 1586
+// Msamples/s.
+#ifndef GR_EXTEND_REFILL
+#define GR_EXTEND_REFILL 16
+#endif
 
 struct TravState {
     V3 o, d, inv;
@@ -365,6 +274,37 @@ GR_D bool trav_step(const DeviceScene& s, TravState& t, const StackView& stk, in
 
 inline size_t step_stack_smem_bytes(int threads) {
     return static_cast<size_t>(SMEM_STACK) * threads * (sizeof(int32_t) + sizeof(float));
+}
+
+// A thread's traversal stack: its column of the block's shared stack (dynamic shared
+// memory starting at `smem`, step_stack_smem_bytes(blockDim.x) bytes) and its local
+// spill array.
+GR_D StackView thread_stack(unsigned char* smem, int2* spill) {
+    int32_t* sref = reinterpret_cast<int32_t*>(smem);
+    float* st = reinterpret_cast<float*>(smem + sizeof(int32_t) * SMEM_STACK * blockDim.x);
+    return StackView{sref + threadIdx.x, st + threadIdx.x, static_cast<int>(blockDim.x), spill};
+}
+
+// Traces one ray to the end.  ANY_HIT: stops at the first hit closer than t_max (shadow
+// rays).  A miss returns t = t_max and k = -1.  A ray that needs more than the scene's
+// step budget is abandoned as a miss and flagged: *err = 2 and, if err_ray is given, the
+// ray's index there.  A stack overflow (impossible for trees the builds accept) sets
+// *err = 1.  With COUNT, counts[0] / counts[1] accumulate nodes visited / primitives
+// tested.
+template <int W, bool ANY_HIT, bool COUNT = false>
+GR_D TraceResult trace_ray(const DeviceScene& s, V3 o, V3 d, float t_max, const StackView& stk, int* err,
+                           int* err_ray = nullptr, uint32_t ray = 0, uint32_t* counts = nullptr) {
+    TravState t;
+    trav_init(t, o, d, t_max);
+    uint32_t steps = 0;
+    while (!trav_step<W, ANY_HIT, COUNT>(s, t, stk, err, counts)) {
+        if (++steps > s.step_budget) {
+            atomicExch(err, 2);
+            if (err_ray) atomicExch(err_ray, static_cast<int>(ray));
+            return TraceResult{t_max, -1, 0.0f, 0.0f};
+        }
+    }
+    return TraceResult{t.closest, t.hit, t.hu, t.hv};
 }
 
 }  // namespace gr
