@@ -148,7 +148,10 @@ def cpu_baseline(w, budget_s, lib=None):
     import gammaray_gb300 as g
     from gammaray_gb300 import _abi
 
-    lib = lib or _abi.Lib(os.path.join(ROOT, "oracle", "libgammaray_ref.so"))
+    if lib is None:
+        if not os.path.exists(os.path.join(ROOT, "oracle", "libgammaray_ref.so")):
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+        lib = _abi.Lib(os.path.join(ROOT, "oracle", "libgammaray_ref.so"))
     st = g.Stage(w.prims, lib=lib, environment=w.environment, seed=1)
     film = g.Film(w.width, w.height, lib=lib)
     passes, t0 = 0, time.perf_counter()
@@ -540,9 +543,10 @@ def run_ours(args, rank, world, local):
     roofline["traffic_source"] = (f"{EXTEND_DRAM_CAPTURE}: {EXTEND_DRAM_BYTES_PER_RAY} B/ray, "
                                   "x rays per timed launch")
 
-    batched = served = bdpt = None
+    batched = served = bdpt = cornell = None
     if rank == 0 and not args.no_bdpt:
         bdpt = run_bdpt(lib, min(args.cpu_seconds, 8.0))
+        cornell = run_cornell(lib, min(args.cpu_seconds, 3.0))
     if rank == 0 and not args.no_batch:
         batched = run_batched(lib)
     if rank == 0 and not args.no_serve:
@@ -554,7 +558,7 @@ def run_ours(args, rank, world, local):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": config_of(w), "mrays_per_s": mrays, "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
                 "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s": wall,
-                "batched": batched, "served": served, "bdpt": bdpt, "device_build": dev_build,
+                "batched": batched, "served": served, "bdpt": bdpt, "cornell": cornell, "device_build": dev_build,
                 "scene": {"components": int(info.num_components), "wide_nodes": int(info.num_wide_nodes),
                           "device_bytes": int(info.device_bytes), "build_s": info.build_seconds}}
         print(json.dumps(line), flush=True)
@@ -603,6 +607,38 @@ def run_bdpt(lib, cpu_seconds):
     out["cpu_oracle_msamples_per_s"] = passes * w.width * w.height / dt / 1e6
     out["cpu_oracle_sample"] = f"{passes} x 1-spp pass(es), {dt:.1f} s, {os.cpu_count()} threads"
     return out
+
+
+def run_cornell(lib, cpu_seconds):
+    """Config 1: the closed box with two spheres, path tracer, 256x256, 16 spp, max depth 8,
+    roulette after depth 3; device time of the GPU render beside the oracle on the host
+    cores (whole 1-spp passes of the same workload)."""
+    import gammaray_gb300 as g
+    from gammaray_gb300 import _abi, scenes
+
+    w = scenes.cornell_spheres(256, 256, 16)
+    st = g.Stage(w.prims, lib=lib, seed=7)
+    f = g.Film(w.width, w.height, lib=lib)
+    st.render(w.camera, w.integrator, f, 2)  # warm
+    ms = []
+    for _ in range(5):
+        f.clear()
+        st.render(w.camera, w.integrator, f, w.spp)
+        ms.append(st.last_stats().device_ms)
+    samples = w.width * w.height * w.spp
+    t = statistics.median(ms)
+    orc = _abi.Lib(os.path.join(ROOT, "oracle", "libgammaray_ref.so"))
+    so = g.Stage(w.prims, lib=orc, seed=7)
+    fo = g.Film(w.width, w.height, lib=orc)
+    passes, t0 = 0, time.perf_counter()
+    while passes == 0 or time.perf_counter() - t0 < cpu_seconds:
+        so.render(w.camera, w.integrator, fo, 1)
+        passes += 1
+    dt = time.perf_counter() - t0
+    return {"workload": "pt_cornell_spheres", "width": w.width, "height": w.height, "spp": w.spp, "max_depth": 8,
+            "msamples_per_s": samples / (t * 1e-3) / 1e6, "device_ms": t,
+            "cpu_oracle_msamples_per_s": passes * w.width * w.height / dt / 1e6,
+            "cpu_oracle_sample": f"{passes} x 1-spp pass(es), {dt:.1f} s, {os.cpu_count()} threads"}
 
 
 def profile_case(args):
