@@ -32,10 +32,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 # DRAM bytes (read + written) per extension ray of k_extend: ncu's dram__bytes_read.sum +
 # dram__bytes_write.sum summed over every k_extend launch of a 4-spp render of this
 # workload (bench.py --profile-case --spp 4; its 4 M-ray queues exceed L2 as the timed
-# renders' do), divided by that render's extension rays.  Re-measured whenever k_extend
-# changes; EXTEND_DRAM_CAPTURE says which capture the figure comes from.
-EXTEND_DRAM_BYTES_PER_RAY = 46.4
-EXTEND_DRAM_CAPTURE = "ncu, 4-spp render of the bench workload, all 12 k_extend launches"
+# renders' do), divided by that render's extension rays.  Re-measured whenever the
+# extension kernel changes; EXTEND_DRAM_CAPTURE says which capture the figure comes from.
+EXTEND_DRAM_BYTES_PER_RAY = 46.6
+EXTEND_DRAM_CAPTURE = "ncu, 4-spp render of the bench workload, all 12 k_extend_refill launches"
 sys.path.insert(0, ROOT)
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -530,7 +530,7 @@ def run_ours(args, rank, world, local):
     b_ray = nodes_per_ray * node_bytes + prims_per_ray * 48 + 48
     achieved = b_ray * rays / (ext_ms * 1e-3) / 1e9 if ext_ms > 0 else None
     peak, peak_kind = hbm_peak()
-    roofline = {"bound": "hbm", "kernel": "k_extend (closest-hit traversal)", "achieved": achieved, "peak": peak,
+    roofline = {"bound": "hbm", "kernel": "k_extend_refill (closest-hit traversal)", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
                 "peak_source": peak_kind,
                 "bytes_per_ray": b_ray, "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
