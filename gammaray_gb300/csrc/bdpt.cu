@@ -224,9 +224,17 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams
     push_warp(light_alive, count_out, 2 * i + 1, lo, ld, nslot, no, nd, p.nslots);
 }
 
-constexpr uint32_t BSHADE_PER_THREAD = SHADE_PER_THREAD;
+// BDPT walk shading in blocks of GR_BDPT_SHADE_BLOCK threads (128 or 768), each sorting its
+// chunk by code path; at 768 one block fills an SM (85 registers), so its warps shade the
+// same code path at a time (as the path tracer's k_shade, where 768 measured 9% faster).
+#ifndef GR_BDPT_SHADE_BLOCK
+#define GR_BDPT_SHADE_BLOCK 768
+#endif
+constexpr int BSBLOCK = GR_BDPT_SHADE_BLOCK;
+static_assert(BSBLOCK == 128 || BSBLOCK == 768, "BDPT shading block of 128 or 768 threads");
+constexpr uint32_t BSHADE_PER_THREAD = BSBLOCK == 128 ? SHADE_PER_THREAD : 85u;
 
-__global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts vs,
+__global__ void __launch_bounds__(BSBLOCK, 768 / BSBLOCK) k_bdpt_shade(DeviceScene s, BdptParams p, Verts vs,
                                                       const uint32_t* __restrict__ count_in,
                                                       const uint32_t* __restrict__ q_slot,
                                                       const float4* __restrict__ q_o, const float4* __restrict__ q_d,
@@ -237,15 +245,15 @@ __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts 
                                                       uint32_t* count_out, uint32_t* __restrict__ nslot,
                                                       float4* __restrict__ no, float4* __restrict__ nd) {
     extern __shared__ unsigned char dsmem[];
-    const SortView sm = sort_view<BLOCK, BSHADE_PER_THREAD>(dsmem);
+    const SortView sm = sort_view<BSBLOCK, BSHADE_PER_THREAD>(dsmem);
     const uint32_t n = *count_in;
     // Material-sorted shading (shade_sort.cuh), by (walk, material, chosen lobe).
     // Block-uniform chunk loop.
-    const uint32_t per = chunk_per_thread<BLOCK, BSHADE_PER_THREAD>(n, gridDim.x);
-    const uint32_t chunk = BLOCK * per;
+    const uint32_t per = chunk_per_thread<BSBLOCK, BSHADE_PER_THREAD>(n, gridDim.x);
+    const uint32_t chunk = BSBLOCK * per;
     for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
         const uint32_t cn = min(chunk, n - c0);
-        sort_chunk<BLOCK, SHADE_PER_THREAD>(sm, cn, per, [&](uint32_t i) {
+        sort_chunk<BSBLOCK, BSHADE_PER_THREAD>(sm, cn, per, [&](uint32_t i) {
             uint32_t q = c0 + i;
             uint32_t sl = q_slot[q];
             uint32_t w = sl & 1u;
@@ -253,7 +261,7 @@ __global__ void GR_SHADE_BOUNDS k_bdpt_shade(DeviceScene s, BdptParams p, Verts 
             return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(key_buf[sl >> 1], dim), w);
         });
         for (uint32_t e = 0; e < per; ++e) {
-            uint32_t i = e * BLOCK + threadIdx.x;
+            uint32_t i = e * BSBLOCK + threadIdx.x;
             bool alive = false;
             uint32_t slot = 0;
             V3 new_o = v3zero(), new_d = v3zero();
@@ -907,10 +915,10 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             if (s1 != GR_OK) return s1;
             GR_CUDA_TRY(cudaGetLastError());
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            const size_t ssmem = sort_smem_bytes(BLOCK, BSHADE_PER_THREAD);
+            const size_t ssmem = sort_smem_bytes(BSBLOCK, BSHADE_PER_THREAD);
             GR_CUDA_TRY(allow_sort_smem(k_bdpt_shade, ssmem));
-            int grid = resident_grid(k_bdpt_shade, ssmem, p.nslots);
-            k_bdpt_shade<<<grid, BLOCK, ssmem, st>>>(job.scene, p, vs, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
+            int grid = resident_grid(k_bdpt_shade, ssmem, p.nslots, BSBLOCK);
+            k_bdpt_shade<<<grid, BSBLOCK, ssmem, st>>>(job.scene, p, vs, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                                  ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
                                                  ps.q_hit.as<float4>(), bs.vcount.as<uint32_t>(), ps.tp.as<float4>(),
                                                  ps.key.as<unsigned long long>(), bs.flags.as<uint32_t>(),

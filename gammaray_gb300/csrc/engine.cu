@@ -12,10 +12,16 @@ namespace gr {
 namespace {
 
 constexpr int EBLOCK = 128;
-constexpr uint32_t ESHADE_PER_THREAD = SHADE_PER_THREAD;
-#ifndef GR_SHADE_MIN_BLOCKS
-#define GR_SHADE_MIN_BLOCKS 6
+// The engine's shading kernel: blocks of GR_ENG_SHADE_BLOCK threads (128 or 768), each
+// sorting its chunk of the queue by code path.  At 768 one block fills an SM (85
+// registers), so all of an SM's warps shade the same code path at a time, as in the
+// path tracer's k_shade.
+#ifndef GR_ENG_SHADE_BLOCK
+#define GR_ENG_SHADE_BLOCK 768
 #endif
+constexpr int ESBLOCK = GR_ENG_SHADE_BLOCK;
+static_assert(ESBLOCK == 128 || ESBLOCK == 768, "engine shading block of 128 or 768 threads");
+constexpr uint32_t ESHADE_PER_THREAD = ESBLOCK == 128 ? SHADE_PER_THREAD : 85u;
 constexpr int GATHER_BLOCKS = 512;
 
 // Path state.  The queue entry of a live path carries its ray, its job (o.w) and its
@@ -281,25 +287,25 @@ __global__ void __launch_bounds__(BS) k_eng_extend_refill(EngineCtl* c, int cur,
     }
 }
 
-__global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
+__global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
     k_eng_shade(EngineCtl* c, int cur, const DevJob* __restrict__ jobs, uint32_t* unit_done,
                 const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
                 const float4* __restrict__ q_d, const float4* __restrict__ q_hit, float4* __restrict__ s_hot,
                 const uint4* __restrict__ s_cold, uint32_t* __restrict__ nslot, float4* __restrict__ no,
                 float4* __restrict__ nd, uint32_t cap) {
     extern __shared__ unsigned char dsmem[];
-    const SortView sm = sort_view<EBLOCK, ESHADE_PER_THREAD>(dsmem);
+    const SortView sm = sort_view<ESBLOCK, ESHADE_PER_THREAD>(dsmem);
     const int nxt = cur ^ 1;
     const uint32_t n = c->q[cur];
     const unsigned lane = threadIdx.x & 31u;
     // Material-sorted shading (shade_sort.cuh), by code path (chosen lobe type and the
     // material's lobe types, whatever the job); misses, cancelled and display-colour
     // jobs share bucket 0.  Block-uniform chunk loop.
-    const uint32_t per = chunk_per_thread<EBLOCK, ESHADE_PER_THREAD>(n, gridDim.x);
-    const uint32_t chunk = EBLOCK * per;
+    const uint32_t per = chunk_per_thread<ESBLOCK, ESHADE_PER_THREAD>(n, gridDim.x);
+    const uint32_t chunk = ESBLOCK * per;
     for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
         const uint32_t cn = min(chunk, n - c0);
-        sort_chunk<EBLOCK, ESHADE_PER_THREAD>(sm, cn, per, [&](uint32_t i) {
+        sort_chunk<ESBLOCK, ESHADE_PER_THREAD>(sm, cn, per, [&](uint32_t i) {
             uint32_t q = c0 + i;
             uint32_t jb = __float_as_uint(q_o[q].w);
             const DevJob& J = jobs[jb];
@@ -310,7 +316,7 @@ __global__ void __launch_bounds__(EBLOCK, GR_SHADE_MIN_BLOCKS)
             return shade_bucket(J.scene, k, uniform01(key, DIM_CAMERA_WALK + 4 * __float_as_uint(q_d[q].w)), 0);
         });
         for (uint32_t e = 0; e < per; ++e) {
-            uint32_t i = e * EBLOCK + threadIdx.x;
+            uint32_t i = e * ESBLOCK + threadIdx.x;
             bool alive = false, finished = false;
             uint32_t slot = 0, job = 0, unit = 0xFFFFFFFFu, depth = 0;
             V3 new_o = v3zero(), new_d = v3zero();
@@ -475,7 +481,7 @@ gr_status Engine::init(const EngineConfig& cfg, cudaStream_t) {
     GR_CUDA_TRY(cudaMemsetAsync(unit_done_.ptr, 0, ENGINE_MAX_UNITS * sizeof(uint32_t), st_));
     GR_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&h_pinned_), 8 * sizeof(uint64_t), cudaHostAllocDefault));
     GR_CUDA_TRY(cudaStreamSynchronize(st_));
-    GR_CUDA_TRY(allow_sort_smem(k_eng_shade, sort_smem_bytes(EBLOCK, ESHADE_PER_THREAD)));
+    GR_CUDA_TRY(allow_sort_smem(k_eng_shade, sort_smem_bytes(ESBLOCK, ESHADE_PER_THREAD)));
     return record_pair();
 }
 
@@ -507,9 +513,9 @@ gr_status Engine::enqueue_iteration(int cur) {
                                        q_d_[cur].as<float4>(), q_hit_.as<float4>(), C, st_));
     }
     GR_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(c) + offsetof(EngineCtl, q) + nxt * sizeof(uint32_t), 0, 4, st_));
-    const size_t ssmem = sort_smem_bytes(EBLOCK, ESHADE_PER_THREAD);
-    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), EBLOCK, ssmem, C);
-    k_eng_shade<<<sgrid, EBLOCK, ssmem, st_>>>(c, cur, jobs_.as<DevJob>(), unit_done_.as<uint32_t>(),
+    const size_t ssmem = sort_smem_bytes(ESBLOCK, ESHADE_PER_THREAD);
+    int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), ESBLOCK, ssmem, C);
+    k_eng_shade<<<sgrid, ESBLOCK, ssmem, st_>>>(c, cur, jobs_.as<DevJob>(), unit_done_.as<uint32_t>(),
                                            q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>(),
                                            q_hit_.as<float4>(), s_hot_.as<float4>(), s_cold_.as<uint4>(),
                                            q_slot_[nxt].as<uint32_t>(), q_o_[nxt].as<float4>(),
