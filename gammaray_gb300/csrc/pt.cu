@@ -34,23 +34,26 @@ namespace gr {
 
 namespace {
 
-// Threads per block of the path tracer's shading kernel (128, 384 or 768), each block
-// sorting its chunk of the queue by code path.  With larger blocks, fewer blocks share an
-// SM, so more of its warps run the same code path at a time.  The register cap (85) and
-// the warps per SM stay those of six 128-thread blocks.  On the 102,422-triangle
-// 1024 x 1024 64-spp render, 128 / 384 / 768 measured 1585 / 1605 / 1726 Msamples/s
-// (shading 37% / 36% / 31% of device time): one block per SM, whose warps all shade the
-// same code path, relieves the instruction fetch that bounded the kernel.
+// Threads per block of the path tracer's shading kernel, each block sorting its chunk of
+// the queue by code path.  With larger blocks, fewer blocks share an SM, so more of its
+// warps run the same code path at a time; the register cap (85) and the warps per SM
+// stay those of six 128-thread blocks.  On the 102,422-triangle 1024 x 1024 64-spp
+// render, blocks of 128 / 384 / 768 measured 1585 / 1605 / 1726 Msamples/s (shading 37%
+// / 36% / 31% of device time): one block per SM, whose warps all shade the same code
+// path, relieves the instruction fetch that bounded the kernel.  A queue too short to
+// give every SM two such blocks is shaded in 128-thread blocks instead, which spread
+// it over all SMs.
 #ifndef GR_SHADE_BLOCK
 #define GR_SHADE_BLOCK 768
 #endif
-constexpr int SBLOCK = GR_SHADE_BLOCK;
-static_assert(SBLOCK == 128 || SBLOCK == 384 || SBLOCK == 768, "shading block of 128, 384 or 768 threads");
-constexpr int SBLOCKS_PER_SM = 768 / SBLOCK;
+constexpr int SHADE_BIG = GR_SHADE_BLOCK;
+static_assert(SHADE_BIG == 128 || SHADE_BIG == 384 || SHADE_BIG == 768, "shading block of 128, 384 or 768 threads");
 // Entries per thread per chunk: 64 at 128 threads; larger blocks as many as fit the
 // 16-bit chunk positions and the shared memory of their blocks per SM.
-constexpr uint32_t SPER = SBLOCK == 128 ? SHADE_PER_THREAD : (SBLOCK == 384 ? 96u : 85u);
-#define GR_PT_SHADE_BOUNDS __launch_bounds__(SBLOCK, SBLOCKS_PER_SM)
+template <int NT>
+constexpr uint32_t shade_per() {
+    return NT == 128 ? SHADE_PER_THREAD : (NT == 384 ? 96u : 85u);
+}
 
 struct PTParams {
     DevCamera cam;
@@ -89,7 +92,8 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
 // Material-sorted shading (shade_sort.cuh): each block sorts its chunk of the queue by
 // code path (chosen lobe type, the material's lobe types), then shades it in that order.
 
-__global__ void GR_PT_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t depth,
+template <int NT>
+__global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams p, uint32_t depth,
                                                  const uint32_t* __restrict__ count_in,
                                                  const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
                                                  const float4* __restrict__ q_d, const float4* __restrict__ q_hit,
@@ -98,21 +102,22 @@ __global__ void GR_PT_SHADE_BOUNDS k_shade(DeviceScene s, PTParams p, uint32_t d
                                                  uint32_t* __restrict__ nslot, float4* __restrict__ no,
                                                  float4* __restrict__ nd) {
     extern __shared__ unsigned char dsmem[];
-    const SortView sm = sort_view<SBLOCK, SPER>(dsmem);
+    constexpr uint32_t PER = shade_per<NT>();
+    const SortView sm = sort_view<NT, PER>(dsmem);
     const uint32_t n = *count_in;
     const uint32_t base = DIM_CAMERA_WALK + 4 * depth;
     // Block-uniform chunk loop (sort_chunk's barriers need every thread).
-    const uint32_t per = chunk_per_thread<SBLOCK, SPER>(n, gridDim.x);
-    const uint32_t chunk = SBLOCK * per;
+    const uint32_t per = chunk_per_thread<NT, PER>(n, gridDim.x);
+    const uint32_t chunk = NT * per;
     for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
         const uint32_t cn = min(chunk, n - c0);
-        sort_chunk<SBLOCK, SPER>(sm, cn, per, [&](uint32_t i) {
+        sort_chunk<NT, PER>(sm, cn, per, [&](uint32_t i) {
             uint32_t q = c0 + i;
             return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(key_buf[q_slot[q]], base), 0);
         });
         // Every lane runs every step so that all of them reach the ballot in push_warp.
         for (uint32_t e = 0; e < per; ++e) {
-            uint32_t i = e * SBLOCK + threadIdx.x;
+            uint32_t i = e * NT + threadIdx.x;
             bool alive = false;
             uint32_t slot = 0;
             V3 new_o = v3zero(), new_d = v3zero();
@@ -173,6 +178,25 @@ __global__ void __launch_bounds__(BLOCK) k_shade_display(DeviceScene s, const ui
     }
 }
 
+template <int NT, class... A>
+gr_status launch_shade_nt(uint32_t n_bound, cudaStream_t st, A... a) {
+    const size_t smem = sort_smem_bytes(NT, shade_per<NT>());
+    GR_CUDA_TRY(allow_sort_smem(k_shade<NT>, smem));
+    // Every resident block; each picks its entries per thread from the queue length.
+    int grid = resident_grid(k_shade<NT>, smem, n_bound, NT);
+    k_shade<NT><<<grid, NT, smem, st>>>(a...);
+    return GR_OK;
+}
+
+// Shades a queue of at most n_bound entries (the device holds the exact length): in
+// SHADE_BIG-thread blocks while that fills two blocks per SM, else in 128-thread blocks.
+template <class... A>
+gr_status launch_shade(uint32_t n_bound, cudaStream_t st, A... a) {
+    if (SHADE_BIG != 128 && n_bound >= 2u * static_cast<uint32_t>(device_sm_count()) * SHADE_BIG)
+        return launch_shade_nt<SHADE_BIG>(n_bound, st, a...);
+    return launch_shade_nt<128>(n_bound, st, a...);
+}
+
 __global__ void k_samples_out(uint32_t n, const float2* __restrict__ st, const float4* __restrict__ L, float* out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -225,8 +249,6 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     if (static_cast<uint64_t>(group) * npix > 0xFFFFFFFFull / 2) group = 1;
     PathState& ps = device_work().paths;
     GR_CUDA_TRY(ps.ensure(static_cast<size_t>(group) * npix));
-    const size_t shade_smem = sort_smem_bytes(SBLOCK, SPER);
-    GR_CUDA_TRY(allow_sort_smem(k_shade, shade_smem));
     uint32_t* cnt = sc->counters.as<uint32_t>();
     int* err = reinterpret_cast<int*>(cnt + CNT_ERROR);
     unsigned long long* rays = reinterpret_cast<unsigned long long*>(cnt + CNT_RAYS);
@@ -281,6 +303,7 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         uint32_t n = g * npix;
         p.first_pass = rp.first_pass + done;
         GR_CUDA_TRY(cudaMemcpyAsync(cnt + CNT_QUEUE0, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        uint32_t bound = n;  // an upper bound of the current queue length
         k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, ps.tp.as<float4>(), ps.light.as<float4>(),
                                                             ps.key.as<unsigned long long>(), ps.st.as<float2>(),
                                                             ps.q_slot[0].as<uint32_t>(), ps.q_o[0].as<float4>(),
@@ -314,14 +337,11 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
             if (timed) GR_TRY_S(mark(e0));
-            // Every resident block; each picks its entries per thread from the queue length.
-            int grid = resident_grid(k_shade, shade_smem, n, SBLOCK);
-            k_shade<<<grid, SBLOCK, shade_smem, st>>>(job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
-                                            ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(),
-                                            ps.q_hit.as<float4>(), ps.tp.as<float4>(), ps.light.as<float4>(),
-                                            ps.key.as<unsigned long long>(), cnt + nxt,
-                                            ps.q_slot[nxt].as<uint32_t>(), ps.q_o[nxt].as<float4>(),
-                                            ps.q_d[nxt].as<float4>());
+            GR_TRY_S(launch_shade(bound, st, job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
+                                  ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(),
+                                  ps.tp.as<float4>(), ps.light.as<float4>(), ps.key.as<unsigned long long>(),
+                                  cnt + nxt, ps.q_slot[nxt].as<uint32_t>(), ps.q_o[nxt].as<float4>(),
+                                  ps.q_d[nxt].as<float4>()));
             GR_CUDA_TRY(cudaGetLastError());
             ++launches;
             GR_TRY_S(sync_check(st, "shade", depth, n));
@@ -335,6 +355,9 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             if (depth >= 2) {
                 GR_CUDA_TRY(cudaEventSynchronize(evs[(depth - 2) & 3]));
                 if (host_cnt[(depth - 2) & 3] == 0) break;
+                // Paths only leave the queue within a group, so the length known for
+                // bounce depth - 1 bounds every later bounce's.
+                bound = host_cnt[(depth - 2) & 3];
             }
         }
         if (job.film) {
@@ -483,8 +506,6 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
     void* base = nullptr;
     GR_TRY_S(static_scratch(&base));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const size_t shade_smem = sort_smem_bytes(SBLOCK, SPER);
-    GR_CUDA_TRY(allow_sort_smem(k_shade, shade_smem));
     const uint32_t npix = static_cast<uint32_t>(npix64);
     const size_t cap = STATIC_MAX_PATHS;
     // Carve the array (same layout for every call; every region is 16-byte aligned).
@@ -545,10 +566,8 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
                 break;
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            // Every resident block; each picks its entries per thread from the queue length.
-            int grid = resident_grid(k_shade, shade_smem, n, SBLOCK);
-            k_shade<<<grid, SBLOCK, shade_smem, st>>>(sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit, tp,
-                                            light, key, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt]);
+            GR_TRY_S(launch_shade(n, st, sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit, tp,
+                                  light, key, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt]));
             GR_CUDA_TRY(cudaGetLastError());
             if (p.max_depth == 0 && (depth & 3) == 3) {
                 // Unbounded (reference) depth: stop once no path is left.  The copy goes
