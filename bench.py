@@ -280,7 +280,7 @@ def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3, other_policy=True
     resolution 256^2..1920x1080, spp 1-256, depth 4-16.  Served by the continuous-
     batching loop (arrival order with backfill, the default policy) vs a FIFO timeline of
     one gr_render per request on the same GPU; then the same requests under the
-    shortest-remaining-work policy."""
+    shortest-remaining-work policy.  Both latencies run from the request's arrival."""
     import gammaray_gb300 as g
     from gammaray_gb300 import _abi, scenes, serve
 
@@ -313,7 +313,7 @@ def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3, other_policy=True
     plain_span = finish - reqs[0]["arrival"]
     def serve_all(policy):
         srv = serve.Server(lib, max_active=16, policy=policy)
-        ids = {}
+        ids, late = {}, {}
         t0 = time.perf_counter()
         nxt = 0
         while nxt < len(reqs) or any(srv.poll(i).state < 2 for i in ids.values()):
@@ -322,6 +322,7 @@ def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3, other_policy=True
                 r = reqs[nxt]
                 ids[nxt] = srv.submit(stages[r["scene"]], r["cam"], g.PathTracerIntegrator(max_depth=r["depth"]),
                                       r["res"][0], r["res"][1], r["spp"])
+                late[nxt] = (time.perf_counter() - t0 - r["arrival"]) * 1e3  # arrival -> submission
                 nxt += 1
             if nxt < len(reqs) and not any(srv.poll(i).state < 2 for i in ids.values()):
                 time.sleep(max(0.0, reqs[nxt]["arrival"] - now))
@@ -331,7 +332,7 @@ def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3, other_policy=True
         lat = []
         for k, rid in ids.items():
             st = srv.poll(rid)
-            lat.append(st.finish_ms - st.submit_ms)
+            lat.append(st.finish_ms - st.submit_ms + late[k])  # from the request's arrival
             srv.take(rid)
         srv.close()
         return span, lat
@@ -343,7 +344,12 @@ def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3, other_policy=True
            "plain_fifo_msamples_per_s": samples / plain_span / 1e6, "plain_fifo_latency_ms": percentiles(lat_plain),
            "plain_busy_msamples_per_s": samples / sum(dur) / 1e6,
            "speedup_vs_plain_fifo": plain_span / span,
-           "requests_slower_than_fifo": int(sum(a > b for a, b in zip(lat, lat_plain)))}
+           "requests_slower_than_fifo": int(sum(a > b for a, b in zip(lat, lat_plain))),
+           "per_request": {"fields": ["width", "height", "spp", "max_depth", "arrival_ms", "alone_ms", "fifo_ms",
+                                      "served_ms"],
+                           "rows": [[r["res"][0], r["res"][1], r["spp"], r["depth"], round(r["arrival"] * 1e3, 1),
+                                     round(d * 1e3, 1), round(lp, 1), round(ls, 1)]
+                                    for r, d, lp, ls in zip(reqs, dur, lat_plain, lat)]}}
     if other_policy:
         span2, lat2 = serve_all(_abi.SERVE_SHORTEST_FIRST)
         out["shortest_first"] = {"msamples_per_s": samples / span2 / 1e6, "latency_ms": percentiles(lat2),
@@ -362,7 +368,7 @@ def run_progressive(lib, g, serve, stages, reqs, target):
     drawn spp is not used here: relMSE, not a pass count, ends a request).  The plain comparator renders each request's final pass count with one
     gr_render, FIFO, as if it had known the count in advance."""
     srv = serve.Server(lib, max_active=16)
-    ids = {}
+    ids, late = {}, {}
     t0 = time.perf_counter()
     nxt = 0
     while nxt < len(reqs) or any(srv.poll(i).state < 2 for i in ids.values()):
@@ -371,6 +377,7 @@ def run_progressive(lib, g, serve, stages, reqs, target):
             r = reqs[nxt]
             ids[nxt] = srv.submit(stages[r["scene"]], r["cam"], g.PathTracerIntegrator(max_depth=r["depth"]),
                                   r["res"][0], r["res"][1], PROGRESSIVE_MAX_PASSES, target_rel_mse=target)
+            late[nxt] = (time.perf_counter() - t0 - r["arrival"]) * 1e3
             nxt += 1
         if nxt < len(reqs) and not any(srv.poll(i).state < 2 for i in ids.values()):
             time.sleep(max(0.0, reqs[nxt]["arrival"] - now))
@@ -380,7 +387,7 @@ def run_progressive(lib, g, serve, stages, reqs, target):
     lat, passes, met, est = [], [], 0, []
     for k, rid in ids.items():
         st = srv.poll(rid)
-        lat.append(st.finish_ms - st.submit_ms)
+        lat.append(st.finish_ms - st.submit_ms + late[k])  # from the request's arrival
         passes.append(int(st.passes_done))
         est.append(float(st.rel_mse))
         met += st.rel_mse <= target

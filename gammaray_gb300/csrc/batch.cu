@@ -328,6 +328,7 @@ struct gr_server {
     // be queued, so the scene is released once the engine reports all work gathered.
     std::vector<gr_scene*> retired;
     uint64_t resets = 0;  // times the engine's job and unit tables were cleared at idle
+    double pair_ms = 0.0;  // moving average of one graph pair's wall time, for step sizing
     std::chrono::steady_clock::time_point t0;
     double now_ms() const {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -374,10 +375,10 @@ gr_status schedule(gr_server* s) {
         r->start_ms = s->now_ms();
         ++active;
     }
-    // Keep about two pools' worth of paths appended but not yet issued.
-    EngineCtl c;
-    gr_status st = s->engine.read_ctl(c);
-    if (st != GR_OK) return st;
+    // Keep about two pools' worth of paths appended but not yet issued (from the control
+    // block the last run read: only this function appends, and it runs before each run).
+    const EngineCtl& c = s->engine.last_ctl();
+    gr_status st = GR_OK;
     uint64_t backlog = c.paths_total - c.gcur;
     const uint64_t want = 2ull * s->engine.capacity();
     // Which request's passes go first (gr_server_options.policy):
@@ -468,9 +469,8 @@ gr_status reset_if_idle(gr_server* s) {
 
 // Marks passes gathered (every unit below the engine's g_lo is in its film).
 gr_status progress(gr_server* s) {
-    EngineCtl c;
-    gr_status st = s->engine.read_ctl(c);
-    if (st != GR_OK) return st;
+    const EngineCtl& c = s->engine.last_ctl();  // as the last run left it
+    gr_status st = GR_OK;
     for (auto& r : s->reqs) {
         if (r->state != GR_REQUEST_RUNNING) continue;
         uint32_t d = 0;
@@ -592,9 +592,27 @@ gr_status gr_server_step(gr_server* s, double budget_ms) {
         bool any = false;
         for (auto& r : s->reqs) any |= r->state == GR_REQUEST_RUNNING;
         if (!any) return reset_if_idle(s);
-        bool done = false;
-        st = s->engine.run(4, done);
+        // As many pairs as the step's budget allows (from the time pairs have taken so
+        // far; at least 1, at most 4), ending early once every unit of the running
+        // request that completes first in unit order is gathered, so the host hears of
+        // finished requests (and takes new ones) within about one pair.
+        uint32_t stop = 0xFFFFFFFFu;
+        for (auto& r : s->reqs)
+            if (r->state == GR_REQUEST_RUNNING && r->appended == r->cap() && !r->units.empty())
+                stop = std::min(stop, r->units.back() + 1);
+        const double left = t_end - s->now_ms();
+        uint32_t pairs = 4;
+        if (s->pair_ms > 0.0) pairs = static_cast<uint32_t>(std::max(1.0, std::min(4.0, left / s->pair_ms)));
+        st = s->engine.set_flush_unit(stop == 0xFFFFFFFFu ? 0u : stop);
         if (st != GR_OK) return st;
+        bool done = false;
+        const double t_run = s->now_ms();
+        st = s->engine.run(pairs, done, stop);
+        if (st != GR_OK) return st;
+        if (s->engine.last_pairs() > 0) {
+            const double per = (s->now_ms() - t_run) / s->engine.last_pairs();
+            s->pair_ms = s->pair_ms > 0.0 ? 0.7 * s->pair_ms + 0.3 * per : per;
+        }
         if (done && !s->retired.empty()) {  // every appended unit gathered: no path left
             GR_CUDA_TRY(cudaStreamSynchronize(s->engine.stream()));
             for (gr_scene* sc : s->retired) scene_release(sc);

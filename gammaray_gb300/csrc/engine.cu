@@ -93,7 +93,7 @@ __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const 
     // every appended unit has finished, or the ring would soon limit the fill.
     const unsigned long long fin = (u < c->units_count ? units[u].prefix : c->paths_total) - c->gather_lo_prefix;
     const bool flush = n == GATHER_MAX || u == c->units_count || fin >= cap / 2 ||
-                       c->gcur + cap > c->gather_lo_prefix + ring;
+                       c->gcur + cap > c->gather_lo_prefix + ring || (c->flush_unit != 0 && u >= c->flush_unit);
     if (!flush) {
         n = 0;
         groups = 0;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(BS) k_eng_extend_refill(EngineCtl* c, int cur,
     const unsigned lane = threadIdx.x & 31u;
     const unsigned below = (1u << lane) - 1u;
     TravState t;
-    const DeviceScene* s = nullptr;
+    TraceScene s{nullptr, nullptr};
     uint32_t q = 0, steps = 0, budget = 0;
     bool busy = false, exhausted = false;
     for (;;) {
@@ -262,8 +262,9 @@ __global__ void __launch_bounds__(BS) k_eng_extend_refill(EngineCtl* c, int cur,
                 const uint32_t mine = base + __popc(idle & below);
                 if (mine < n) {
                     float4 o4 = q_o[mine], d4 = q_d[mine];
-                    s = &jobs[__float_as_uint(o4.w)].scene;
-                    budget = s->step_budget;
+                    const DeviceScene& js = jobs[__float_as_uint(o4.w)].scene;
+                    s = TraceScene{js.nodes, js.prims};
+                    budget = js.step_budget;
                     trav_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX);
                     q = mine;
                     steps = 0;
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(BS) k_eng_extend_refill(EngineCtl* c, int cur,
         }
         if (__ballot_sync(0xffffffffu, busy) == 0u) break;
         if (busy) {
-            bool done = trav_step<W, false, false>(*s, t, stk, &c->err, nullptr);
+            bool done = trav_step<W, false, false>(s, t, stk, &c->err, nullptr);
             if (!done && ++steps > budget) {
                 atomicExch(&c->err, 2);
                 t.hit = -1;
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
     // material's lobe types, whatever the job); misses, cancelled and display-colour
     // jobs share bucket 0.  Block-uniform chunk loop.
     const uint32_t per = chunk_per_thread<ESBLOCK, ESHADE_PER_THREAD>(n, gridDim.x);
-    const uint32_t chunk = ESBLOCK * per;
+    const uint32_t chunk = chunk_entries<ESBLOCK>(n, gridDim.x, per);
     for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
         const uint32_t cn = min(chunk, n - c0);
         sort_chunk<ESBLOCK, ESHADE_PER_THREAD>(sm, cn, per, [&](uint32_t i) {
@@ -479,7 +480,7 @@ gr_status Engine::init(const EngineConfig& cfg, cudaStream_t) {
     GR_CUDA_TRY(alloc(q_hit_, C * 16));
     GR_CUDA_TRY(cudaMemsetAsync(ctl_.ptr, 0, sizeof(EngineCtl), st_));
     GR_CUDA_TRY(cudaMemsetAsync(unit_done_.ptr, 0, ENGINE_MAX_UNITS * sizeof(uint32_t), st_));
-    GR_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&h_pinned_), 8 * sizeof(uint64_t), cudaHostAllocDefault));
+    GR_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&h_pinned_), 16 * sizeof(uint64_t), cudaHostAllocDefault));
     GR_CUDA_TRY(cudaStreamSynchronize(st_));
     GR_CUDA_TRY(allow_sort_smem(k_eng_shade, sort_smem_bytes(ESBLOCK, ESHADE_PER_THREAD)));
     return record_pair();
@@ -607,6 +608,16 @@ gr_status Engine::reset() {
     GR_CUDA_TRY(cudaStreamSynchronize(st_));
     h_jobs_.clear();
     h_units_.clear();
+    last_ctl_ = EngineCtl{};
+    return GR_OK;
+}
+
+gr_status Engine::set_flush_unit(uint32_t unit) {
+    h_pinned_[12] = unit;
+    // Ordered before the next run's replays on the same stream; the pinned word is not
+    // written again before that run has synchronised the stream.
+    GR_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(EngineCtl, flush_unit), &h_pinned_[12],
+                                4, cudaMemcpyHostToDevice, st_));
     return GR_OK;
 }
 
@@ -622,11 +633,12 @@ gr_status Engine::cancel_job(uint32_t j) {
     return GR_OK;
 }
 
-gr_status Engine::run(uint32_t max_pairs, bool& done) {
+gr_status Engine::run(uint32_t max_pairs, bool& done, uint32_t stop_at_unit) {
     done = false;
-    // Replays graph pairs; the done flag is copied back after each replay and read two
-    // replays behind, so the host never stalls the GPU.  Replays after completion are
-    // empty iterations.
+    // Replays graph pairs; the done flag and the oldest ungathered unit are copied back
+    // after each replay and read one replay behind (the next replay is already queued,
+    // so the GPU does not wait for the host).  Replays after completion are empty
+    // iterations.
     cudaEvent_t ev[4];
     for (auto& e : ev) GR_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     struct Free {
@@ -636,9 +648,11 @@ gr_status Engine::run(uint32_t max_pairs, bool& done) {
         }
     } fr{ev};
     const char* done_ptr = reinterpret_cast<const char*>(ctl_.ptr) + offsetof(EngineCtl, done);
+    const char* glo_ptr = reinterpret_cast<const char*>(ctl_.ptr) + offsetof(EngineCtl, g_lo);
     // Progress guard: every 256 replays the traced-ray / gathered counters must have
     // moved.
     unsigned long long last_rays = ~0ull;
+    uint32_t launched = 0;
     uint32_t last_glo = ~0u;
     for (uint32_t k = 0; k < max_pairs; ++k) {
         if (k && (k & 255) == 0) {
@@ -654,17 +668,22 @@ gr_status Engine::run(uint32_t max_pairs, bool& done) {
             last_glo = c.g_lo;
         }
         GR_CUDA_TRY(cudaGraphLaunch(graph_, st_));
+        ++launched;
         h_pinned_[k & 3] = 0;
+        h_pinned_[8 + (k & 3)] = 0;
         GR_CUDA_TRY(cudaMemcpyAsync(&h_pinned_[k & 3], done_ptr, 4, cudaMemcpyDeviceToHost, st_));
+        GR_CUDA_TRY(cudaMemcpyAsync(&h_pinned_[8 + (k & 3)], glo_ptr, 4, cudaMemcpyDeviceToHost, st_));
         GR_CUDA_TRY(cudaEventRecord(ev[k & 3], st_));
-        if (k >= 2) {
-            GR_CUDA_TRY(cudaEventSynchronize(ev[(k - 2) & 3]));
-            if (h_pinned_[(k - 2) & 3]) break;
+        if (k >= 1) {
+            GR_CUDA_TRY(cudaEventSynchronize(ev[(k - 1) & 3]));
+            if (h_pinned_[(k - 1) & 3]) break;
+            if (h_pinned_[8 + ((k - 1) & 3)] >= stop_at_unit) break;
         }
     }
     GR_CUDA_TRY(cudaStreamSynchronize(st_));
-    EngineCtl c;
+    EngineCtl& c = last_ctl_;
     GR_CUDA_TRY(cudaMemcpy(&c, ctl_.ptr, sizeof(EngineCtl), cudaMemcpyDeviceToHost));
+    last_pairs_ = launched;
     done = c.done != 0;
     last_rays_ = c.rays;
     if (c.err == 2) {

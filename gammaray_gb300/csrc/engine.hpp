@@ -64,6 +64,10 @@ struct EngineCtl {
     int32_t err;
     uint32_t iter;
     uint32_t fetch;  // rays handed out by the refilling extension kernel this iteration
+    // Set by the host (0 = none): gather as soon as every unit below this one has
+    // finished, without waiting for a larger batch, so the request those units complete
+    // is done within one iteration.
+    uint32_t flush_unit;
     uint32_t gather_units[GATHER_MAX];      // unit indices, each job's units contiguous and in pass order
     uint32_t gather_group_first[GATHER_MAX];  // per group: first entry in gather_units
     uint32_t gather_group_count[GATHER_MAX];
@@ -88,13 +92,21 @@ class Engine {
     // Appends units of several jobs round-robin by pass: units[k] = (job, pass).
     gr_status append_units(const std::vector<std::pair<uint32_t, uint32_t>>& units);
     gr_status cancel_job(uint32_t job_index);
+    // Sets EngineCtl::flush_unit (0 = none) for the iterations that follow.
+    gr_status set_flush_unit(uint32_t unit);
     // Forgets every job and unit (buffers and the captured graph are kept).
     gr_status reset();
-    // Runs iteration pairs (graph replays) until every appended unit is gathered or
-    // `max_pairs` pairs ran.  Returns whether all work is done.
-    gr_status run(uint32_t max_pairs, bool& done);
+    // Runs iteration pairs (graph replays) until every appended unit is gathered,
+    // `max_pairs` pairs ran, or the oldest ungathered unit reaches `stop_at_unit` (so a
+    // caller waiting for the units before it hears of them within one pair).  Returns
+    // whether all work is done.
+    gr_status run(uint32_t max_pairs, bool& done, uint32_t stop_at_unit = 0xFFFFFFFFu);
     // Host copies of the control block and unit progress (synchronises the stream).
     gr_status read_ctl(EngineCtl& ctl);
+    // The control block as the last run() left it (read there, no further sync), and the
+    // graph pairs that run launched.
+    const EngineCtl& last_ctl() const { return last_ctl_; }
+    uint32_t last_pairs() const { return last_pairs_; }
     gr_status unit_done_counts(std::vector<uint32_t>& done);
     const std::vector<DevUnit>& units() const { return h_units_; }
     const std::vector<DevJob>& jobs() const { return h_jobs_; }
@@ -119,6 +131,8 @@ class Engine {
     uint32_t jobs_cap_ = 0, units_cap_ = 0;
     cudaGraphExec_t graph_ = nullptr;
     uint64_t last_rays_ = 0;
+    EngineCtl last_ctl_{};
+    uint32_t last_pairs_ = 0;
     uint64_t bytes_ = 0;
     uint64_t* h_pinned_ = nullptr;
 };

@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
     const uint32_t base = DIM_CAMERA_WALK + 4 * depth;
     // Block-uniform chunk loop (sort_chunk's barriers need every thread).
     const uint32_t per = chunk_per_thread<NT, PER>(n, gridDim.x);
-    const uint32_t chunk = NT * per;
+    const uint32_t chunk = chunk_entries<NT>(n, gridDim.x, per);
     for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
         const uint32_t cn = min(chunk, n - c0);
         sort_chunk<NT, PER>(sm, cn, per, [&](uint32_t i) {

@@ -66,6 +66,18 @@ GR_D uint32_t chunk_per_thread(uint32_t n, uint32_t blocks) {
     return per < 1 ? 1 : (per > PER ? PER : per);
 }
 
+// Entries per chunk for a queue of n entries over `blocks` blocks of NT threads taking
+// `per` entries per thread: NT * per, or, when the queue cannot give every block NT
+// entries (per == 1), a multiple of 32 that spreads it over all blocks, so a short queue
+// still runs on every SM.
+template <uint32_t NT>
+GR_D uint32_t chunk_entries(uint32_t n, uint32_t blocks, uint32_t per) {
+    if (per > 1) return NT * per;
+    uint32_t c = (n + blocks - 1) / blocks;
+    c = (c + 31u) & ~31u;
+    return c == 0 ? 32u : (c < NT ? c : NT);
+}
+
 // Sorts positions 0..cn-1 (cn <= NT * per, per <= PER) by bucket_of(i) < SORT_BUCKETS
 // into sm.order.  Every thread of an NT-thread block must call it with the same cn and
 // per.  It ends with a barrier; the caller needs one more before the next call reuses

@@ -109,6 +109,14 @@ constexpr int SMEM_STACK = 16;  // MAX_STACK (common.cuh): both builds reject de
 #define GR_EXTEND_REFILL 16
 #endif
 
+// The two arrays a traversal step reads.  A kernel whose lanes trace rays of different
+// scenes keeps one per lane in registers instead of reloading them through a scene
+// record at every step.
+struct TraceScene {
+    const float4* nodes;
+    const float4* prims;
+};
+
 struct TravState {
     V3 o, d, inv;
     float closest;
@@ -162,8 +170,8 @@ struct StackView {
 // distance, nearest last) and makes the nearest hit child the current reference.
 // Returns false when no child is hit.  A push beyond MAX_STACK sets *err = 1 and
 // `overflow`.
-template <int W, bool COUNT>
-GR_D bool visit_node(const DeviceScene& s, TravState& t, const StackView& stk, int* err, uint32_t* counts,
+template <int W, bool COUNT, class S>
+GR_D bool visit_node(const S& s, TravState& t, const StackView& stk, int* err, uint32_t* counts,
                      bool& overflow) {
     const float inflate = 1.0f + 2.0f * gamma_n(3.0f);
     if (COUNT) counts[0] += 1;
@@ -216,8 +224,8 @@ GR_D bool visit_node(const DeviceScene& s, TravState& t, const StackView& stk, i
 
 // Intersects the primitives of leaf `ref`, keeping the closest hit in t.  With ANY_HIT
 // it returns true at the first hit closer than t.closest.
-template <bool ANY_HIT, bool COUNT>
-GR_D bool visit_leaf(const DeviceScene& s, TravState& t, int32_t ref, uint32_t* counts) {
+template <bool ANY_HIT, bool COUNT, class S>
+GR_D bool visit_leaf(const S& s, TravState& t, int32_t ref, uint32_t* counts) {
     uint32_t enc = ~static_cast<uint32_t>(ref);
     uint32_t first = enc >> LEAF_COUNT_BITS;
     uint32_t count = (enc & (MAX_LEAF_PRIMS - 1)) + 1;
@@ -256,8 +264,9 @@ GR_D bool pop_next(TravState& t, const StackView& stk) {
 
 // One traversal step.  Returns true when the ray is finished (t.hit / t.closest hold
 // the closest hit).  With ANY_HIT it finishes at the first hit closer than t_max.
-template <int W, bool ANY_HIT, bool COUNT>
-GR_D bool trav_step(const DeviceScene& s, TravState& t, const StackView& stk, int* err, uint32_t* counts) {
+// S is DeviceScene or TraceScene: the step functions read only `nodes` and `prims`.
+template <int W, bool ANY_HIT, bool COUNT, class S>
+GR_D bool trav_step(const S& s, TravState& t, const StackView& stk, int* err, uint32_t* counts) {
     if (t.ref >= 0) {
         bool overflow = false;
         bool descended = visit_node<W, COUNT>(s, t, stk, err, counts, overflow);
