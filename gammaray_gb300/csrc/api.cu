@@ -374,17 +374,17 @@ gr_status gr_film_read_splat(const gr_film* f, float* splat) {
 
 gr_status gr_film_read(const gr_film* f, float* accum, float* weight) {
     if (!f) return fail(GR_ERR_INVALID_ARGUMENT, "null film");
-    size_t n = static_cast<size_t>(f->width) * f->height;
-    std::vector<float4> px(n);
-    GR_CUDA_TRY(cudaMemcpy(px.data(), f->pixels.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < n; ++i) {
-        if (accum) {
-            accum[3 * i] = px[i].x;
-            accum[3 * i + 1] = px[i].y;
-            accum[3 * i + 2] = px[i].z;
-        }
-        if (weight) weight[i] = px[i].w;
-    }
+    if (!accum && !weight) return GR_OK;
+    // The planes are split on the device and copied straight into the caller's arrays
+    // (a DMA transfer when the caller's memory is pinned).
+    const size_t n = static_cast<size_t>(f->width) * f->height;
+    GR_CUDA_TRY(f->readback.ensure(n * 4 * sizeof(float)));
+    float* acc_d = f->readback.as<float>();
+    float* w_d = acc_d + 3 * n;
+    GR_TRY(film_split(f->pixels.as<float4>(), static_cast<uint32_t>(n), acc_d, w_d, 0));
+    if (accum) GR_CUDA_TRY(cudaMemcpyAsync(accum, acc_d, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, 0));
+    if (weight) GR_CUDA_TRY(cudaMemcpyAsync(weight, w_d, n * sizeof(float), cudaMemcpyDeviceToHost, 0));
+    GR_CUDA_TRY(cudaStreamSynchronize(0));
     return GR_OK;
 }
 

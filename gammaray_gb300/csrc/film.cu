@@ -43,6 +43,18 @@ __global__ void k_resolve(const float4* __restrict__ film, const float4* __restr
     rgb[3 * i + 2] = v.z;
 }
 
+// Film::pixels as two planes: accum (3 floats per pixel) and weight (1 float per pixel).
+__global__ void k_film_split(const float4* __restrict__ film, uint32_t n, float* __restrict__ accum,
+                             float* __restrict__ weight) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = film[i];
+    accum[3 * i] = p.x;
+    accum[3 * i + 1] = p.y;
+    accum[3 * i + 2] = p.z;
+    weight[i] = p.w;
+}
+
 // ExrWriter::write_channels (render/exr.rs:138-166): per scanline y, the int32 line
 // number, the uint32 byte count and the B, G, R planes of film row height - y - 1.
 __global__ void k_exr_pack(const float4* __restrict__ film, const float4* __restrict__ splat, float scale,
@@ -79,6 +91,12 @@ gr_status film_gather(const float2* st, const float4* color, uint32_t width, uin
 gr_status film_resolve(const float4* film, const float4* splat, float splat_scale, uint32_t n, float* rgb,
                        cudaStream_t s) {
     k_resolve<<<(n + 255) / 256, 256, 0, s>>>(film, splat, splat_scale, n, rgb);
+    GR_CUDA_TRY(cudaGetLastError());
+    return GR_OK;
+}
+
+gr_status film_split(const float4* film, uint32_t n, float* accum, float* weight, cudaStream_t s) {
+    k_film_split<<<(n + 255) / 256, 256, 0, s>>>(film, n, accum, weight);
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }

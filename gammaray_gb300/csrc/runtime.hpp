@@ -134,6 +134,7 @@ struct gr_film {
     uint32_t width = 0, height = 0;
     gr::DevBuf pixels;  // float4 (accum.rgb, weight) per pixel
     gr::DevBuf splat;   // float4 light-tracing splat sums (BDPT extension); allocated on first use
+    mutable gr::DevBuf readback;  // accum and weight planes for gr_film_read (a cache); allocated on first use
     uint32_t passes = 0;
     int device = 0;
 };
@@ -182,6 +183,8 @@ gr_status film_gather(const float2* st_buf, const float4* color, uint32_t width,
 // Resolve and EXR packing add splat * splat_scale when splat is not null.
 gr_status film_resolve(const float4* film, const float4* splat, float splat_scale, uint32_t n, float* rgb,
                        cudaStream_t s);
+// Splits the float4 film into an accum plane (3 floats per pixel) and a weight plane.
+gr_status film_split(const float4* film, uint32_t n, float* accum, float* weight, cudaStream_t s);
 gr_status film_exr_pack(const float4* film, const float4* splat, float splat_scale, uint32_t width, uint32_t height,
                         unsigned char* out, size_t data_offset, cudaStream_t s);
 
