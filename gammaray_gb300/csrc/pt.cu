@@ -64,10 +64,21 @@ struct PTParams {
     uint32_t qcap;  // queue capacity (paths of the group)
 };
 
-__global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4* __restrict__ tp,
-                                                  float4* __restrict__ L, unsigned long long* __restrict__ key,
+// Path state travels with its ray in the queue, two float4 per queue entry:
+//   state[2q]     = (throughput.xyz, radiance.x)
+//   state[2q + 1] = (radiance.y, radiance.z, key low 32 bits, key high 32 bits)
+// Shading reads it where the entry sits and writes it where the surviving path is pushed
+// (consecutive positions per warp), instead of gathering and scattering slot-indexed
+// arrays at random.  A finished path writes its radiance to its slot (the index of its
+// film position), which the film gather reads.
+GR_D uint64_t state_key(float4 b) {
+    return (static_cast<uint64_t>(__float_as_uint(b.w)) << 32) | __float_as_uint(b.z);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4* __restrict__ L,
                                                   float2* __restrict__ st, uint32_t* __restrict__ q_slot,
-                                                  float4* __restrict__ q_o, float4* __restrict__ q_d) {
+                                                  float4* __restrict__ q_o, float4* __restrict__ q_d,
+                                                  float4* __restrict__ q_state) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t pass_local = i / p.npix;
@@ -79,15 +90,38 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
     film_sample_point(p.width, p.height, row, col, k, s, t);
     V3 o, d;
     camera_ray(p.cam, s, t, o, d);
-    tp[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    key[i] = k;
     st[i] = make_float2(s, t);
     q_slot[i] = i;
     q_o[i] = make_float4(o.x, o.y, o.z, 0.0f);
     q_d[i] = make_float4(d.x, d.y, d.z, 0.0f);
+    q_state[2 * static_cast<size_t>(i)] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    q_state[2 * static_cast<size_t>(i) + 1] = make_float4(0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(k)),
+                                                          __uint_as_float(static_cast<uint32_t>(k >> 32)));
 }
 
+// Appends this lane's surviving path (slot, ray, state) to the next queue with one atomic
+// per warp (ballot + popc).  Every lane of the warp must call it.
+GR_D void push_path(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, float4 sa, float4 sb,
+                    uint32_t* __restrict__ nslot, float4* __restrict__ no, float4* __restrict__ nd,
+                    float4* __restrict__ nstate, uint32_t cap) {
+    const unsigned lane = threadIdx.x & 31;
+    unsigned m = __ballot_sync(0xffffffffu, alive);
+    if (!m) return;
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == static_cast<unsigned>(leader)) base = atomicAdd(count_out, static_cast<uint32_t>(__popc(m)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (alive) {
+        uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
+        if (!GR_IN_RANGE(pos, cap)) return;
+        nslot[pos] = slot;
+        no[pos] = make_float4(o.x, o.y, o.z, 0.0f);
+        nd[pos] = make_float4(d.x, d.y, d.z, 0.0f);
+        nstate[2 * static_cast<size_t>(pos)] = sa;
+        nstate[2 * static_cast<size_t>(pos) + 1] = sb;
+    }
+}
 
 // Material-sorted shading (shade_sort.cuh): each block sorts its chunk of the queue by
 // code path (chosen lobe type, the material's lobe types), then shades it in that order.
@@ -97,10 +131,10 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
                                                  const uint32_t* __restrict__ count_in,
                                                  const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
                                                  const float4* __restrict__ q_d, const float4* __restrict__ q_hit,
-                                                 float4* __restrict__ tp_buf, float4* __restrict__ L_buf,
-                                                 const unsigned long long* __restrict__ key_buf, uint32_t* count_out,
-                                                 uint32_t* __restrict__ nslot, float4* __restrict__ no,
-                                                 float4* __restrict__ nd) {
+                                                 const float4* __restrict__ q_state, float4* __restrict__ L_buf,
+                                                 uint32_t* count_out, uint32_t* __restrict__ nslot,
+                                                 float4* __restrict__ no, float4* __restrict__ nd,
+                                                 float4* __restrict__ nstate) {
     extern __shared__ unsigned char dsmem[];
     constexpr uint32_t PER = shade_per<NT>();
     const SortView sm = sort_view<NT, PER>(dsmem);
@@ -113,22 +147,24 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
         const uint32_t cn = min(chunk, n - c0);
         sort_chunk<NT, PER>(sm, cn, per, [&](uint32_t i) {
             uint32_t q = c0 + i;
-            return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(key_buf[q_slot[q]], base), 0);
+            return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(state_key(q_state[2 * q + 1]), base), 0);
         });
-        // Every lane runs every step so that all of them reach the ballot in push_warp.
+        // Every lane runs every step so that all of them reach the ballot in push_path.
         for (uint32_t e = 0; e < per; ++e) {
             uint32_t i = e * NT + threadIdx.x;
             bool alive = false;
             uint32_t slot = 0;
             V3 new_o = v3zero(), new_d = v3zero();
+            float4 sa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sb = sa;
             if (i < cn) {
                 uint32_t q = c0 + sm.order[i];
                 slot = q_slot[q];
                 float4 h = q_hit[q];
                 float4 o4 = q_o[q], d4 = q_d[q];
                 V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
-                float4 tp4 = tp_buf[slot], L4 = L_buf[slot];
-                V3 tp = V3{tp4.x, tp4.y, tp4.z}, L = V3{L4.x, L4.y, L4.z};
+                sa = q_state[2 * static_cast<size_t>(q)];
+                sb = q_state[2 * static_cast<size_t>(q) + 1];
+                V3 tp = V3{sa.x, sa.y, sa.z}, L = V3{sa.w, sb.x, sb.y};
                 int32_t k = __float_as_int(h.y);
                 if (k < 0) {
                     if (s.has_env) L = L + mul(tp, V3{s.env[0], s.env[1], s.env[2]});
@@ -136,7 +172,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
                     uint32_t prim;
                     Frame f = hit_frame(s, k, o, d, h.x, h.z, h.w, prim);
                     const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
-                    uint64_t key = key_buf[slot];
+                    uint64_t key = state_key(sb);
                     MaterialSample ms = sample_world(m, -d, f, true, uniform01(key, base), uniform01(key, base + 1),
                                                      uniform01(key, base + 2));
                     L = L + mul(tp, ms.emission);
@@ -151,11 +187,15 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
                         tp = rv < prob ? tp / prob : v3zero();
                     }
                     alive = !is_zero(tp) && (p.max_depth == 0 || depth + 1 < p.max_depth);
-                    if (alive) tp_buf[slot] = make_float4(tp.x, tp.y, tp.z, 0.0f);
                 }
-                L_buf[slot] = make_float4(L.x, L.y, L.z, 0.0f);
+                if (alive) {
+                    sa = make_float4(tp.x, tp.y, tp.z, L.x);
+                    sb = make_float4(L.y, L.z, sb.z, sb.w);
+                } else {
+                    L_buf[slot] = make_float4(L.x, L.y, L.z, 0.0f);
+                }
             }
-            push_warp(alive, count_out, slot, new_o, new_d, nslot, no, nd, p.qcap);
+            push_path(alive, count_out, slot, new_o, new_d, sa, sb, nslot, no, nd, nstate, p.qcap);
         }
         __syncthreads();  // sm is reused by the next chunk
     }
@@ -224,14 +264,13 @@ cudaError_t PathState::ensure(size_t n) {
     cudaError_t e;
 #define GR_ENS(buf, bytes)                  \
     if ((e = (buf).ensure(bytes)) != cudaSuccess) return e;
-    GR_ENS(tp, n * sizeof(float4));
     GR_ENS(light, n * sizeof(float4));
-    GR_ENS(key, n * sizeof(unsigned long long));
     GR_ENS(st, n * sizeof(float2));
     for (int k = 0; k < 2; ++k) {
         GR_ENS(q_slot[k], n * sizeof(uint32_t));
         GR_ENS(q_o[k], n * sizeof(float4));
         GR_ENS(q_d[k], n * sizeof(float4));
+        GR_ENS(q_state[k], n * 2 * sizeof(float4));
     }
     GR_ENS(q_hit, n * sizeof(float4));
 #undef GR_ENS
@@ -304,10 +343,9 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         p.first_pass = rp.first_pass + done;
         GR_CUDA_TRY(cudaMemcpyAsync(cnt + CNT_QUEUE0, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
         uint32_t bound = n;  // an upper bound of the current queue length
-        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, ps.tp.as<float4>(), ps.light.as<float4>(),
-                                                            ps.key.as<unsigned long long>(), ps.st.as<float2>(),
+        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, ps.light.as<float4>(), ps.st.as<float2>(),
                                                             ps.q_slot[0].as<uint32_t>(), ps.q_o[0].as<float4>(),
-                                                            ps.q_d[0].as<float4>());
+                                                            ps.q_d[0].as<float4>(), ps.q_state[0].as<float4>());
         GR_CUDA_TRY(cudaGetLastError());
         ++launches;
         GR_TRY_S(sync_check(st, "raygen", 0, n));
@@ -339,9 +377,9 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             if (timed) GR_TRY_S(mark(e0));
             GR_TRY_S(launch_shade(bound, st, job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                   ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(),
-                                  ps.tp.as<float4>(), ps.light.as<float4>(), ps.key.as<unsigned long long>(),
-                                  cnt + nxt, ps.q_slot[nxt].as<uint32_t>(), ps.q_o[nxt].as<float4>(),
-                                  ps.q_d[nxt].as<float4>()));
+                                  ps.q_state[cur].as<float4>(), ps.light.as<float4>(), cnt + nxt,
+                                  ps.q_slot[nxt].as<uint32_t>(), ps.q_o[nxt].as<float4>(), ps.q_d[nxt].as<float4>(),
+                                  ps.q_state[nxt].as<float4>()));
             GR_CUDA_TRY(cudaGetLastError());
             ++launches;
             GR_TRY_S(sync_check(st, "shade", depth, n));
@@ -415,7 +453,7 @@ int device_sm_count() {
 //
 // Limits and sharing:
 //   - at most STATIC_MAX_PATHS (131072) pixels per image; larger sizes are rejected;
-//   - the array (STATIC_SCRATCH_BYTES, about 18 MB) is held by every GPU that loads the
+//   - the array (STATIC_SCRATCH_BYTES, about 23 MB) is held by every GPU that loads the
 //     library until the process exits;
 //   - every call uses the same array and it keeps the last call's contents (each call
 //     clears the counters it needs), so calls that overlap on the GPU (other threads,
@@ -431,9 +469,9 @@ namespace gr {
 namespace {
 
 constexpr uint32_t STATIC_MAX_PATHS = 1u << 17;
-// Per path: tp, light (float4), key (u64), st (float2), queue slot x2, queue o/d x2
-// (float4), hit (float4); plus a 256-byte block of counters.
-constexpr size_t STATIC_PER_PATH = 16 + 16 + 8 + 8 + 2 * 4 + 2 * 16 + 2 * 16 + 16;
+// Per path: light (float4), st (float2), queue slot x2, queue o/d x2 (float4), queue
+// state x2 (2 float4), hit (float4); plus a 256-byte block of counters.
+constexpr size_t STATIC_PER_PATH = 16 + 8 + 2 * 4 + 2 * 16 + 2 * 16 + 2 * 32 + 16;
 constexpr size_t STATIC_SCRATCH_BYTES = STATIC_MAX_PATHS * STATIC_PER_PATH + 256;
 
 static __device__ __align__(256) unsigned char g_static_scratch[STATIC_SCRATCH_BYTES];
@@ -517,9 +555,10 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
         off += bytes;
         return p;
     };
-    float4* tp = static_cast<float4*>(take(cap * sizeof(float4)));
     float4* light = static_cast<float4*>(take(cap * sizeof(float4)));
-    unsigned long long* key = static_cast<unsigned long long*>(take(cap * sizeof(unsigned long long)));
+    float4* q_state[2];
+    q_state[0] = static_cast<float4*>(take(cap * 2 * sizeof(float4)));
+    q_state[1] = static_cast<float4*>(take(cap * 2 * sizeof(float4)));
     float2* stb = static_cast<float2*>(take(cap * sizeof(float2)));
     float4* q_o[2];
     float4* q_d[2];
@@ -551,7 +590,7 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
         p.first_pass = rp->first_pass + pass;
         uint32_t n = npix;
         k_set_count<<<1, 1, 0, st>>>(cnt + CNT_QUEUE0, n);
-        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, tp, light, key, stb, q_slot[0], q_o[0], q_d[0]);
+        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, light, stb, q_slot[0], q_o[0], q_d[0], q_state[0]);
         GR_CUDA_TRY(cudaGetLastError());
         for (uint32_t depth = 0;; ++depth) {
             if (p.max_depth && depth >= p.max_depth) break;
@@ -566,8 +605,8 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
                 break;
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            GR_TRY_S(launch_shade(n, st, sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit, tp,
-                                  light, key, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt]));
+            GR_TRY_S(launch_shade(n, st, sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit,
+                                  q_state[cur], light, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt], q_state[nxt]));
             GR_CUDA_TRY(cudaGetLastError());
             if (p.max_depth == 0 && (depth & 3) == 3) {
                 // Unbounded (reference) depth: stop once no path is left.  The copy goes

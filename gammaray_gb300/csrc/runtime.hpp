@@ -70,8 +70,10 @@ struct DevBuf {
 
 // Path-tracer wavefront state, reused across renders of a scene (grown on demand).
 struct PathState {
-    DevBuf tp, light, key, st;                // per slot: throughput, radiance, random key, film (s, t)
-    DevBuf q_slot[2], q_o[2], q_d[2], q_hit;  // ping-pong queues of live slots and their rays
+    DevBuf light, st;  // per slot: final radiance, film (s, t)
+    // Ping-pong queues of live paths: slot, ray, and state (throughput, radiance so far,
+    // random key: two float4 per entry); one hit per entry.
+    DevBuf q_slot[2], q_o[2], q_d[2], q_state[2], q_hit;
     size_t capacity = 0;
     cudaError_t ensure(size_t n);
 };

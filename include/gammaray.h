@@ -284,7 +284,7 @@ gr_status gr_render_samples(gr_scene* scene, const gr_camera* camera,
  * No counterpart in the reference.  Runs the same path-tracer (or display-colour)
  * passes as gr_render on `stream` (a cudaStream_t, or 0) and accumulates them into
  * `film_dev`, caller-owned device memory of width * height float4 {accum.rgb, weight}.
- * Its scratch is one fixed array inside the library (about 18 MB, held by every GPU
+ * Its scratch is one fixed array inside the library (about 23 MB, held by every GPU
  * that loads the library until exit): at most 131072 pixels per image, larger images
  * are rejected with GR_ERR_INVALID_ARGUMENT.  All calls share that array and each
  * call clears the counters it uses, so calls that overlap on the GPU race: serialise
