@@ -2,8 +2,9 @@
 // (render/integrators.rs:42-100) and DisplayColorIntegrator (integrators.rs:18-34),
 // driven as Stage::trace passes (render/stage.rs:23-36).
 //
-// State lives in "slots", one per camera path (pass-local sample index); the rays of
-// live paths travel in a compacted queue:
+// Each camera path has a "slot" (pass-local sample index) holding its film position and,
+// once it ends, its radiance; while it lives, its ray and state (throughput, radiance so
+// far, random key) travel together in a compacted queue:
 //   raygen   one slot per pixel and pass: jitter (film.rs:55-76), camera ray
 //            (camera.rs:87-97), throughput 1, radiance 0
 //   extend   closest hit for every queued ray (wide BVH, shared-memory stack)
