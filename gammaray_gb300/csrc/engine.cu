@@ -24,19 +24,25 @@ static_assert(ESBLOCK == 128 || ESBLOCK == 768, "engine shading block of 128 or 
 constexpr uint32_t ESHADE_PER_THREAD = ESBLOCK == 128 ? SHADE_PER_THREAD : 85u;
 constexpr int GATHER_BLOCKS = 512;
 
-// Path state.  The queue entry of a live path carries its ray, its job (o.w) and its
-// depth (d.w).  Global path p (the paths of all units, in unit order) keeps its state in
-// ring slot p & (ring - 1):
-//   s_hot[2 * slot]     = (throughput.xyz, radiance.x); once finished (radiance.xyz, 0)
-//   s_hot[2 * slot + 1] = (radiance.y, radiance.z, key low 32 bits, key high 32 bits)
-//   s_cold[slot]        = (unit, 0, film s bits, film t bits)
-// The hot record is read and written at every bounce and holds the finished sample's
-// radiance in its first half; the cold record is written when the path starts.  The gather reads a
-// finished unit's samples straight from its slots, so a slot is reused only once the
-// unit of its previous path is gathered: paths are issued up to `ring` past the oldest
-// ungathered one.  At most `capacity` paths are live (the queues' size).
+// Path state.  The queue entry of a live path carries its ray, its job (o.w), its depth
+// (d.w) and its state, two float4:
+//   state[2q]     = (throughput.xyz, radiance.x)
+//   state[2q + 1] = (radiance.y, radiance.z, key low 32 bits, key high 32 bits)
+// read where the entry is shaded and written where the surviving path is pushed.  Global
+// path p (the paths of all units, in unit order) has ring slot p & (ring - 1):
+//   s_hot[slot]  = (radiance.xyz, 0), written when the path finishes
+//   s_cold[slot] = (unit, 0, film s bits, film t bits), written when it starts
+// The gather reads a finished unit's samples straight from its slots, so a slot is
+// reused only once the unit of its previous path is gathered: paths are issued up to
+// `ring` past the oldest ungathered one.  At most `capacity` paths are live (the queues'
+// size).
+GR_D uint64_t state_key(float4 b) {
+    return (static_cast<uint64_t>(__float_as_uint(b.w)) << 32) | __float_as_uint(b.z);
+}
+
 GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, uint32_t job, uint32_t depth,
-                   uint32_t* __restrict__ nslot, float4* __restrict__ no, float4* __restrict__ nd, uint32_t cap) {
+                   float4 sa, float4 sb, uint32_t* __restrict__ nslot, float4* __restrict__ no,
+                   float4* __restrict__ nd, float4* __restrict__ nstate, uint32_t cap) {
     const unsigned lane = threadIdx.x & 31;
     unsigned m = __ballot_sync(0xffffffffu, alive);
     if (!m) return;
@@ -50,6 +56,8 @@ GR_D void push_ray(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, u
         nslot[pos] = slot;
         no[pos] = make_float4(o.x, o.y, o.z, __uint_as_float(job));
         nd[pos] = make_float4(d.x, d.y, d.z, __uint_as_float(depth));
+        nstate[2 * static_cast<size_t>(pos)] = sa;
+        nstate[2 * static_cast<size_t>(pos) + 1] = sb;
     }
 }
 
@@ -144,7 +152,7 @@ struct RingSamples {
     uint32_t width, mask;
     GR_D void operator()(uint32_t r, uint32_t col, float2& st, V3& rgb) const {
         size_t slot = static_cast<size_t>((prefix + static_cast<unsigned long long>(r) * width + col) & mask);
-        float4 a = hot[2 * slot];  // (radiance, 0) of the finished path
+        float4 a = hot[slot];  // (radiance, 0) of the finished path
         uint4 cd = cold[slot];
         st = make_float2(__uint_as_float(cd.z), __uint_as_float(cd.w));
         rgb = V3{a.x, a.y, a.z};
@@ -182,9 +190,9 @@ __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const Engin
 // (no atomics).
 __global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob* __restrict__ jobs,
                                                      const DevUnit* __restrict__ units, uint32_t mask,
-                                                     float4* __restrict__ s_hot, uint4* __restrict__ s_cold,
-                                                     uint32_t* __restrict__ q_slot, float4* __restrict__ q_o,
-                                                     float4* __restrict__ q_d, uint32_t cap) {
+                                                     uint4* __restrict__ s_cold, uint32_t* __restrict__ q_slot,
+                                                     float4* __restrict__ q_o, float4* __restrict__ q_d,
+                                                     float4* __restrict__ q_state, uint32_t cap) {
     const uint32_t n = c->fill_n, qbase = c->fill_qbase;
     const unsigned long long base = c->fill_base;
     const uint32_t ulo = c->fill_ulo, uhi = c->fill_uhi + 1;
@@ -201,14 +209,15 @@ __global__ void __launch_bounds__(EBLOCK) k_eng_fill(EngineCtl* c, const DevJob*
         film_sample_point(J.width, J.height, row, col, key, s, t);
         V3 o, d;
         camera_ray(J.cam, s, t, o, d);
-        s_hot[2 * static_cast<size_t>(slot)] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        s_hot[2 * static_cast<size_t>(slot) + 1] = make_float4(
-            0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(key)), __uint_as_float(static_cast<uint32_t>(key >> 32)));
         s_cold[slot] = make_uint4(u, 0, __float_as_uint(s), __float_as_uint(t));
         if (!GR_IN_RANGE(qbase + i, cap)) continue;
-        q_slot[qbase + i] = slot;
-        q_o[qbase + i] = make_float4(o.x, o.y, o.z, __uint_as_float(U.job));
-        q_d[qbase + i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
+        const size_t qi = qbase + i;
+        q_slot[qi] = slot;
+        q_o[qi] = make_float4(o.x, o.y, o.z, __uint_as_float(U.job));
+        q_d[qi] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
+        q_state[2 * qi] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        q_state[2 * qi + 1] = make_float4(0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(key)),
+                                          __uint_as_float(static_cast<uint32_t>(key >> 32)));
     }
 }
 
@@ -291,9 +300,10 @@ __global__ void __launch_bounds__(BS) k_eng_extend_refill(EngineCtl* c, int cur,
 __global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
     k_eng_shade(EngineCtl* c, int cur, const DevJob* __restrict__ jobs, uint32_t* unit_done,
                 const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
-                const float4* __restrict__ q_d, const float4* __restrict__ q_hit, float4* __restrict__ s_hot,
-                const uint4* __restrict__ s_cold, uint32_t* __restrict__ nslot, float4* __restrict__ no,
-                float4* __restrict__ nd, uint32_t cap) {
+                const float4* __restrict__ q_d, const float4* __restrict__ q_hit,
+                const float4* __restrict__ q_state, float4* __restrict__ s_hot, const uint4* __restrict__ s_cold,
+                uint32_t* __restrict__ nslot, float4* __restrict__ no, float4* __restrict__ nd,
+                float4* __restrict__ nstate, uint32_t cap) {
     extern __shared__ unsigned char dsmem[];
     const SortView sm = sort_view<ESBLOCK, ESHADE_PER_THREAD>(dsmem);
     const int nxt = cur ^ 1;
@@ -312,8 +322,7 @@ __global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
             const DevJob& J = jobs[jb];
             int32_t k = __float_as_int(q_hit[q].y);
             if (!J.live || J.display || k < 0) return 0u;
-            float4 kb = s_hot[2 * static_cast<size_t>(q_slot[q]) + 1];
-            uint64_t key = (static_cast<uint64_t>(__float_as_uint(kb.w)) << 32) | __float_as_uint(kb.z);
+            uint64_t key = state_key(q_state[2 * static_cast<size_t>(q) + 1]);
             return shade_bucket(J.scene, k, uniform01(key, DIM_CAMERA_WALK + 4 * __float_as_uint(q_d[q].w)), 0);
         });
         for (uint32_t e = 0; e < per; ++e) {
@@ -321,6 +330,7 @@ __global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
             bool alive = false, finished = false;
             uint32_t slot = 0, job = 0, unit = 0xFFFFFFFFu, depth = 0;
             V3 new_o = v3zero(), new_d = v3zero();
+            float4 sa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sb = sa;
             if (i < cn) {
                 uint32_t q = c0 + sm.order[i];
                 slot = q_slot[q];
@@ -331,8 +341,7 @@ __global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
                 const DevJob& J = jobs[job];
                 const DeviceScene& s = J.scene;
                 V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
-                const size_t hs = 2 * static_cast<size_t>(slot);
-                float4 ha = s_hot[hs], hb = s_hot[hs + 1];
+                float4 ha = q_state[2 * static_cast<size_t>(q)], hb = q_state[2 * static_cast<size_t>(q) + 1];
                 V3 tp = V3{ha.x, ha.y, ha.z}, L = V3{ha.w, hb.x, hb.y};
                 int32_t k = __float_as_int(h.y);
                 if (!J.live) {
@@ -349,7 +358,7 @@ __global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
                     uint32_t prim;
                     Frame f = hit_frame(s, k, o, d, h.x, h.z, h.w, prim);
                     const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
-                    uint64_t key = (static_cast<uint64_t>(__float_as_uint(hb.w)) << 32) | __float_as_uint(hb.z);
+                    uint64_t key = state_key(hb);
                     uint32_t base = DIM_CAMERA_WALK + 4 * depth;
                     MaterialSample ms = sample_world(m, -d, f, true, uniform01(key, base), uniform01(key, base + 1),
                                                      uniform01(key, base + 2));
@@ -366,16 +375,14 @@ __global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
                     }
                     alive = !is_zero(tp) && (J.max_depth == 0 || depth + 1 < J.max_depth);
                 }
-                // A live path keeps (throughput, radiance, key); a finished one leaves its
-                // radiance in the first half, which with the cold record's film position
-                // is all the gather reads.
+                // A live path carries (throughput, radiance, key) to its next queue entry; a
+                // finished one leaves its radiance in its slot, which with the cold record's
+                // film position is all the gather reads.
                 if (alive) {
-                    s_hot[hs] = make_float4(tp.x, tp.y, tp.z, L.x);
-                    s_hot[hs + 1] = make_float4(L.y, L.z, hb.z, hb.w);
+                    sa = make_float4(tp.x, tp.y, tp.z, L.x);
+                    sb = make_float4(L.y, L.z, hb.z, hb.w);
                 } else {
-                    s_hot[hs] = make_float4(L.x, L.y, L.z, 0.0f);
-                }
-                if (!alive) {
+                    s_hot[slot] = make_float4(L.x, L.y, L.z, 0.0f);
                     finished = true;
                     unit = s_cold[slot].x;
                 }
@@ -388,7 +395,7 @@ __global__ void __launch_bounds__(ESBLOCK, 768 / ESBLOCK)
                 if (finished && lane == static_cast<unsigned>(__ffs(same) - 1))
                     atomicAdd(unit_done + unit, static_cast<uint32_t>(__popc(same)));
             }
-            push_ray(alive, &c->q[nxt], slot, new_o, new_d, job, depth + 1, nslot, no, nd, cap);
+            push_ray(alive, &c->q[nxt], slot, new_o, new_d, job, depth + 1, sa, sb, nslot, no, nd, nstate, cap);
         }
         __syncthreads();  // sm is reused by the next chunk
     }
@@ -470,12 +477,13 @@ gr_status Engine::init(const EngineConfig& cfg, cudaStream_t) {
     GR_CUDA_TRY(alloc(jobs_, ENGINE_MAX_JOBS * sizeof(DevJob)));
     GR_CUDA_TRY(alloc(units_, ENGINE_MAX_UNITS * sizeof(DevUnit)));
     GR_CUDA_TRY(alloc(unit_done_, ENGINE_MAX_UNITS * sizeof(uint32_t)));
-    GR_CUDA_TRY(alloc(s_hot_, static_cast<size_t>(ring_) * 32));
+    GR_CUDA_TRY(alloc(s_hot_, static_cast<size_t>(ring_) * 16));
     GR_CUDA_TRY(alloc(s_cold_, static_cast<size_t>(ring_) * 16));
     for (int k = 0; k < 2; ++k) {
         GR_CUDA_TRY(alloc(q_slot_[k], C * 4));
         GR_CUDA_TRY(alloc(q_o_[k], C * 16));
         GR_CUDA_TRY(alloc(q_d_[k], C * 16));
+        GR_CUDA_TRY(alloc(q_state_[k], C * 32));
     }
     GR_CUDA_TRY(alloc(q_hit_, C * 16));
     GR_CUDA_TRY(cudaMemsetAsync(ctl_.ptr, 0, sizeof(EngineCtl), st_));
@@ -497,8 +505,8 @@ gr_status Engine::enqueue_iteration(int cur) {
     GR_CUDA_TRY(cudaGetLastError());
     int fgrid = grid_for(reinterpret_cast<const void*>(k_eng_fill), EBLOCK, 0, C);
     k_eng_fill<<<fgrid, EBLOCK, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), ring_ - 1,
-                                          s_hot_.as<float4>(), s_cold_.as<uint4>(), q_slot_[cur].as<uint32_t>(),
-                                          q_o_[cur].as<float4>(), q_d_[cur].as<float4>(), C);
+                                          s_cold_.as<uint4>(), q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(),
+                                          q_d_[cur].as<float4>(), q_state_[cur].as<float4>(), C);
     GR_CUDA_TRY(cudaGetLastError());
     switch (cfg_.width) {
         case 2:
@@ -518,9 +526,9 @@ gr_status Engine::enqueue_iteration(int cur) {
     int sgrid = grid_for(reinterpret_cast<const void*>(k_eng_shade), ESBLOCK, ssmem, C);
     k_eng_shade<<<sgrid, ESBLOCK, ssmem, st_>>>(c, cur, jobs_.as<DevJob>(), unit_done_.as<uint32_t>(),
                                            q_slot_[cur].as<uint32_t>(), q_o_[cur].as<float4>(), q_d_[cur].as<float4>(),
-                                           q_hit_.as<float4>(), s_hot_.as<float4>(), s_cold_.as<uint4>(),
-                                           q_slot_[nxt].as<uint32_t>(), q_o_[nxt].as<float4>(),
-                                           q_d_[nxt].as<float4>(), C);
+                                           q_hit_.as<float4>(), q_state_[cur].as<float4>(), s_hot_.as<float4>(),
+                                           s_cold_.as<uint4>(), q_slot_[nxt].as<uint32_t>(), q_o_[nxt].as<float4>(),
+                                           q_d_[nxt].as<float4>(), q_state_[nxt].as<float4>(), C);
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }

@@ -125,7 +125,7 @@ class Engine {
     uint32_t ring_ = 0;
     DevBuf ctl_, jobs_, units_, unit_done_;
     DevBuf s_hot_, s_cold_;  // path state ring (see engine.cu)
-    DevBuf q_slot_[2], q_o_[2], q_d_[2], q_hit_;
+    DevBuf q_slot_[2], q_o_[2], q_d_[2], q_state_[2], q_hit_;
     std::vector<DevJob> h_jobs_;
     std::vector<DevUnit> h_units_;
     uint32_t jobs_cap_ = 0, units_cap_ = 0;
