@@ -359,13 +359,14 @@ def run_served(lib, n_req, rate, seed=11, target_rel_mse=1e-3, other_policy=True
     return out
 
 
-PROGRESSIVE_MAX_PASSES = 1024
+PROGRESSIVE_MAX_PASSES = 4096
 
 
 def run_progressive(lib, g, serve, stages, reqs, target):
-    """The same requests refined progressively: each stops at the first checkpoint (8, 16,
-    32, ... passes) whose half-film relMSE estimate is <= target, or at 1024 passes (the
-    drawn spp is not used here: relMSE, not a pass count, ends a request).  The plain comparator renders each request's final pass count with one
+    """The same requests refined progressively: each stops at the first checkpoint whose
+    half-film relMSE estimate is <= target (checkpoints after 8 passes, then where the
+    last estimate predicts the target), or at 4096 passes (the drawn spp is not used
+    here: relMSE, not a pass count, ends a request).  The plain comparator renders each request's final pass count with one
     gr_render, FIFO, as if it had known the count in advance."""
     srv = serve.Server(lib, max_active=16)
     ids, late = {}, {}

@@ -3,6 +3,7 @@
 // Stage::trace call (render/stage.rs:23-36).
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -267,7 +268,7 @@ struct ServerRequest {
     uint64_t bytes = 0;
     bool admitted = false;  // its job is in the engine
     // Progressive refinement: even passes go to `film` (job), odd passes to `film2`
-    // (job2); passes are appended up to `limit`, the next checkpoint (8, 16, 32, ...).
+    // (job2); passes are appended up to `limit`, the next checkpoint (next_checkpoint).
     bool progressive = false;
     DevBuf film2;
     uint32_t job2 = 0;
@@ -277,6 +278,21 @@ struct ServerRequest {
 };
 
 constexpr uint32_t FIRST_CHECKPOINT = 8;
+
+// The checkpoint after `done` passes of a progressive request whose error estimate `est`
+// is above `target`.  The estimate falls about as 1 / passes, so the next checkpoint is
+// the pass count expected to meet the target with a 10% margin, at least 1.25x and at
+// most 8x `done`, rounded up to a multiple of 8 (both half-films get whole passes) and
+// at most `cap` (the request's spp).  An infinite estimate takes the 8x step, a NaN one
+// the 1.25x step.
+uint32_t next_checkpoint(uint32_t done, float est, float target, uint32_t cap) {
+    double want = static_cast<double>(done) * static_cast<double>(est) / static_cast<double>(target) * 1.1;
+    const double lo = 1.25 * done, hi = 8.0 * done;
+    if (!(want >= lo)) want = lo;
+    if (want > hi) want = hi;
+    const uint64_t n = (static_cast<uint64_t>(std::ceil(want)) + 7) / 8 * 8;
+    return static_cast<uint32_t>(std::min<uint64_t>(n, cap));
+}
 // Aging of the shortest-remaining-work order.  On the saturated progressive serving
 // workload (24 requests, relMSE 1e-3) p50 / p95 / p99 latency measured 1540 / 4210 /
 // 5612 ms without aging, 1507 / 4120 / 4207 at 1000 ms and 1653 / 3693 / 4066 at 250 ms.
@@ -481,7 +497,7 @@ gr_status progress(gr_server* s) {
             st = half_film_rel_mse(s, *r, r->rel_mse);
             if (st != GR_OK) return st;
             if (!(r->rel_mse <= r->req.target_rel_mse) && r->limit < r->req.params.spp) {
-                r->limit = std::min(2 * r->limit, r->req.params.spp);
+                r->limit = next_checkpoint(r->limit, r->rel_mse, r->req.target_rel_mse, r->req.params.spp);
                 continue;
             }
         }

@@ -112,7 +112,7 @@ __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const 
         c->gather_group_first[g] = first;
         c->gather_group_tiles[g] = tiles;
         const DevJob& J = jobs[gjob[g]];
-        tiles += ((J.width + FILM_TILE - 1) / FILM_TILE) * ((J.height + FILM_TILE - 1) / FILM_TILE);
+        tiles += film_tiles_x(J.width) * film_tiles_y(J.height);
         first += c->gather_group_count[g];
     }
     uint32_t fill[GATHER_MAX];
@@ -159,7 +159,7 @@ struct RingSamples {
     }
 };
 
-__global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const EngineCtl* c, const DevJob* __restrict__ jobs,
+__global__ void __launch_bounds__(FILM_THREADS, 3) k_eng_gather(const EngineCtl* c, const DevJob* __restrict__ jobs,
                                                                     const DevUnit* __restrict__ units,
                                                                     const float4* __restrict__ s_hot,
                                                                     const uint4* __restrict__ s_cold, uint32_t mask) {
@@ -172,9 +172,9 @@ __global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_eng_gather(const Engin
         const uint32_t first = c->gather_group_first[g], cnt = c->gather_group_count[g];
         const DevJob& J = jobs[units[c->gather_units[first]].job];
         const uint32_t w = J.width, h = J.height;
-        const uint32_t tx = (w + FILM_TILE - 1) / FILM_TILE;
-        const int ox = static_cast<int>((t % tx) * FILM_TILE), oy = static_cast<int>((t / tx) * FILM_TILE);
-        const int x = ox + threadIdx.x % FILM_TILE, y = oy + threadIdx.x / FILM_TILE;
+        const uint32_t tx = film_tiles_x(w);
+        const int ox = static_cast<int>((t % tx) * FILM_TILE_W), oy = static_cast<int>((t / tx) * FILM_TILE_H);
+        const int x = ox + threadIdx.x % FILM_TILE_W, y = oy + threadIdx.x / FILM_TILE_W;
         const bool inside = x < static_cast<int>(w) && y < static_cast<int>(h);
         float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (inside) acc = J.film[static_cast<size_t>(y) * w + x];
@@ -500,7 +500,7 @@ gr_status Engine::enqueue_iteration(int cur) {
     const int nxt = cur ^ 1;
     k_eng_plan<<<1, 1, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), C, ring_, cur);
     GR_CUDA_TRY(cudaGetLastError());
-    k_eng_gather<<<GATHER_BLOCKS, FILM_TILE * FILM_TILE, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(),
+    k_eng_gather<<<GATHER_BLOCKS, FILM_THREADS, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(),
                                                                    s_hot_.as<float4>(), s_cold_.as<uint4>(), ring_ - 1);
     GR_CUDA_TRY(cudaGetLastError());
     int fgrid = grid_for(reinterpret_cast<const void*>(k_eng_fill), EBLOCK, 0, C);

@@ -7,12 +7,12 @@ namespace gr {
 
 namespace {
 
-__global__ void __launch_bounds__(FILM_TILE* FILM_TILE) k_film_gather(const float2* __restrict__ st,
-                                                                     const float4* __restrict__ color, uint32_t width,
-                                                                     uint32_t height, uint32_t passes, float4* film) {
+__global__ void __launch_bounds__(FILM_THREADS, 3) k_film_gather(const float2* __restrict__ st,
+                                                              const float4* __restrict__ color, uint32_t width,
+                                                              uint32_t height, uint32_t passes, float4* film) {
     __shared__ StagedSample sm;
-    const int ox = blockIdx.x * FILM_TILE, oy = blockIdx.y * FILM_TILE;
-    const int x = ox + threadIdx.x % FILM_TILE, y = oy + threadIdx.x / FILM_TILE;
+    const int ox = blockIdx.x * FILM_TILE_W, oy = blockIdx.y * FILM_TILE_H;
+    const int x = ox + threadIdx.x % FILM_TILE_W, y = oy + threadIdx.x / FILM_TILE_W;
     const bool inside = x < static_cast<int>(width) && y < static_cast<int>(height);
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (inside) acc = film[static_cast<size_t>(y) * width + x];
@@ -82,8 +82,8 @@ __global__ void k_exr_pack(const float4* __restrict__ film, const float4* __rest
 
 gr_status film_gather(const float2* st, const float4* color, uint32_t width, uint32_t height, uint32_t passes,
                       float4* film, cudaStream_t s) {
-    dim3 grid((width + FILM_TILE - 1) / FILM_TILE, (height + FILM_TILE - 1) / FILM_TILE);
-    k_film_gather<<<grid, FILM_TILE * FILM_TILE, 0, s>>>(st, color, width, height, passes, film);
+    dim3 grid(film_tiles_x(width), film_tiles_y(height));
+    k_film_gather<<<grid, FILM_THREADS, 0, s>>>(st, color, width, height, passes, film);
     GR_CUDA_TRY(cudaGetLastError());
     return GR_OK;
 }

@@ -2,21 +2,39 @@
 //
 // Film::report_samples (render/film.rs:78-114) splats each sample, serially and in
 // sample order, over the pixels within 2 px of its jittered position with a Mitchell
-// weight.  Samples are jittered at most 2 px from their own pixel, so a pixel only
-// receives samples from pixels at most 4 away.  gather_tile gives each thread one
-// destination pixel; a 16x16 tile stages the samples of its 24x24 neighbourhood
-// (footprint precomputed) in shared memory, and every pixel adds its contributors in
-// increasing sample index (rows, then columns).  That is the order of the reference's
-// serial loop, so the sums are bit-identical to it, with no atomics.
+// weight.  Samples are jittered less than 2 px from their own pixel centre (the camera
+// jitter of film_sample_point), so a sample covers at most 5 consecutive columns and 5
+// consecutive rows, all within 4 px of its own pixel.
+//
+// gather_passes gives each thread one destination pixel of a 24x16 tile.  Per pass, the
+// block stages the samples of the tile's 32x24 neighbourhood (the tile and 4 px of halo)
+// in shared memory, one warp per neighbourhood row and one lane per column; then every
+// pixel adds its contributors in increasing sample index (rows, then columns).  That is
+// the order of the reference's serial loop, so the sums are bit-identical to it, with
+// no atomics.
 #pragma once
 
 #include "common.cuh"
 
 namespace gr {
 
-constexpr int FILM_TILE = 16;
+constexpr int FILM_TILE_W = 24;
+constexpr int FILM_TILE_H = 16;
 constexpr int FILM_HALO = 4;
-constexpr int FILM_SPAN = FILM_TILE + 2 * FILM_HALO;  // 24
+constexpr int FILM_SPAN_W = FILM_TILE_W + 2 * FILM_HALO;  // 32: one lane per neighbourhood column
+constexpr int FILM_SPAN_H = FILM_TILE_H + 2 * FILM_HALO;  // 24
+constexpr int FILM_SPAN_N = FILM_SPAN_W * FILM_SPAN_H;
+constexpr int FILM_THREADS = FILM_TILE_W * FILM_TILE_H;  // 384, one per tile pixel
+constexpr int FILM_WARPS = FILM_THREADS / 32;
+constexpr int FILM_ROWS_PER_WARP = FILM_SPAN_H / FILM_WARPS;  // 2
+constexpr int FILM_WIN = 2 * FILM_HALO + 1;                   // 9 candidate rows and columns per pixel
+constexpr int FILM_FOOT = 5;                                  // columns (rows) one sample covers, at most
+static_assert(FILM_SPAN_W == 32 && FILM_THREADS % 32 == 0 && FILM_SPAN_H % FILM_WARPS == 0,
+              "one warp per neighbourhood row, the rows shared evenly");
+
+// Film tiles of a width x height image.
+GR_HD uint32_t film_tiles_x(uint32_t width) { return (width + FILM_TILE_W - 1) / FILM_TILE_W; }
+GR_HD uint32_t film_tiles_y(uint32_t height) { return (height + FILM_TILE_H - 1) / FILM_TILE_H; }
 
 // core/math.rs:92-123 (B = C = 1/3)
 GR_D float mitchell1(float x) {
@@ -33,126 +51,137 @@ GR_D float mitchell1(float x) {
            (1.0f / 6.0f);
 }
 
-// A tile's staged samples (structure of arrays, FILM_SPAN^2 of them) and, per tile pixel,
-// an 81-bit mask of the samples in its 9x9 neighbourhood whose footprint covers it (bit
-// dy * 9 + dx for the sample dy rows and dx columns below / right of the neighbourhood's
-// corner).  Visiting set bits in increasing order is visiting contributors in
-// increasing sample index, the reference's order.
-constexpr int FILM_WIN = 2 * FILM_HALO + 1;                      // 9
-constexpr int FILM_MASK_WORDS = (FILM_WIN * FILM_WIN + 31) / 32;  // 3
-// A sample's footprint spans at most 5 columns and 5 rows (film.rs:90-97); its Mitchell
-// factors for the tile columns and rows it covers are evaluated once when it is staged:
-// mx[j][k] = mitchell1((cb + j - col_discr) / 2) for tile column cb + j, and my likewise,
-// so a pixel's weight is mx * my, the reference's product of the same two factors.
-constexpr int FILM_FOOT = 5;
+// A tile's staged samples, sample k = row * 32 + column of the neighbourhood:
+//   color[k]             its radiance (w unused)
+//   mx[t % 5][k]         mitchell1((ox + t - col_discr) / 2) for each tile column t it
+//                        covers; its at most 5 consecutive columns have distinct t % 5
+//   my[t % 5][k]         likewise for the tile rows t it covers
+//   colmask[row][t]      bit c set when sample (row, c) covers tile column t
+//   rowmask[row][t]      bit c set when sample (row, c) covers tile row t
+// so sample (row, c) covers pixel (tx, ty) when bit c is set in
+// colmask[row][tx] & rowmask[row][ty], and its weight there is mx[tx % 5] * my[ty % 5]:
+// the reference's product of the same two factors.
 struct StagedSample {
-    float r[FILM_SPAN * FILM_SPAN], g[FILM_SPAN * FILM_SPAN], b[FILM_SPAN * FILM_SPAN];
-    float mx[FILM_FOOT][FILM_SPAN * FILM_SPAN], my[FILM_FOOT][FILM_SPAN * FILM_SPAN];
-    uint8_t cb[FILM_SPAN * FILM_SPAN], rb[FILM_SPAN * FILM_SPAN];  // first covered tile column / row
-    uint32_t mask[FILM_TILE * FILM_TILE][FILM_MASK_WORDS];
+    float4 color[FILM_SPAN_N];
+    float mx[FILM_FOOT][FILM_SPAN_N], my[FILM_FOOT][FILM_SPAN_N];
+    uint32_t colmask[FILM_SPAN_H][FILM_TILE_W], rowmask[FILM_SPAN_H][FILM_TILE_H];
 };
+
+// Transposes the 32x32 bit matrix whose row i (bit j = column j) lane i holds: returns
+// column `lane` (bit i = row i's bit `lane`).  Recursive block swap: at stride s the
+// two s x s blocks off the diagonal of every 2s x 2s block trade places between lanes
+// s apart, then the blocks are transposed at stride s / 2.
+GR_D uint32_t transpose32(uint32_t x, unsigned lane) {
+    const uint32_t m[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const int s = 16 >> i;
+        uint32_t y = __shfl_xor_sync(0xffffffffu, x, s);
+        x = (lane & s) ? ((x & ~m[i]) | ((y >> s) & m[i])) : ((x & m[i]) | ((y & m[i]) << s));
+    }
+    return x;
+}
 
 // Adds the samples of `npass` passes, in pass order, to the tile (ox, oy) of `film`.
 // src_at(k) gives pass k's sample source: src(row, col, st, rgb) loads that pixel's
-// sample, its film position (s, t) and its radiance.  Every thread of the block (256 =
-// FILM_TILE^2) must call it; `sm` is the block's staging area.
+// sample, its film position (s, t) and its radiance.  Every thread of the block
+// (FILM_THREADS) must call it; `sm` is the block's staging area.
 //
-// Per pass: each thread stages up to three samples (film.rs:82-97: continuous position,
-// footprint) and sets their bit in the mask of every tile pixel their footprint covers;
-// then each pixel adds its contributors, set bits in increasing order, with the Mitchell
-// weight of film.rs:100-106.  The footprint is the reference's, clamped to the image
-// the same way (film.rs:90-97).
+// Per pass: each lane stages its column's sample in the warp's neighbourhood rows
+// (film.rs:82-97: continuous position, footprint clamped to the image as the reference
+// clamps it), evaluates the Mitchell factors of the tile columns and rows the footprint
+// covers (film.rs:100-106, the arguments as the reference's pixel loop forms them), and
+// the warp transposes its lanes' coverage bits into the row's column and row masks.
+// Then each pixel adds its contributors, rows then columns in increasing order, which
+// is increasing sample index.
 //
 // Software-pipelined: the global loads of pass k + 1 are issued into registers before
 // pass k is accumulated.  The additions per pixel are the reference's: pass by pass,
 // then in increasing sample index.
-constexpr int FILM_STAGE_PER_THREAD = (FILM_SPAN * FILM_SPAN + FILM_TILE * FILM_TILE - 1) / (FILM_TILE * FILM_TILE);
-
 template <class SrcAt>
 GR_D void gather_passes(StagedSample& sm, uint32_t width, uint32_t height, int ox, int oy, float4& acc,
                         uint32_t npass, const SrcAt& src_at) {
-    const int tx = threadIdx.x % FILM_TILE, ty = threadIdx.x / FILM_TILE;
-    const int x = ox + tx, y = oy + ty;
-    const bool inside = x < static_cast<int>(width) && y < static_cast<int>(height);
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const int tx = static_cast<int>(threadIdx.x) % FILM_TILE_W, ty = static_cast<int>(threadIdx.x) / FILM_TILE_W;
+    const bool inside = ox + tx < static_cast<int>(width) && oy + ty < static_cast<int>(height);
     const float wf = static_cast<float>(width), hf = static_cast<float>(height);
     const long long last_col = static_cast<long long>(width) - 1, last_row = static_cast<long long>(height) - 1;
-    float2 rs[FILM_STAGE_PER_THREAD];
-    V3 rc[FILM_STAGE_PER_THREAD];
+    const int scol = ox - FILM_HALO + static_cast<int>(lane);  // this lane's image column
+    const bool col_in = scol >= 0 && scol < static_cast<int>(width);
+    const float* mxs = sm.mx[tx % FILM_FOOT];
+    const float* mys = sm.my[ty % FILM_FOOT];
+    float2 rs[FILM_ROWS_PER_WARP];
+    V3 rc[FILM_ROWS_PER_WARP];
     auto load = [&](uint32_t pass) {
         const auto src = src_at(pass);
 #pragma unroll
-        for (int j = 0; j < FILM_STAGE_PER_THREAD; ++j) {
-            int k = threadIdx.x + j * FILM_TILE * FILM_TILE;
-            int sr = oy - FILM_HALO + k / FILM_SPAN, sc = ox - FILM_HALO + k % FILM_SPAN;
-            if (k < FILM_SPAN * FILM_SPAN && sr >= 0 && sc >= 0 && sr < static_cast<int>(height) &&
-                sc < static_cast<int>(width))
-                src(static_cast<uint32_t>(sr), static_cast<uint32_t>(sc), rs[j], rc[j]);
+        for (int j = 0; j < FILM_ROWS_PER_WARP; ++j) {
+            int srow = oy - FILM_HALO + static_cast<int>(warp) + j * FILM_WARPS;
+            if (col_in && srow >= 0 && srow < static_cast<int>(height))
+                src(static_cast<uint32_t>(srow), static_cast<uint32_t>(scol), rs[j], rc[j]);
         }
     };
     if (npass) load(0);
     for (uint32_t pass = 0; pass < npass; ++pass) {
         __syncthreads();  // the previous pass's accumulation is done with sm
 #pragma unroll
-        for (int w = 0; w < FILM_MASK_WORDS; ++w) sm.mask[threadIdx.x][w] = 0u;
-        __syncthreads();
+        for (int j = 0; j < FILM_ROWS_PER_WARP; ++j) {
+            const int row = static_cast<int>(warp) + j * FILM_WARPS;
+            const int srow = oy - FILM_HALO + row;
+            const int k = row * FILM_SPAN_W + static_cast<int>(lane);
+            uint32_t cm = 0u, rm = 0u;  // tile columns / rows this sample covers
+            if (col_in && srow >= 0 && srow < static_cast<int>(height)) {
+                float2 s = rs[j];
+                // film.rs:82-97
+                float col_cont = lerp(0.0f, wf, 0.5f * (s.x + 1.0f));
+                float row_cont = lerp(0.0f, hf, 0.5f * (s.y + 1.0f));
+                float cd = col_cont - 0.5f, rd = row_cont - 0.5f;
+                long long mnc = static_cast<long long>(ceilf(cd - 2.0f));
+                long long mxc = static_cast<long long>(floorf(cd + 2.0f));
+                long long mnr = static_cast<long long>(ceilf(rd - 2.0f));
+                long long mxr = static_cast<long long>(floorf(rd + 2.0f));
+                mnc = mnc < 0 ? 0 : (mnc > last_col ? last_col : mnc);
+                mxc = mxc < 0 ? 0 : (mxc > last_col ? last_col : mxc);
+                mnr = mnr < 0 ? 0 : (mnr > last_row ? last_row : mnr);
+                mxr = mxr < 0 ? 0 : (mxr > last_row ? last_row : mxr);
+                int c0 = max(0, static_cast<int>(mnc) - ox), c1 = min(FILM_TILE_W - 1, static_cast<int>(mxc) - ox);
+                int r0 = max(0, static_cast<int>(mnr) - oy), r1 = min(FILM_TILE_H - 1, static_cast<int>(mxr) - oy);
+                if (c0 <= c1 && r0 <= r1) {
+                    sm.color[k] = make_float4(rc[j].x, rc[j].y, rc[j].z, 0.0f);
 #pragma unroll
-        for (int j = 0; j < FILM_STAGE_PER_THREAD; ++j) {
-            int k = threadIdx.x + j * FILM_TILE * FILM_TILE;
-            if (k >= FILM_SPAN * FILM_SPAN) break;
-            int ky = k / FILM_SPAN, kx = k % FILM_SPAN;
-            int sr = oy - FILM_HALO + ky, sc = ox - FILM_HALO + kx;
-            if (sr < 0 || sc < 0 || sr >= static_cast<int>(height) || sc >= static_cast<int>(width)) continue;
-            float2 s = rs[j];
-            // film.rs:82-97
-            float col_cont = lerp(0.0f, wf, 0.5f * (s.x + 1.0f));
-            float row_cont = lerp(0.0f, hf, 0.5f * (s.y + 1.0f));
-            float cd = col_cont - 0.5f, rd = row_cont - 0.5f;
-            sm.r[k] = rc[j].x;
-            sm.g[k] = rc[j].y;
-            sm.b[k] = rc[j].z;
-            // Footprint (film.rs:90-97), then the tile pixels it covers; footprints never
-            // exceed +-4 px of the source pixel.
-            long long mnc = static_cast<long long>(ceilf(cd - 2.0f));
-            long long mxc = static_cast<long long>(floorf(cd + 2.0f));
-            long long mnr = static_cast<long long>(ceilf(rd - 2.0f));
-            long long mxr = static_cast<long long>(floorf(rd + 2.0f));
-            mnc = mnc < 0 ? 0 : (mnc > last_col ? last_col : mnc);
-            mxc = mxc < 0 ? 0 : (mxc > last_col ? last_col : mxc);
-            mnr = mnr < 0 ? 0 : (mnr > last_row ? last_row : mnr);
-            mxr = mxr < 0 ? 0 : (mxr > last_row ? last_row : mxr);
-            int c0 = max(0, static_cast<int>(mnc) - ox), c1 = min(FILM_TILE - 1, static_cast<int>(mxc) - ox);
-            int r0 = max(0, static_cast<int>(mnr) - oy), r1 = min(FILM_TILE - 1, static_cast<int>(mxr) - oy);
-            if (c0 > c1 || r0 > r1) continue;  // covers no pixel of this tile
-            sm.cb[k] = static_cast<uint8_t>(c0);
-            sm.rb[k] = static_cast<uint8_t>(r0);
-            // film.rs:100-106 factors, the arguments as the pixel loop below forms them
+                    for (int f = 0; f < FILM_FOOT; ++f) {
+                        int t = c0 + f;
+                        if (t <= c1) sm.mx[t % FILM_FOOT][k] = mitchell1((static_cast<float>(ox + t) - cd) / 2.0f);
+                    }
 #pragma unroll
-            for (int f = 0; f < FILM_FOOT; ++f)
-                if (f <= c1 - c0) sm.mx[f][k] = mitchell1((static_cast<float>(ox + c0 + f) - cd) / 2.0f);
-#pragma unroll
-            for (int f = 0; f < FILM_FOOT; ++f)
-                if (f <= r1 - r0) sm.my[f][k] = mitchell1((static_cast<float>(oy + r0 + f) - rd) / 2.0f);
-            for (int py = r0; py <= r1; ++py)
-                for (int px = c0; px <= c1; ++px) {
-                    int bit = (ky - py) * FILM_WIN + (kx - px);
-                    atomicOr(&sm.mask[py * FILM_TILE + px][bit >> 5], 1u << (bit & 31));
+                    for (int f = 0; f < FILM_FOOT; ++f) {
+                        int t = r0 + f;
+                        if (t <= r1) sm.my[t % FILM_FOOT][k] = mitchell1((static_cast<float>(oy + t) - rd) / 2.0f);
+                    }
+                    cm = (2u << c1) - (1u << c0);
+                    rm = (2u << r1) - (1u << r0);
                 }
+            }
+            const uint32_t xc = transpose32(cm, lane), yc = transpose32(rm, lane);
+            if (lane < static_cast<unsigned>(FILM_TILE_W)) sm.colmask[row][lane] = xc;
+            if (lane < static_cast<unsigned>(FILM_TILE_H)) sm.rowmask[row][lane] = yc;
         }
         __syncthreads();
         if (pass + 1 < npass) load(pass + 1);  // in flight while this pass accumulates
         if (!inside) continue;
 #pragma unroll
-        for (int w = 0; w < FILM_MASK_WORDS; ++w) {
-            uint32_t m = sm.mask[threadIdx.x][w];
+        for (int dy = 0; dy < FILM_WIN; ++dy) {
+            const int row = ty + dy;
+            // candidates: columns tx .. tx + 8 of the row (footprints reach 4 px)
+            uint32_t m = ((sm.colmask[row][tx] & sm.rowmask[row][ty]) >> tx) & ((1u << FILM_WIN) - 1u);
             while (m) {
-                int bit = w * 32 + __ffs(m) - 1;
+                const int k = row * FILM_SPAN_W + tx + __ffs(m) - 1;
                 m &= m - 1;
-                int dy = bit / FILM_WIN, dx = bit - dy * FILM_WIN;
-                int k = (ty + dy) * FILM_SPAN + (tx + dx);
-                float wgt = sm.mx[tx - sm.cb[k]][k] * sm.my[ty - sm.rb[k]][k];
-                acc.x = acc.x + sm.r[k] * wgt;
-                acc.y = acc.y + sm.g[k] * wgt;
-                acc.z = acc.z + sm.b[k] * wgt;
+                const float4 c = sm.color[k];
+                const float wgt = mxs[k] * mys[k];
+                acc.x = acc.x + c.x * wgt;
+                acc.y = acc.y + c.y * wgt;
+                acc.z = acc.z + c.z * wgt;
                 acc.w += wgt;
             }
         }

@@ -465,8 +465,10 @@ typedef struct gr_request {
     /* Progressive refinement (serving extension).  0: render exactly params.spp passes.
      * > 0: render passes until the estimated relative MSE of the image falls to this
      * target, at most params.spp passes.  The estimate compares two half-images (even and
-     * odd passes): relMSE ~ sum |a - b|^2 / 4 / sum |(a + b) / 2|^2.  It is taken after 8,
-     * 16, 32, ... passes, so the pass count, and the image, depend on the request alone. */
+     * odd passes): relMSE ~ sum |a - b|^2 / 4 / sum |(a + b) / 2|^2.  It is taken after 8
+     * passes, then at the pass count the last estimate predicts will meet the target
+     * (estimate ~ 1 / passes, 10% margin; 1.25x to 8x the passes so far, a multiple of 8),
+     * so the pass count, and the image, depend on the request alone. */
     float target_rel_mse;
     uint32_t reserved;
 } gr_request;

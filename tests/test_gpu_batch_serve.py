@@ -1,6 +1,8 @@
 """Batched rendering and the serving loop on the GPU, against the per-image render."""
 from __future__ import annotations
 
+import math
+
 import numpy as np
 import pytest
 
@@ -206,13 +208,31 @@ def test_server_progressive_stops_at_a_checkpoint(gpu):
     np.testing.assert_allclose(wt, fa[1] + fb[1], rtol=1e-6, atol=1e-7)
 
 
+def next_checkpoint(done, est, target, cap):
+    """The server's checkpoint rule (batch.cu next_checkpoint), restated: the pass count
+    at which an estimate falling as 1 / passes meets the target with a 10% margin, within
+    1.25x to 8x the passes so far, rounded up to a multiple of 8, at most cap."""
+    want = done * float(np.float32(est)) / float(np.float32(target)) * 1.1
+    want = min(max(want, 1.25 * done), 8.0 * done)
+    return min((math.ceil(want) + 7) // 8 * 8, cap)
+
+
 def test_server_progressive_target_and_mix(gpu):
     ws = small_workloads(3, seed=12)
     stages = [g.Stage(w.prims, lib=gpu, environment=w.environment, seed=k) for k, w in enumerate(ws)]
     w0 = ws[0]
-    est = {n: rel_mse_estimate(*half_films(stages[0], w0, n, gpu)) for n in (8, 16, 32, 64)}
-    target = est[32] * 1.01  # met at 32 passes at the latest
-    want = min(n for n in est if est[n] <= target)
+    cache = {}
+
+    def est(n):
+        if n not in cache:
+            cache[n] = rel_mse_estimate(*half_films(stages[0], w0, n, gpu))
+        return cache[n]
+
+    target = est(32) * 1.01  # met by 64 passes
+    want = 8  # the checkpoints the server visits, replayed on the same estimates
+    while est(want) > target and want < 64:
+        want = next_checkpoint(want, est(want), target, 64)
+    assert want > 8
     alone = serve.Server(gpu, path_capacity=1 << 16)
     rid = alone.submit(stages[0], w0.camera, w0.integrator, w0.width, w0.height, 64, target_rel_mse=target)
     alone.run_until_done([rid])
