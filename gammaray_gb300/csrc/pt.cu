@@ -35,6 +35,10 @@ namespace gr {
 
 namespace {
 
+// Writes a group's starting queue length (the copy from a host variable it replaces
+// would stage through pageable memory).
+__global__ void k_set_count(uint32_t* c, uint32_t n) { *c = n; }
+
 // Threads per block of the path tracer's shading kernel, each block sorting its chunk of
 // the queue by code path.  With larger blocks, fewer blocks share an SM, so more of its
 // warps run the same code path at a time; the register cap (85) and the warps per SM
@@ -292,20 +296,10 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     uint32_t* cnt = sc->counters.as<uint32_t>();
     int* err = reinterpret_cast<int*>(cnt + CNT_ERROR);
     unsigned long long* rays = reinterpret_cast<unsigned long long*>(cnt + CNT_RAYS);
-    uint32_t* host_cnt = nullptr;
-    GR_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&host_cnt), 4 * sizeof(uint32_t), cudaHostAllocDefault));
-    struct Free {
-        uint32_t* p;
-        ~Free() { cudaFreeHost(p); }
-    } free_host{host_cnt};
-    cudaEvent_t evs[4];
-    for (auto& e : evs) GR_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    struct FreeEv {
-        cudaEvent_t* e;
-        ~FreeEv() {
-            for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
-        }
-    } free_ev{evs};
+    BounceReadback& rb = device_work().readback;  // the caller holds device_work().mu
+    GR_CUDA_TRY(rb.ensure());
+    uint32_t* host_cnt = rb.host;
+    cudaEvent_t* evs = rb.ev;
 
     // Optional per-kernel timing: one event pair per extend / shade launch.
     const bool timed = (rp.flags & GR_RENDER_TIME_KERNELS) != 0;
@@ -342,7 +336,8 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         uint32_t g = std::min(group, total - done);
         uint32_t n = g * npix;
         p.first_pass = rp.first_pass + done;
-        GR_CUDA_TRY(cudaMemcpyAsync(cnt + CNT_QUEUE0, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        k_set_count<<<1, 1, 0, st>>>(cnt + CNT_QUEUE0, n);
+        GR_CUDA_TRY(cudaGetLastError());
         uint32_t bound = n;  // an upper bound of the current queue length
         k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, ps.light.as<float4>(), ps.st.as<float2>(),
                                                             ps.q_slot[0].as<uint32_t>(), ps.q_o[0].as<float4>(),
@@ -476,10 +471,6 @@ constexpr size_t STATIC_PER_PATH = 16 + 8 + 2 * 4 + 2 * 16 + 2 * 16 + 2 * 32 + 1
 constexpr size_t STATIC_SCRATCH_BYTES = STATIC_MAX_PATHS * STATIC_PER_PATH + 256;
 
 static __device__ __align__(256) unsigned char g_static_scratch[STATIC_SCRATCH_BYTES];
-
-// Writes a pass's starting queue length (the copy from a host variable it replaces
-// would stage through pageable memory).
-__global__ void k_set_count(uint32_t* c, uint32_t n) { *c = n; }
 
 constexpr int STATIC_MAX_DEVICES = 64;
 std::mutex g_static_mu;

@@ -90,10 +90,28 @@ struct BdptState {
 
 // The large wavefront buffers are shared by every scene on a device (renders on one
 // GPU run one after another anyway); a scene keeps only its small counter block.
+// The path tracer's view of its queue lengths: a pinned copy of the last four bounces'
+// counts and an event after each copy.  Made once per device and kept (freeing pinned
+// memory synchronises the device), so a render starts without host allocations.
+struct BounceReadback {
+    uint32_t* host = nullptr;
+    cudaEvent_t ev[4] = {};
+    cudaError_t ensure() {
+        if (host) return cudaSuccess;
+        for (cudaEvent_t& e : ev) {
+            if (e) continue;
+            cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+            if (r != cudaSuccess) return r;
+        }
+        return cudaHostAlloc(reinterpret_cast<void**>(&host), 4 * sizeof(uint32_t), cudaHostAllocDefault);
+    }
+};
+
 struct DeviceWork {
     std::mutex mu;
     PathState paths;
     BdptState bdpt;
+    BounceReadback readback;
 };
 DeviceWork& device_work();  // of the current device
 
