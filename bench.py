@@ -457,6 +457,7 @@ def run_ours(args, rank, world, local):
             torch.distributed.barrier()
 
     dev_ms, ext_ms, ext_launch, rays, launches, shade_ms = [], 0.0, 0, 0, 0, 0.0
+    raygen_ms, film_ms = 0.0, 0.0
     barrier()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
@@ -467,6 +468,8 @@ def run_ours(args, rank, world, local):
             dev_ms.append(s.device_ms)
             ext_ms += s.extend_ms
             shade_ms += s.shade_ms
+            raygen_ms += s.raygen_ms
+            film_ms += s.film_ms
             ext_launch += s.extend_launches
             rays += s.extension_rays
             launches += s.kernel_launches
@@ -546,6 +549,11 @@ def run_ours(args, rank, world, local):
                 "extend_share_of_device_time": ext_ms / total_ms if total_ms else None,
                 "shade_share_of_device_time": shade_ms / total_ms if total_ms else None,
                 "extend_ms_per_launch": ext_ms / max(1, ext_launch)}
+    # Where a render's device time goes (CUDA events on the render stream, per render):
+    # the rest is queue-length copies, counter resets and launch gaps between kernels.
+    per = float(args.steps)
+    breakdown = {"extend": ext_ms / per, "shade": shade_ms / per, "raygen": raygen_ms / per, "film": film_ms / per}
+    breakdown["between_launches"] = sum(dev_ms) / per - sum(breakdown.values())
     # DRAM traffic of k_extend per launch: the captured bytes per ray (see
     # EXTEND_DRAM_BYTES_PER_RAY) times the rays of an average timed launch.
     roofline["traffic"] = EXTEND_DRAM_BYTES_PER_RAY * rays / max(1, ext_launch)
@@ -565,7 +573,8 @@ def run_ours(args, rank, world, local):
         line = {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": config_of(w), "mrays_per_s": mrays, "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
+                "config": config_of(w), "mrays_per_s": mrays, "roofline": roofline,
+                "device_ms_per_render": breakdown, "cpu_baseline": cb, "e2e": e2e,
                 "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s": wall,
                 "batched": batched, "served": served, "bdpt": bdpt, "cornell": cornell, "device_build": dev_build,
                 "scene": {"components": int(info.num_components), "wide_nodes": int(info.num_wide_nodes),

@@ -157,6 +157,8 @@ class RenderStats(C.Structure):
         ("device_ms", C.c_double),
         ("extend_ms", C.c_double),
         ("shade_ms", C.c_double),
+        ("raygen_ms", C.c_double),
+        ("film_ms", C.c_double),
     ]
 
 

@@ -521,6 +521,7 @@ static gr_status run_render(gr_scene* s, const gr_camera* c, const gr_render_par
     std::memcpy(&s->stats.prim_tests, cnt + CNT_PRIMS, 8);
     if (cnt[CNT_ERROR] == 2)
         return fail(GR_ERR_TIMEOUT, "traversal step budget exceeded (ray " + std::to_string(cnt[CNT_ERROR + 1]) + ")");
+    if (cnt[CNT_ERROR] == 3) return fail(GR_ERR_TIMEOUT, "film accumulation: a wait between pass chunks ran out");
     if (cnt[CNT_ERROR]) return fail(GR_ERR_STACK_OVERFLOW, "traversal stack bound exceeded");
     return p->integrator == GR_INTEGRATOR_BDPT ? bdpt_index_check() : pt_index_check();
 }

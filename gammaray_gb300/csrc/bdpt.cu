@@ -974,8 +974,10 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         GR_CUDA_TRY(cudaGetLastError());
         launches += 3;
         if (job.film) {
+            DevBuf& fs = device_work().film_sched;
+            GR_CUDA_TRY(fs.ensure(film_sched_words(job.width, job.height) * sizeof(uint32_t)));
             gr_status s3 = film_gather(ps.st.as<float2>(), ps.light.as<float4>(), job.width, job.height, g, job.film,
-                                       st);
+                                       st, fs.as<uint32_t>(), err);
             if (s3 != GR_OK) return s3;
             ++launches;
         }

@@ -159,7 +159,7 @@ struct RingSamples {
     }
 };
 
-__global__ void __launch_bounds__(FILM_THREADS, 3) k_eng_gather(const EngineCtl* c, const DevJob* __restrict__ jobs,
+__global__ void __launch_bounds__(FILM_THREADS, GR_FILM_BLOCKS_PER_SM) k_eng_gather(const EngineCtl* c, const DevJob* __restrict__ jobs,
                                                                     const DevUnit* __restrict__ units,
                                                                     const float4* __restrict__ s_hot,
                                                                     const uint4* __restrict__ s_cold, uint32_t mask) {

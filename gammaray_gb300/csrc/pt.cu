@@ -310,7 +310,7 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             for (cudaEvent_t e : v) cudaEventDestroy(e);
         }
     } free_tev{tev};
-    std::vector<std::pair<int, int>> ext_pairs, shade_pairs;
+    std::vector<std::pair<int, int>> ext_pairs, shade_pairs, raygen_pairs, film_pairs;
     auto mark = [&](int& idx) -> gr_status {
         cudaEvent_t e;
         GR_CUDA_TRY(cudaEventCreate(&e));
@@ -336,6 +336,8 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         uint32_t g = std::min(group, total - done);
         uint32_t n = g * npix;
         p.first_pass = rp.first_pass + done;
+        int r0 = -1, r1 = -1;
+        if (timed) GR_TRY_S(mark(r0));
         k_set_count<<<1, 1, 0, st>>>(cnt + CNT_QUEUE0, n);
         GR_CUDA_TRY(cudaGetLastError());
         uint32_t bound = n;  // an upper bound of the current queue length
@@ -345,6 +347,10 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         GR_CUDA_TRY(cudaGetLastError());
         ++launches;
         GR_TRY_S(sync_check(st, "raygen", 0, n));
+        if (timed) {
+            GR_TRY_S(mark(r1));
+            raygen_pairs.emplace_back(r0, r1);
+        }
         for (uint32_t depth = 0;; ++depth) {
             if (p.max_depth && depth >= p.max_depth) break;
             int cur = depth & 1, nxt = cur ^ 1;
@@ -395,10 +401,18 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             }
         }
         if (job.film) {
+            int f0 = -1, f1 = -1;
+            if (timed) GR_TRY_S(mark(f0));
+            DevBuf& fs = device_work().film_sched;
+            GR_CUDA_TRY(fs.ensure(film_sched_words(job.width, job.height) * sizeof(uint32_t)));
             gr_status s2 = film_gather(ps.st.as<float2>(), ps.light.as<float4>(), job.width, job.height, g, job.film,
-                                       st);
+                                       st, fs.as<uint32_t>(), err);
             if (s2 != GR_OK) return s2;
             ++launches;
+            if (timed) {
+                GR_TRY_S(mark(f1));
+                film_pairs.emplace_back(f0, f1);
+            }
         }
         if (job.samples_out) {
             k_samples_out<<<(n + 255) / 256, 256, 0, st>>>(n, ps.st.as<float2>(), ps.light.as<float4>(),
@@ -411,16 +425,18 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     sc->stats.kernel_launches += launches;
     if (timed) {
         GR_CUDA_TRY(cudaStreamSynchronize(st));
-        for (auto& pr : ext_pairs) {
-            float ms = 0.0f;
-            GR_CUDA_TRY(cudaEventElapsedTime(&ms, tev[pr.first], tev[pr.second]));
-            sc->stats.extend_ms += ms;
-        }
-        for (auto& pr : shade_pairs) {
-            float ms = 0.0f;
-            GR_CUDA_TRY(cudaEventElapsedTime(&ms, tev[pr.first], tev[pr.second]));
-            sc->stats.shade_ms += ms;
-        }
+        auto sum = [&](const std::vector<std::pair<int, int>>& pairs, double& out) -> gr_status {
+            for (auto& pr : pairs) {
+                float ms = 0.0f;
+                GR_CUDA_TRY(cudaEventElapsedTime(&ms, tev[pr.first], tev[pr.second]));
+                out += ms;
+            }
+            return GR_OK;
+        };
+        GR_TRY_S(sum(ext_pairs, sc->stats.extend_ms));
+        GR_TRY_S(sum(shade_pairs, sc->stats.shade_ms));
+        GR_TRY_S(sum(raygen_pairs, sc->stats.raygen_ms));
+        GR_TRY_S(sum(film_pairs, sc->stats.film_ms));
         sc->stats.extend_launches += ext_pairs.size();
     }
     return GR_OK;

@@ -112,6 +112,7 @@ struct DeviceWork {
     PathState paths;
     BdptState bdpt;
     BounceReadback readback;
+    DevBuf film_sched;  // film_gather's chunk counter and tile flags
 };
 DeviceWork& device_work();  // of the current device
 
@@ -198,8 +199,14 @@ void scene_release(gr_scene* s);
 
 gr_status pt_index_check();
 gr_status bdpt_index_check();
+// Adds `passes` passes of samples (pass k at k * width * height in st_buf and color) to
+// `film`, each pixel's sum in the reference's serial order.  With `sched` (device
+// scratch of film_sched_words(width, height) words) and `err` (the error word; 3 = a
+// wait between chunks ran out), many passes over a large image run as ordered chunks of
+// passes (film.cu); otherwise one block per tile.
 gr_status film_gather(const float2* st_buf, const float4* color, uint32_t width, uint32_t height, uint32_t passes,
-                      float4* film, cudaStream_t s);
+                      float4* film, cudaStream_t s, uint32_t* sched = nullptr, int* err = nullptr);
+size_t film_sched_words(uint32_t width, uint32_t height);
 // Resolve and EXR packing add splat * splat_scale when splat is not null.
 gr_status film_resolve(const float4* film, const float4* splat, float splat_scale, uint32_t n, float* rgb,
                        cudaStream_t s);

@@ -168,6 +168,8 @@ pub struct gr_render_stats {
     pub device_ms: f64,
     pub extend_ms: f64,
     pub shade_ms: f64,
+    pub raygen_ms: f64,
+    pub film_ms: f64,
 }
 
 #[repr(C)]

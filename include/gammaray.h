@@ -259,7 +259,8 @@ typedef struct gr_render_params {
  * (gr_render_stats.node_visits / prim_tests); slows the render slightly. */
 #define GR_RENDER_COUNT_TRAVERSAL 1u
 /* Time every extension (closest-hit) and shade launch with CUDA events on the render
- * stream (gr_render_stats.extend_ms / shade_ms). */
+ * stream (gr_render_stats.extend_ms / shade_ms), and for the path tracer its camera
+ * rays and film accumulation (raygen_ms / film_ms). */
 #define GR_RENDER_TIME_KERNELS 2u
 
 void gr_render_params_default(int32_t integrator, gr_render_params* out);
@@ -310,6 +311,8 @@ typedef struct gr_render_stats {
     double device_ms;         /* CUDA-event time of the render */
     double extend_ms;         /* with GR_RENDER_TIME_KERNELS: sum over extension launches */
     double shade_ms;          /* with GR_RENDER_TIME_KERNELS: sum over shade launches */
+    double raygen_ms;         /* with GR_RENDER_TIME_KERNELS (path tracer): camera-ray generation */
+    double film_ms;           /* with GR_RENDER_TIME_KERNELS (path tracer): film accumulation */
 } gr_render_stats;
 gr_status gr_scene_last_stats(const gr_scene* scene, gr_render_stats* out);
 

@@ -382,6 +382,32 @@ def test_pt_groups_do_not_change_the_film(gpu, monkeypatch):
     np.testing.assert_array_equal(films[0][1], films[1][1])
 
 
+@pytest.mark.parametrize("bdpt", [False, True])
+def test_chunked_film_gather_equals_pass_by_pass(gpu, monkeypatch, bdpt):
+    # A 768x512 image has 1,024 film tiles, more than the gather's resident blocks, so
+    # 16 passes in one group are added in ordered 8-pass chunks over all tiles; one pass
+    # per group adds each pass with one block per tile.  Both sum every pixel in pass
+    # order: the films are bit-identical.
+    width, height, spp = 768, 512, 16
+    w = scenes.displaced_sphere(width, height, spp, bdpt=bdpt)
+    st = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=9)
+    integ = g.BdptIntegrator(max_depth=6, mis=1) if bdpt else w.integrator
+    env = "GR_BDPT_PATHS_IN_FLIGHT" if bdpt else "GR_PATHS_IN_FLIGHT"
+    films = []
+    for paths in (None, str(width * height)):
+        if paths is None:
+            monkeypatch.delenv(env, raising=False)
+        else:
+            monkeypatch.setenv(env, paths)
+        st._pass = 0
+        f = g.Film(width, height, lib=gpu)
+        st.render(w.camera, integ, f, spp)
+        films.append(f.read())
+    assert films[0][1].min() > 0
+    np.testing.assert_array_equal(films[0][1], films[1][1])
+    np.testing.assert_array_equal(films[0][0], films[1][0])
+
+
 def test_sync_check_reports_a_slow_launch(gpu):
     # GR_SYNC_CHECK bounds every host wait of a render.  With a limit no launch can meet,
     # the render returns GR_ERR_TIMEOUT naming the kernel, the work in flight finishes
