@@ -76,14 +76,22 @@ struct PTParams {
 // (consecutive positions per warp), instead of gathering and scattering slot-indexed
 // arrays at random.  A finished path writes its radiance to its slot (the index of its
 // film position), which the film gather reads.
+//
+// The first queue (camera rays) holds only rays: its entry q is path q (slot q), whose
+// state is unit throughput, no radiance and the key of its pass and pixel, so shading
+// makes that state instead of reading it, and raygen writes 52 bytes per path less.
 GR_D uint64_t state_key(float4 b) {
     return (static_cast<uint64_t>(__float_as_uint(b.w)) << 32) | __float_as_uint(b.z);
 }
 
-__global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4* __restrict__ L,
-                                                  float2* __restrict__ st, uint32_t* __restrict__ q_slot,
-                                                  float4* __restrict__ q_o, float4* __restrict__ q_d,
-                                                  float4* __restrict__ q_state) {
+// The random key of path q of the group (pass first_pass + q / npix, pixel q % npix).
+GR_D uint64_t first_key(const PTParams& p, uint32_t q) {
+    const uint32_t pass_local = q / p.npix;
+    return path_key(p.seed, p.first_pass + pass_local, q - pass_local * p.npix);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float2* __restrict__ st,
+                                                  float4* __restrict__ q_o, float4* __restrict__ q_d) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t pass_local = i / p.npix;
@@ -95,14 +103,9 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float4
     film_sample_point(p.width, p.height, row, col, k, s, t);
     V3 o, d;
     camera_ray(p.cam, s, t, o, d);
-    L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     st[i] = make_float2(s, t);
-    q_slot[i] = i;
     q_o[i] = make_float4(o.x, o.y, o.z, 0.0f);
     q_d[i] = make_float4(d.x, d.y, d.z, 0.0f);
-    q_state[2 * static_cast<size_t>(i)] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    q_state[2 * static_cast<size_t>(i) + 1] = make_float4(0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(k)),
-                                                          __uint_as_float(static_cast<uint32_t>(k >> 32)));
 }
 
 // Appends this lane's surviving path (slot, ray, state) to the next queue with one atomic
@@ -131,7 +134,8 @@ GR_D void push_path(bool alive, uint32_t* count_out, uint32_t slot, V3 o, V3 d, 
 // Material-sorted shading (shade_sort.cuh): each block sorts its chunk of the queue by
 // code path (chosen lobe type, the material's lobe types), then shades it in that order.
 
-template <int NT>
+// FIRST: the queue of camera rays (no slots or states stored; see first_key).
+template <int NT, bool FIRST>
 __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams p, uint32_t depth,
                                                  const uint32_t* __restrict__ count_in,
                                                  const uint32_t* __restrict__ q_slot, const float4* __restrict__ q_o,
@@ -152,7 +156,8 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
         const uint32_t cn = min(chunk, n - c0);
         sort_chunk<NT, PER>(sm, cn, per, [&](uint32_t i) {
             uint32_t q = c0 + i;
-            return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(state_key(q_state[2 * q + 1]), base), 0);
+            const uint64_t key = FIRST ? first_key(p, q) : state_key(q_state[2 * q + 1]);
+            return shade_bucket(s, __float_as_int(q_hit[q].y), uniform01(key, base), 0);
         });
         // Every lane runs every step so that all of them reach the ballot in push_path.
         for (uint32_t e = 0; e < per; ++e) {
@@ -163,12 +168,20 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
             float4 sa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sb = sa;
             if (i < cn) {
                 uint32_t q = c0 + sm.order[i];
-                slot = q_slot[q];
                 float4 h = q_hit[q];
                 float4 o4 = q_o[q], d4 = q_d[q];
                 V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
-                sa = q_state[2 * static_cast<size_t>(q)];
-                sb = q_state[2 * static_cast<size_t>(q) + 1];
+                if (FIRST) {
+                    slot = q;
+                    const uint64_t k0 = first_key(p, q);
+                    sa = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+                    sb = make_float4(0.0f, 0.0f, __uint_as_float(static_cast<uint32_t>(k0)),
+                                     __uint_as_float(static_cast<uint32_t>(k0 >> 32)));
+                } else {
+                    slot = q_slot[q];
+                    sa = q_state[2 * static_cast<size_t>(q)];
+                    sb = q_state[2 * static_cast<size_t>(q) + 1];
+                }
                 V3 tp = V3{sa.x, sa.y, sa.z}, L = V3{sa.w, sb.x, sb.y};
                 int32_t k = __float_as_int(h.y);
                 if (k < 0) {
@@ -206,8 +219,8 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
     }
 }
 
+// DisplayColorIntegrator: one bounce, so the queue is the camera rays (entry q is path q).
 __global__ void __launch_bounds__(BLOCK) k_shade_display(DeviceScene s, const uint32_t* __restrict__ count_in,
-                                                         const uint32_t* __restrict__ q_slot,
                                                          const float4* __restrict__ q_hit, float4* __restrict__ L_buf) {
     const uint32_t n = *count_in;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
@@ -219,27 +232,29 @@ __global__ void __launch_bounds__(BLOCK) k_shade_display(DeviceScene s, const ui
             const DevMaterial& m = s.materials[__ldg(s.prim_material + prim)];
             c = make_float4(m.display[0], m.display[1], m.display[2], 0.0f);
         }
-        L_buf[q_slot[q]] = c;
+        L_buf[q] = c;
     }
 }
 
-template <int NT, class... A>
+template <int NT, bool FIRST, class... A>
 gr_status launch_shade_nt(uint32_t n_bound, cudaStream_t st, A... a) {
     const size_t smem = sort_smem_bytes(NT, shade_per<NT>());
-    GR_CUDA_TRY(allow_sort_smem(k_shade<NT>, smem));
+    GR_CUDA_TRY(allow_sort_smem(k_shade<NT, FIRST>, smem));
     // Every resident block; each picks its entries per thread from the queue length.
-    int grid = resident_grid(k_shade<NT>, smem, n_bound, NT);
-    k_shade<NT><<<grid, NT, smem, st>>>(a...);
+    int grid = resident_grid(k_shade<NT, FIRST>, smem, n_bound, NT);
+    k_shade<NT, FIRST><<<grid, NT, smem, st>>>(a...);
     return GR_OK;
 }
 
 // Shades a queue of at most n_bound entries (the device holds the exact length): in
 // SHADE_BIG-thread blocks while that fills two blocks per SM, else in 128-thread blocks.
+// `first`: the queue of camera rays (depth 0).
 template <class... A>
-gr_status launch_shade(uint32_t n_bound, cudaStream_t st, A... a) {
-    if (SHADE_BIG != 128 && n_bound >= 2u * static_cast<uint32_t>(device_sm_count()) * SHADE_BIG)
-        return launch_shade_nt<SHADE_BIG>(n_bound, st, a...);
-    return launch_shade_nt<128>(n_bound, st, a...);
+gr_status launch_shade(uint32_t n_bound, bool first, cudaStream_t st, A... a) {
+    const bool big = SHADE_BIG != 128 && n_bound >= 2u * static_cast<uint32_t>(device_sm_count()) * SHADE_BIG;
+    if (first) return big ? launch_shade_nt<SHADE_BIG, true>(n_bound, st, a...)
+                          : launch_shade_nt<128, true>(n_bound, st, a...);
+    return big ? launch_shade_nt<SHADE_BIG, false>(n_bound, st, a...) : launch_shade_nt<128, false>(n_bound, st, a...);
 }
 
 __global__ void k_samples_out(uint32_t n, const float2* __restrict__ st, const float4* __restrict__ L, float* out) {
@@ -341,9 +356,8 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         k_set_count<<<1, 1, 0, st>>>(cnt + CNT_QUEUE0, n);
         GR_CUDA_TRY(cudaGetLastError());
         uint32_t bound = n;  // an upper bound of the current queue length
-        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, ps.light.as<float4>(), ps.st.as<float2>(),
-                                                            ps.q_slot[0].as<uint32_t>(), ps.q_o[0].as<float4>(),
-                                                            ps.q_d[0].as<float4>(), ps.q_state[0].as<float4>());
+        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, ps.st.as<float2>(), ps.q_o[0].as<float4>(),
+                                                            ps.q_d[0].as<float4>());
         GR_CUDA_TRY(cudaGetLastError());
         ++launches;
         GR_TRY_S(sync_check(st, "raygen", 0, n));
@@ -369,15 +383,15 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             }
             if (display) {
                 int grid = resident_grid(k_shade_display, 0, n);
-                k_shade_display<<<grid, BLOCK, 0, st>>>(job.scene, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
-                                                        ps.q_hit.as<float4>(), ps.light.as<float4>());
+                k_shade_display<<<grid, BLOCK, 0, st>>>(job.scene, cnt + cur, ps.q_hit.as<float4>(),
+                                                        ps.light.as<float4>());
                 GR_CUDA_TRY(cudaGetLastError());
                 ++launches;
                 break;
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
             if (timed) GR_TRY_S(mark(e0));
-            GR_TRY_S(launch_shade(bound, st, job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
+            GR_TRY_S(launch_shade(bound, depth == 0, st, job.scene, p, depth, cnt + cur, ps.q_slot[cur].as<uint32_t>(),
                                   ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(),
                                   ps.q_state[cur].as<float4>(), ps.light.as<float4>(), cnt + nxt,
                                   ps.q_slot[nxt].as<uint32_t>(), ps.q_o[nxt].as<float4>(), ps.q_d[nxt].as<float4>(),
@@ -598,7 +612,7 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
         p.first_pass = rp->first_pass + pass;
         uint32_t n = npix;
         k_set_count<<<1, 1, 0, st>>>(cnt + CNT_QUEUE0, n);
-        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, light, stb, q_slot[0], q_o[0], q_d[0], q_state[0]);
+        k_raygen<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(p, n, stb, q_o[0], q_d[0]);
         GR_CUDA_TRY(cudaGetLastError());
         for (uint32_t depth = 0;; ++depth) {
             if (p.max_depth && depth >= p.max_depth) break;
@@ -608,12 +622,12 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
             GR_CUDA_TRY(cudaGetLastError());
             if (display) {
                 int grid = resident_grid(k_shade_display, 0, n);
-                k_shade_display<<<grid, BLOCK, 0, st>>>(sc->dev, cnt + cur, q_slot[cur], q_hit, light);
+                k_shade_display<<<grid, BLOCK, 0, st>>>(sc->dev, cnt + cur, q_hit, light);
                 GR_CUDA_TRY(cudaGetLastError());
                 break;
             }
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));
-            GR_TRY_S(launch_shade(n, st, sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit,
+            GR_TRY_S(launch_shade(n, depth == 0, st, sc->dev, p, depth, cnt + cur, q_slot[cur], q_o[cur], q_d[cur], q_hit,
                                   q_state[cur], light, cnt + nxt, q_slot[nxt], q_o[nxt], q_d[nxt], q_state[nxt]));
             GR_CUDA_TRY(cudaGetLastError());
             if (p.max_depth == 0 && (depth & 3) == 3) {
