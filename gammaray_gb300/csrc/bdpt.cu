@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(BLOCK) k_bdpt_raygen(DeviceScene s, BdptParams
 #endif
 constexpr int BSBLOCK = GR_BDPT_SHADE_BLOCK;
 static_assert(BSBLOCK == 128 || BSBLOCK == 768, "BDPT shading block of 128 or 768 threads");
-constexpr uint32_t BSHADE_PER_THREAD = BSBLOCK == 128 ? SHADE_PER_THREAD : 85u;
+constexpr uint32_t BSHADE_PER_THREAD = BSBLOCK == 128 ? SHADE_PER_THREAD : SHADE_BIG_PER;
 
 __global__ void __launch_bounds__(BSBLOCK, 768 / BSBLOCK) k_bdpt_shade(DeviceScene s, BdptParams p, Verts vs,
                                                       const uint32_t* __restrict__ count_in,

@@ -21,7 +21,7 @@ constexpr int EBLOCK = 128;
 #endif
 constexpr int ESBLOCK = GR_ENG_SHADE_BLOCK;
 static_assert(ESBLOCK == 128 || ESBLOCK == 768, "engine shading block of 128 or 768 threads");
-constexpr uint32_t ESHADE_PER_THREAD = ESBLOCK == 128 ? SHADE_PER_THREAD : 85u;
+constexpr uint32_t ESHADE_PER_THREAD = ESBLOCK == 128 ? SHADE_PER_THREAD : SHADE_BIG_PER;
 constexpr int GATHER_BLOCKS = 512;
 
 // Path state.  The queue entry of a live path carries its ray, its job (o.w), its depth

@@ -53,11 +53,10 @@ __global__ void k_set_count(uint32_t* c, uint32_t n) { *c = n; }
 #endif
 constexpr int SHADE_BIG = GR_SHADE_BLOCK;
 static_assert(SHADE_BIG == 128 || SHADE_BIG == 384 || SHADE_BIG == 768, "shading block of 128, 384 or 768 threads");
-// Entries per thread per chunk: 64 at 128 threads; larger blocks as many as fit the
-// 16-bit chunk positions and the shared memory of their blocks per SM.
+// Entries per thread per chunk: 64 at 128 threads, SHADE_BIG_PER at 768 (shade_sort.cuh).
 template <int NT>
 constexpr uint32_t shade_per() {
-    return NT == 128 ? SHADE_PER_THREAD : (NT == 384 ? 96u : 85u);
+    return NT == 128 ? SHADE_PER_THREAD : (NT == 384 ? 96u : SHADE_BIG_PER);
 }
 
 struct PTParams {

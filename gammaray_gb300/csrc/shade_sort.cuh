@@ -22,6 +22,17 @@ constexpr uint32_t SORT_BUCKETS = 32;
 #define GR_SHADE_PER_THREAD 64
 #endif
 constexpr uint32_t SHADE_PER_THREAD = GR_SHADE_PER_THREAD;
+// Entries per thread per chunk of the 768-thread shading blocks (one per SM): 85 at most
+// (768 x 85 chunk positions fit 16 bits).  A block sorts its whole chunk (reading every
+// entry's hit and key) before it shades it; at 85 per thread the chunks of all SMs (about
+// 476 MB of those lines) overflow L2 between the two reads.  On the path-tracer workload
+// (102,422 triangles, 1024 x 1024, 64 spp) 16 / 24 / 32 / 40 / 64 / 85 measured shading
+// 9.39 (with an L2 prefetch) / 9.08 / 9.10 / 9.43 / 9.69 / 10.32 ms per render.
+#ifndef GR_SHADE_BIG_PER
+#define GR_SHADE_BIG_PER 32
+#endif
+constexpr uint32_t SHADE_BIG_PER = GR_SHADE_BIG_PER;
+static_assert(SHADE_BIG_PER >= 1 && SHADE_BIG_PER <= 85, "768 x per chunk positions fit 16 bits");
 
 // Rays per thread per chunk when the extension kernels trace their queue grouped by
 // direction (octant and dominant axis; 0: no sort).  Measured on the path-tracer
