@@ -22,7 +22,6 @@ constexpr int EBLOCK = 128;
 constexpr int ESBLOCK = GR_ENG_SHADE_BLOCK;
 static_assert(ESBLOCK == 128 || ESBLOCK == 768, "engine shading block of 128 or 768 threads");
 constexpr uint32_t ESHADE_PER_THREAD = ESBLOCK == 128 ? SHADE_PER_THREAD : SHADE_BIG_PER;
-constexpr int GATHER_BLOCKS = 512;
 
 // Path state.  The queue entry of a live path carries its ray, its job (o.w), its depth
 // (d.w) and its state, two float4:
@@ -142,6 +141,7 @@ __global__ void k_eng_plan(EngineCtl* c, const DevJob* __restrict__ jobs, const 
     c->done = c->g_lo == c->units_count ? 1u : 0u;
     c->iter += 1;
     c->fetch = 0;  // the extension kernel of this iteration starts handing out rays at 0
+    c->gather_next = 0;  // and the gather its film-tile items
 }
 
 // A unit's samples in their ring slots.
@@ -159,13 +159,20 @@ struct RingSamples {
     }
 };
 
-__global__ void __launch_bounds__(FILM_THREADS, GR_FILM_BLOCKS_PER_SM) k_eng_gather(const EngineCtl* c, const DevJob* __restrict__ jobs,
-                                                                    const DevUnit* __restrict__ units,
-                                                                    const float4* __restrict__ s_hot,
-                                                                    const uint4* __restrict__ s_cold, uint32_t mask) {
+__global__ void __launch_bounds__(FILM_THREADS, GR_FILM_BLOCKS_PER_SM)
+    k_eng_gather(EngineCtl* c, const DevJob* __restrict__ jobs, const DevUnit* __restrict__ units,
+                 const float4* __restrict__ s_hot, const uint4* __restrict__ s_cold, uint32_t mask) {
     __shared__ StagedSample sm;
+    __shared__ uint32_t s_item;
     const uint32_t total = c->gather_tiles, groups = c->gather_groups;
-    for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
+    // Items (a job's film tile and its finished passes) are taken from a counter: their
+    // pass counts differ, so a fixed stride would leave blocks idle.
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&c->gather_next, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        __syncthreads();  // every thread has read s_item before it is taken again
+        if (item >= total) break;
         uint32_t g = 0;
         while (g + 1 < groups && c->gather_group_tiles[g + 1] <= item) ++g;
         const uint32_t t = item - c->gather_group_tiles[g];
@@ -500,7 +507,8 @@ gr_status Engine::enqueue_iteration(int cur) {
     const int nxt = cur ^ 1;
     k_eng_plan<<<1, 1, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(), unit_done_.as<uint32_t>(), C, ring_, cur);
     GR_CUDA_TRY(cudaGetLastError());
-    k_eng_gather<<<GATHER_BLOCKS, FILM_THREADS, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(),
+    const int ggrid = grid_for(reinterpret_cast<const void*>(k_eng_gather), FILM_THREADS, 0, 1u << 30);
+    k_eng_gather<<<ggrid, FILM_THREADS, 0, st_>>>(c, jobs_.as<DevJob>(), units_.as<DevUnit>(),
                                                                    s_hot_.as<float4>(), s_cold_.as<uint4>(), ring_ - 1);
     GR_CUDA_TRY(cudaGetLastError());
     int fgrid = grid_for(reinterpret_cast<const void*>(k_eng_fill), EBLOCK, 0, C);

@@ -64,6 +64,7 @@ struct EngineCtl {
     int32_t err;
     uint32_t iter;
     uint32_t fetch;  // rays handed out by the refilling extension kernel this iteration
+    uint32_t gather_next;  // film-tile items handed out by the gather this iteration
     // Set by the host (0 = none): gather as soon as every unit below this one has
     // finished, without waiting for a larger batch, so the request those units complete
     // is done within one iteration.
