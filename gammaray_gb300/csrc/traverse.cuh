@@ -76,6 +76,16 @@ GR_D int32_t select_child(const float (&f)[8 * W], uint32_t slot) {
 
 template <int N>
 GR_D void sort_keys(uint32_t (&k)[N]) {
+    if (N == 4) {  // the 5-comparator network for 4 keys
+        const int pairs[5][2] = {{0, 1}, {2, 3}, {0, 2}, {1, 3}, {1, 2}};
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            uint32_t a = k[pairs[c][0]], b = k[pairs[c][1]];
+            k[pairs[c][0]] = min(a, b);
+            k[pairs[c][1]] = max(a, b);
+        }
+        return;
+    }
     // Odd-even transposition network, fully unrolled (N <= 8).
 #pragma unroll
     for (int pass = 0; pass < N; ++pass) {
@@ -150,28 +160,22 @@ GR_D void trav_init(TravState& t, V3 o, V3 d, float t_max) {
     t.sp = 0;
 }
 
+// Stack entries are (child reference, entry distance bits) pairs, one 64-bit access each.
 struct StackView {
-    int32_t* sref;  // this thread's shared column (stride = blockDim.x)
-    float* st;
+    int2* s;      // this thread's shared column (stride = blockDim.x entries)
     int stride;
-    int2* spill;    // local overflow, MAX_STACK - SMEM_STACK entries
+    int2* spill;  // local overflow, MAX_STACK - SMEM_STACK entries
     GR_D void push(int sp, int32_t ref, float te) const {
-        if (sp < SMEM_STACK) {
-            sref[sp * stride] = ref;
-            st[sp * stride] = te;
-        } else {
-            spill[sp - SMEM_STACK] = make_int2(ref, __float_as_int(te));
-        }
+        const int2 e = make_int2(ref, __float_as_int(te));
+        if (sp < SMEM_STACK) s[sp * stride] = e;
+        else spill[sp - SMEM_STACK] = e;
     }
     GR_D void pop(int sp, int32_t& ref, float& te) const {
-        if (sp < SMEM_STACK) {
-            ref = sref[sp * stride];
-            te = st[sp * stride];
-        } else {
-            int2 e = spill[sp - SMEM_STACK];
-            ref = e.x;
-            te = __int_as_float(e.y);
-        }
+        int2 e;
+        if (sp < SMEM_STACK) e = s[sp * stride];  // shared and local loads kept apart
+        else e = spill[sp - SMEM_STACK];
+        ref = e.x;
+        te = __int_as_float(e.y);
     }
 };
 
@@ -328,9 +332,7 @@ inline size_t step_stack_smem_bytes(int threads) {
 // memory starting at `smem`, step_stack_smem_bytes(blockDim.x) bytes) and its local
 // spill array.
 GR_D StackView thread_stack(unsigned char* smem, int2* spill) {
-    int32_t* sref = reinterpret_cast<int32_t*>(smem);
-    float* st = reinterpret_cast<float*>(smem + sizeof(int32_t) * SMEM_STACK * blockDim.x);
-    return StackView{sref + threadIdx.x, st + threadIdx.x, static_cast<int>(blockDim.x), spill};
+    return StackView{reinterpret_cast<int2*>(smem) + threadIdx.x, static_cast<int>(blockDim.x), spill};
 }
 
 // Traces one ray to the end.  ANY_HIT: stops at the first hit closer than t_max (shadow
