@@ -67,6 +67,11 @@ GR_D float intersect_prim(const float4 p0, const float4 p1, const float4 p2, V3 
 // child[slot] without dynamic register indexing (keeps the node in registers).
 template <int W>
 GR_D int32_t select_child(const float (&f)[8 * W], uint32_t slot) {
+    if (W == 4) {  // by the slot's two bits: three selects
+        const float lo = (slot & 1u) ? f[6 * W + 1] : f[6 * W];
+        const float hi = (slot & 1u) ? f[6 * W + 3] : f[6 * W + 2];
+        return __float_as_int((slot & 2u) ? hi : lo);
+    }
     int32_t r = 0;
 #pragma unroll
     for (int j = 0; j < W; ++j)
@@ -242,8 +247,11 @@ GR_D bool visit_node(const S& s, TravState& t, const StackView& stk, int* err, u
         }
         float tmin = fmaxf(fmaxf(t0x, t0y), t0z);
         float tmax = fminf(fminf(t1x, t1y), t1z) * inflate;
-        bool hit = tmin <= tmax && tmin < t.closest && tmax > 0.0f;
+        // The slab test (tmin <= tmax, tmax > 0, tmin < closest) on te = max(tmin, 0):
+        // the same result (closest > 0), except that a box whose far distance is exactly
+        // 0 counts as hit, which can only add a node to visit.
         float te = fmaxf(tmin, 0.0f);
+        bool hit = te <= tmax && te < t.closest;
         key[j] = hit ? ((__float_as_uint(te) & ~7u) | static_cast<uint32_t>(j)) : 0xFFFFFFFFu;
         h += hit ? 1 : 0;
     }
