@@ -75,6 +75,32 @@ GR_HD bool nearly_zero(float x) { return fabsf(x) < EPS; }
 GR_HD bool nearly_zero(V3 a) { return nearly_zero(dot(a, a)); }
 GR_HD bool is_positive(float x) { return x > EPS; }
 GR_HD float lerp(float x, float y, float a) { return x + a * (y - x); }
+
+// Division of 32-bit unsigned integers by a divisor fixed for a launch (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994): with
+// l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1, floor(n / d) is
+// (t + ((n - t) >> 1)) >> (l - 1) for t = mulhi(m, n), exact for every n and 1 <= d < 2^31.
+struct FastDiv {
+    uint32_t d = 1, m = 0, l = 0;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    if (d > 1) {
+        uint32_t l = 0;
+        while ((1ull << l) < d) ++l;
+        f.l = l;
+        f.m = static_cast<uint32_t>(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    }
+    return f;
+}
+#ifdef __CUDACC__
+GR_D uint32_t fast_div(uint32_t n, const FastDiv& f) {
+    if (f.d == 1) return n;
+    const uint32_t t = __umulhi(f.m, n);
+    return (t + ((n - t) >> 1)) >> (f.l - 1);
+}
+#endif
 GR_HD V3 vlerp(V3 a, V3 b, float t) { return V3{lerp(a.x, b.x, t), lerp(a.y, b.y, t), lerp(a.z, b.z, t)}; }
 GR_HD float clampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }  // NaN passes through
 GR_HD float clamp_unit(float x) { return clampf(x, 0.0f, 1.0f); }

@@ -62,6 +62,7 @@ constexpr uint32_t shade_per() {
 struct PTParams {
     DevCamera cam;
     uint32_t width, height, npix;
+    FastDiv by_npix, by_width;  // divisions by npix and width
     uint32_t first_pass;
     uint64_t seed;
     uint32_t max_depth, rr_depth, rr_aggr;
@@ -85,7 +86,7 @@ GR_D uint64_t state_key(float4 b) {
 
 // The random key of path q of the group (pass first_pass + q / npix, pixel q % npix).
 GR_D uint64_t first_key(const PTParams& p, uint32_t q) {
-    const uint32_t pass_local = q / p.npix;
+    const uint32_t pass_local = fast_div(q, p.by_npix);
     return path_key(p.seed, p.first_pass + pass_local, q - pass_local * p.npix);
 }
 
@@ -93,9 +94,9 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float2
                                                   float4* __restrict__ q_o, float4* __restrict__ q_d) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t pass_local = i / p.npix;
+    uint32_t pass_local = fast_div(i, p.by_npix);
     uint32_t pixel = i - pass_local * p.npix;
-    uint32_t row = pixel / p.width;
+    uint32_t row = fast_div(pixel, p.by_width);
     uint32_t col = pixel - row * p.width;
     uint64_t k = path_key(p.seed, p.first_pass + pass_local, pixel);
     float s, t;
@@ -337,8 +338,10 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
     PTParams p;
     p.cam = job.camera;
     p.width = job.width;
+    p.by_width = make_fastdiv(job.width);
     p.height = job.height;
     p.npix = npix;
+    p.by_npix = make_fastdiv(npix);
     p.qcap = static_cast<uint32_t>(static_cast<size_t>(group) * npix);
     p.seed = rp.seed;
     p.max_depth = display ? 1 : rp.max_depth;
@@ -598,8 +601,10 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
     PTParams p;
     p.cam = make_camera(*camera);
     p.width = width;
+    p.by_width = make_fastdiv(width);
     p.height = height;
     p.npix = npix;
+    p.by_npix = make_fastdiv(npix);
     p.qcap = npix;
     p.seed = rp->seed;
     p.max_depth = display ? 1 : rp->max_depth;
