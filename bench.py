@@ -538,7 +538,9 @@ def run_ours(args, rank, world, local):
         fd.close()
 
     # Roofline of the dominant kernel (extension / closest hit): counted bytes per ray.
-    node_bytes = 32 * info.bvh_width
+    # A node is 32W bytes; at widths 4 and 8 the kernel reads its 7 rows of W floats
+    # (bounds and children), not the padding row.
+    node_bytes = 28 * info.bvh_width if info.bvh_width % 4 == 0 else 32 * info.bvh_width
     b_ray = nodes_per_ray * node_bytes + prims_per_ray * 48 + 48
     achieved = b_ray * rays / (ext_ms * 1e-3) / 1e9 if ext_ms > 0 else None
     peak, peak_kind = hbm_peak()
