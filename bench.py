@@ -34,7 +34,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 # workload (bench.py --profile-case --spp 4; its 4 M-ray queues exceed L2 as the timed
 # renders' do), divided by that render's extension rays.  Re-measured whenever the
 # extension kernel changes; EXTEND_DRAM_CAPTURE says which capture the figure comes from.
-EXTEND_DRAM_BYTES_PER_RAY = 46.6
+EXTEND_DRAM_BYTES_PER_RAY = 46.5
 EXTEND_DRAM_CAPTURE = "ncu, 4-spp render of the bench workload, all 12 k_extend_refill launches"
 sys.path.insert(0, ROOT)
 
