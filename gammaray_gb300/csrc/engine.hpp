@@ -2,12 +2,14 @@
 //
 // Many renders ("jobs": a scene, a camera, settings and a film) share one wavefront.
 // Each job's work is a list of units, one per pass; units are issued in a global order
-// (round-robin over jobs, pass by pass), and global path p keeps its state in slot
-// p mod ring of a ring of path records.  Every iteration:
+// (round-robin over jobs, pass by pass).  A live path's state travels with its ray in
+// the queue; global path p has slot p mod ring of a ring holding its film position and,
+// once it finishes, its radiance.  Every iteration:
 //   plan    (1 thread) picks the finished units to gather (consecutive from the oldest)
 //           and how many new paths to issue (queue room, ring slots already gathered)
 //   gather  splats the picked units into their films from their ring slots (the
-//           deterministic tile gather); each film tile adds its job's units in pass order
+//           deterministic tile gather); each film tile adds its job's units in pass
+//           order, every resident block taking (tile, units) items from a counter
 //   fill    starts the next paths in their slots (jitter, camera ray) and queues them
 //   extend  closest hit for the queued rays of all jobs
 //   shade   path-tracer shading per job, material-sorted; finished paths leave their
