@@ -72,7 +72,8 @@ struct DevBuf {
 struct PathState {
     DevBuf light, st;  // per slot: final radiance, film (s, t)
     // Ping-pong queues of live paths: slot, ray, and state (throughput, radiance so far,
-    // random key: two float4 per entry); one hit per entry.
+    // random key: two float4 per entry); one hit per entry.  The first queue of a group
+    // (camera rays) holds rays only: entry q is path q, whose state shading makes.
     DevBuf q_slot[2], q_o[2], q_d[2], q_state[2], q_hit;
     size_t capacity = 0;
     cudaError_t ensure(size_t n);
