@@ -94,13 +94,18 @@ inline FastDiv make_fastdiv(uint32_t d) {
     }
     return f;
 }
-#ifdef __CUDACC__
-GR_D uint32_t fast_div(uint32_t n, const FastDiv& f) {
+GR_HD uint32_t mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return static_cast<uint32_t>((static_cast<uint64_t>(a) * b) >> 32);
+#endif
+}
+GR_HD uint32_t fast_div(uint32_t n, const FastDiv& f) {
     if (f.d == 1) return n;
-    const uint32_t t = __umulhi(f.m, n);
+    const uint32_t t = mulhi32(f.m, n);
     return (t + ((n - t) >> 1)) >> (f.l - 1);
 }
-#endif
 GR_HD V3 vlerp(V3 a, V3 b, float t) { return V3{lerp(a.x, b.x, t), lerp(a.y, b.y, t), lerp(a.z, b.z, t)}; }
 GR_HD float clampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }  // NaN passes through
 GR_HD float clamp_unit(float x) { return clampf(x, 0.0f, 1.0f); }
