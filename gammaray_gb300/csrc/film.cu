@@ -1,5 +1,7 @@
 // Film accumulation (the deterministic tile gather of film_gather.cuh, pass after pass),
 // resolve and EXR packing.
+#include <cstdlib>
+
 #include "film_gather.cuh"
 #include "runtime.hpp"
 
@@ -12,7 +14,13 @@ constexpr uint32_t FILM_CHUNK_PASSES = 8;
 // Polls an item makes for its tile's previous chunk (an L2 atomic and a 0.1 us sleep
 // each): about 2 s.
 constexpr uint32_t FILM_WAIT_LIMIT = 1u << 21;
+// GR_FILM_WAIT_TEST=1 (tests only): the chunked gather starts its item counter past the
+// first chunk, whose items then never run, so every later item's wait runs out (after
+// FILM_WAIT_TEST_LIMIT polls) and the render reports it.  No fault, and every wait ends.
+constexpr uint32_t FILM_WAIT_TEST_LIMIT = 1u << 12;
 constexpr int FILM_ERR_WAIT = 3;  // error word: a wait ran out
+
+__global__ void k_film_set_word(uint32_t* w, uint32_t v) { *w = v; }
 
 // One block per tile, all passes.
 __global__ void __launch_bounds__(FILM_THREADS, GR_FILM_BLOCKS_PER_SM) k_film_gather(const float2* __restrict__ st,
@@ -40,7 +48,8 @@ __global__ void __launch_bounds__(FILM_THREADS, GR_FILM_BLOCKS_PER_SM) k_film_ga
 // wait is still bounded; one that runs out sets *err and skips its item.
 __global__ void __launch_bounds__(FILM_THREADS, GR_FILM_BLOCKS_PER_SM)
     k_film_gather_chunked(const float2* __restrict__ st, const float4* __restrict__ color, uint32_t width,
-                          uint32_t height, uint32_t passes, float4* film, uint32_t* sched, int* err) {
+                          uint32_t height, uint32_t passes, float4* film, uint32_t* sched, int* err,
+                          uint32_t wait_limit) {
     __shared__ StagedSample sm;
     __shared__ uint32_t s_item;
     __shared__ int s_skip;
@@ -56,7 +65,7 @@ __global__ void __launch_bounds__(FILM_THREADS, GR_FILM_BLOCKS_PER_SM)
                 const uint32_t c = item / ntiles, tile = item - c * ntiles;
                 uint32_t polls = 0;
                 while (atomicAdd(flags + tile, 0u) < c) {
-                    if (++polls > FILM_WAIT_LIMIT) {
+                    if (++polls > wait_limit) {
                         atomicExch(err, FILM_ERR_WAIT);
                         skip = 1;
                         break;
@@ -166,9 +175,14 @@ gr_status film_gather(const float2* st, const float4* color, uint32_t width, uin
     // image's chunks would only wait on one another.
     if (sched && err && passes > FILM_CHUNK_PASSES && ntiles >= slots) {
         GR_CUDA_TRY(cudaMemsetAsync(sched, 0, film_sched_words(width, height) * sizeof(uint32_t), s));
+        const char* wt = std::getenv("GR_FILM_WAIT_TEST");
+        const bool wait_test = wt && std::atoi(wt) > 0;
+        if (wait_test) k_film_set_word<<<1, 1, 0, s>>>(sched, ntiles);
         const uint32_t items = ntiles * ((passes + FILM_CHUNK_PASSES - 1) / FILM_CHUNK_PASSES);
         k_film_gather_chunked<<<std::min(items, slots), FILM_THREADS, 0, s>>>(st, color, width, height, passes, film,
-                                                                              sched, err);
+                                                                              sched, err,
+                                                                              wait_test ? FILM_WAIT_TEST_LIMIT
+                                                                                        : FILM_WAIT_LIMIT);
     } else {
         dim3 grid(film_tiles_x(width), film_tiles_y(height));
         k_film_gather<<<grid, FILM_THREADS, 0, s>>>(st, color, width, height, passes, film);

@@ -408,6 +408,34 @@ def test_chunked_film_gather_equals_pass_by_pass(gpu, monkeypatch, bdpt):
     np.testing.assert_array_equal(films[0][0], films[1][0])
 
 
+def test_film_chunk_wait_runs_out_and_is_reported(gpu, monkeypatch):
+    # A chunk of the film gather waits (bounded) for its tile's previous chunk.  With
+    # GR_FILM_WAIT_TEST set, the first chunk's items never run, so no flag is ever set and
+    # every later item's wait runs out (no fault): the render returns GR_ERR_TIMEOUT, and
+    # the next render on the same scene works and gives the film it should.
+    width, height, spp = 768, 512, 16
+    w = scenes.displaced_sphere(width, height, spp)
+    st = g.Stage(w.prims, lib=gpu, environment=w.environment, seed=9)
+    monkeypatch.setenv("GR_FILM_WAIT_TEST", "1")
+    f = g.Film(width, height, lib=gpu)
+    with pytest.raises(_abi.GrError) as e:
+        st.render(w.camera, w.integrator, f, spp)
+    assert e.value.status == 5 and "wait between pass chunks" in str(e.value)
+    monkeypatch.delenv("GR_FILM_WAIT_TEST")
+    films = []
+    for paths in (None, str(width * height)):  # chunked, then one pass per group
+        if paths is None:
+            monkeypatch.delenv("GR_PATHS_IN_FLIGHT", raising=False)
+        else:
+            monkeypatch.setenv("GR_PATHS_IN_FLIGHT", paths)
+        st._pass = 0
+        f = g.Film(width, height, lib=gpu)
+        st.render(w.camera, w.integrator, f, spp)
+        films.append(f.read())
+    np.testing.assert_array_equal(films[0][1], films[1][1])
+    np.testing.assert_array_equal(films[0][0], films[1][0])
+
+
 def test_sync_check_reports_a_slow_launch(gpu):
     # GR_SYNC_CHECK bounds every host wait of a render.  With a limit no launch can meet,
     # the render returns GR_ERR_TIMEOUT naming the kernel, the work in flight finishes
