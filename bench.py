@@ -31,9 +31,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 # DRAM bytes (read + written) per extension ray of k_extend_refill: ncu's
 # dram__bytes_read.sum + dram__bytes_write.sum summed over every k_extend_refill launch of
-# a 4-spp render of this
-# workload (bench.py --profile-case --spp 4; its 4 M-ray queues exceed L2 as the timed
-# renders' do), divided by that render's extension rays.  Re-measured whenever the
+# a 4-spp render of this workload (bench.py --profile-case --spp 4; its 4 M-ray queues
+# exceed L2 as the timed renders' do), divided by that render's extension rays.  Re-measured whenever the
 # extension kernel changes; EXTEND_DRAM_CAPTURE says which capture the figure comes from.
 EXTEND_DRAM_BYTES_PER_RAY = 46.5
 EXTEND_DRAM_CAPTURE = "ncu, 4-spp render of the bench workload, all 12 k_extend_refill launches"
