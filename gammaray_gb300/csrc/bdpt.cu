@@ -918,7 +918,7 @@ gr_status render_bdpt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
         for (uint32_t depth = 0; depth < max_len; ++depth) {
             int cur = depth & 1, nxt = cur ^ 1;
             gr_status s1 = extend_any(job.scene, false, p.nslots, cnt + cur, ps.q_o[cur].as<float4>(),
-                                      ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(), err, rays, cnt + CNT_FETCH, st);
+                                      ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(), err, rays, cnt + CNT_FETCH, st, false);
             if (s1 != GR_OK) return s1;
             GR_CUDA_TRY(cudaGetLastError());
             GR_CUDA_TRY(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), st));

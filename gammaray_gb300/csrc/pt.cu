@@ -80,7 +80,8 @@ struct PTParams {
 //
 // The first queue (camera rays) holds only rays: its entry q is path q (slot q), whose
 // state is unit throughput, no radiance and the key of its pass and pixel, so shading
-// makes that state instead of reading it, and raygen writes 52 bytes per path less.
+// makes that state instead of reading it; and their one origin (the pinhole's) is stored
+// once, in q_o[0].  Raygen writes 24 bytes per path.
 GR_D uint64_t state_key(float4 b) {
     return (static_cast<uint64_t>(__float_as_uint(b.w)) << 32) | __float_as_uint(b.z);
 }
@@ -105,7 +106,7 @@ __global__ void __launch_bounds__(BLOCK) k_raygen(PTParams p, uint32_t n, float2
     V3 o, d;
     camera_ray(p.cam, s, t, o, d);
     st[i] = make_float2(s, t);
-    q_o[i] = make_float4(o.x, o.y, o.z, 0.0f);
+    if (i == 0) q_o[0] = make_float4(o.x, o.y, o.z, 0.0f);  // the pinhole origin, the same for every ray
     q_d[i] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_shade(DeviceScene s, PTParams 
             if (i < cn) {
                 uint32_t q = c0 + sm.order[i];
                 float4 h = q_hit[q];
-                float4 o4 = q_o[q], d4 = q_d[q];
+                float4 o4 = q_o[FIRST ? 0u : q], d4 = q_d[q];  // camera rays share q_o[0]
                 V3 o = V3{o4.x, o4.y, o4.z}, d = V3{d4.x, d4.y, d4.z};
                 if (FIRST) {
                     slot = q;
@@ -375,7 +376,7 @@ gr_status render_pt(gr_scene* sc, const RenderJob& job, cudaStream_t st) {
             if (timed) GR_TRY_S(mark(e0));
             gr_status s1 = extend_any(job.scene, (rp.flags & GR_RENDER_COUNT_TRAVERSAL) != 0, n, cnt + cur,
                                       ps.q_o[cur].as<float4>(), ps.q_d[cur].as<float4>(), ps.q_hit.as<float4>(), err,
-                                      rays, cnt + CNT_FETCH, st);
+                                      rays, cnt + CNT_FETCH, st, depth == 0);
             if (s1 != GR_OK) return s1;
             GR_CUDA_TRY(cudaGetLastError());
             ++launches;
@@ -623,7 +624,7 @@ extern "C" gr_status gr_render_static(gr_scene* sc, const gr_camera* camera, con
             if (p.max_depth && depth >= p.max_depth) break;
             int cur = depth & 1, nxt = cur ^ 1;
             GR_TRY_S(extend_any(sc->dev, false, n, cnt + cur, q_o[cur], q_d[cur], q_hit, err, rays, cnt + CNT_FETCH,
-                                st));
+                                st, depth == 0));
             GR_CUDA_TRY(cudaGetLastError());
             if (display) {
                 int grid = resident_grid(k_shade_display, 0, n);

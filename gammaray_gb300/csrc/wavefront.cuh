@@ -37,11 +37,13 @@ constexpr int BLOCK = 128;
 #define GR_EXTEND_BOUNDS __launch_bounds__(BLOCK)
 #endif
 
+// one_origin: every ray of the queue starts at q_o[0] (the path tracer's camera rays:
+// one pinhole origin, stored once).
 template <int W, bool COUNT>
 __global__ void GR_EXTEND_BOUNDS k_extend(DeviceScene s, const uint32_t* __restrict__ count,
                                                      const float4* __restrict__ q_o, const float4* __restrict__ q_d,
                                                      float4* __restrict__ q_hit, int* err,
-                                                     unsigned long long* rays) {
+                                                     unsigned long long* rays, bool one_origin) {
     extern __shared__ unsigned char smem[];
     int2 spill[MAX_STACK - SMEM_STACK];
     const StackView stk = thread_stack(smem, spill);
@@ -49,7 +51,7 @@ __global__ void GR_EXTEND_BOUNDS k_extend(DeviceScene s, const uint32_t* __restr
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
     uint32_t counts[2] = {0, 0};
     auto trace = [&](uint32_t q) {
-        float4 o4 = q_o[q], d4 = q_d[q];
+        float4 o4 = q_o[one_origin ? 0 : q], d4 = q_d[q];
         TraceResult r = trace_ray<W, false, COUNT>(s, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX, stk, err,
                                                    err + 1, q, counts);
         q_hit[q] = make_float4(r.t, __int_as_float(r.k), r.u, r.v);
@@ -98,7 +100,7 @@ template <int W, bool COUNT>
 __global__ void GR_EXTEND_BOUNDS k_extend_refill(DeviceScene s, const uint32_t* __restrict__ count,
                                                  const float4* __restrict__ q_o, const float4* __restrict__ q_d,
                                                  float4* __restrict__ q_hit, int* err, unsigned long long* rays,
-                                                 uint32_t* fetch) {
+                                                 uint32_t* fetch, bool one_origin) {
     extern __shared__ unsigned char smem[];
     int2 spill[MAX_STACK - SMEM_STACK];
     const StackView stk = thread_stack(smem, spill);
@@ -121,7 +123,7 @@ __global__ void GR_EXTEND_BOUNDS k_extend_refill(DeviceScene s, const uint32_t* 
             if (!busy) {
                 const uint32_t mine = base + __popc(idle & below);
                 if (mine < n) {
-                    float4 o4 = q_o[mine], d4 = q_d[mine];
+                    float4 o4 = q_o[one_origin ? 0u : mine], d4 = q_d[mine];
                     trav_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX);
                     q = mine;
                     steps = 0;
@@ -190,34 +192,36 @@ int resident_grid(K kernel, size_t smem, uint32_t n, int block = BLOCK) {
 template <int W, bool COUNT>
 gr_status extend_launch(const DeviceScene& s, uint32_t cap_n, const uint32_t* count, const float4* qo,
                         const float4* qd, float4* qh, int* err, unsigned long long* rays, uint32_t* fetch,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool one_origin) {
     if (GR_EXTEND_REFILL > 0) {
         size_t smem = step_stack_smem_bytes(BLOCK);
         GR_CUDA_TRY(cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st));
         int grid = resident_grid(k_extend_refill<W, COUNT>, smem, cap_n);
-        k_extend_refill<W, COUNT><<<grid, BLOCK, smem, st>>>(s, count, qo, qd, qh, err, rays, fetch);
+        k_extend_refill<W, COUNT><<<grid, BLOCK, smem, st>>>(s, count, qo, qd, qh, err, rays, fetch, one_origin);
         return GR_OK;
     }
     size_t smem = step_stack_smem_bytes(BLOCK) + (GR_EXTEND_SORT ? sort_smem_bytes(BLOCK, GR_EXTEND_SORT) : 0);
     int grid = resident_grid(k_extend<W, COUNT>, smem, cap_n);
-    k_extend<W, COUNT><<<grid, BLOCK, smem, st>>>(s, count, qo, qd, qh, err, rays);
+    k_extend<W, COUNT><<<grid, BLOCK, smem, st>>>(s, count, qo, qd, qh, err, rays, one_origin);
     return GR_OK;
 }
 
+// one_origin: every ray of the queue starts at qo[0] (see k_extend).
 gr_status extend_any(const DeviceScene& s, bool count_traversal, uint32_t cap_n, const uint32_t* count,
                      const float4* qo, const float4* qd, float4* qh, int* err, unsigned long long* rays,
-                     uint32_t* fetch, cudaStream_t st) {
+                     uint32_t* fetch, cudaStream_t st, bool one_origin) {
+    const bool o1 = one_origin;
     if (count_traversal) {
         switch (s.width) {
-            case 2: return extend_launch<2, true>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st);
-            case 4: return extend_launch<4, true>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st);
-            default: return extend_launch<8, true>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st);
+            case 2: return extend_launch<2, true>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st, o1);
+            case 4: return extend_launch<4, true>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st, o1);
+            default: return extend_launch<8, true>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st, o1);
         }
     }
     switch (s.width) {
-        case 2: return extend_launch<2, false>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st);
-        case 4: return extend_launch<4, false>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st);
-        default: return extend_launch<8, false>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st);
+        case 2: return extend_launch<2, false>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st, o1);
+        case 4: return extend_launch<4, false>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st, o1);
+        default: return extend_launch<8, false>(s, cap_n, count, qo, qd, qh, err, rays, fetch, st, o1);
     }
 }
 
